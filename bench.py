@@ -1,0 +1,383 @@
+"""Benchmark: ms per FLD linear solve (SOLVE_WITH_SOR's system) to relative
+residual 1e-10 on one GB300, through libttfld's C ABI.
+
+Workload (shell256): the 100 x 256 x 128 (r x phi x theta) synthetic shell
+(3,276,800 cells, dt = 100 s, seed 1) after the set-up BOUNDS/KAPPA and one
+implicit step; a "step" is one solve of that step's SOLVE_WITH_SOR system
+from delta_ER = 0 (ppsor.f:29).  The product path is the FP32 red-black
+sweeps inside FP64 defect correction; the plain FP64 red-black SOR (exact
+reference rounding, and Jacobi-scaled with FMA) are timed in the same run.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun with N > 1 every rank solves its own replica (the path does
+not shard across GPUs here), value = max-over-ranks time / (K * N).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per FLD solve to rel. residual 1e-10: learned+FP32/FP64 vs plain FP64 SOR"
+SHELL = "shell256"
+WORKLOAD = ("shell256: 100x256x128 (r x phi x theta) synthetic spherical shell, 3276800 cells, "
+            "dt=100 s, seed 1; one SOLVE_WITH_SOR system of its implicit step, solved from zero "
+            "to ||b-Ax||_1/||b||_1 <= 1e-10")
+# Algorithmic bytes per cell update of one sweep (both colours):
+#   FP32 scaled sweep: 6 coefficients + rhat + e read + e write  = 9 x 4 B
+#   FP64 exact sweep : 7 coefficients + b + x read + x write      = 10 x 8 B
+BYTES_FP32_SWEEP = 36
+BYTES_FP64_SWEEP = 80
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "sweep32_shell256_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("bytes_per_launch")
+    return None
+
+
+def build_system(device):
+    """One implicit step of the shell on the device; its last SOLVE_WITH_SOR
+    system stays in SOR_A..G / RHS_ER."""
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import shell
+    sh = shell(SHELL, seed=1)
+    sh.params["epsmat"] = 1e-10
+    sh.params["itmax"] = 200000
+    f = start_run(sh, device=device)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)
+    return sh, f
+
+
+def flush_l2(torch, buf):
+    buf.add_(1.0)  # 256 MB written: larger than the 126 MB L2
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from ttcode_gb300 import _ffi
+    L = _ffi.lib()
+    sh, f = build_system(local)
+    nx, ny, nz = sh.dims
+    ncells = nx * ny * nz
+    stream = torch.cuda.ExternalStream(f.stream_ptr(), device=torch.device("cuda", local))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    # reference-accuracy solution: exact FP64 SOR (the reference loop, bitwise)
+    # converged to 1e-12 on the same system
+    f.set_params(epsmat=1e-12)
+    f.set_solver("sor64_exact")
+    st_ref = f.solve_system()
+    x_ref = f.download("DELTA_ER")
+    f.set_params(epsmat=1e-10)
+
+    def solve_timed(solver, guess="zero"):
+        f.set_solver(solver, guess=guess, tol=1e-10, inner_min=16, inner_max=512)
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = f.solve_system()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), st
+
+    # warm-up
+    for _ in range(args.warmup):
+        solve_timed("mixed")
+    # timed region: K product-path solves
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.ttfld_kernel_launches()
+    times, stats = [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            ms, st = solve_timed("mixed")
+            times.append(ms)
+            stats.append(st)
+    torch.cuda.synchronize()
+    launches = int(L.ttfld_kernel_launches() - launches0)
+    if ws > 1:
+        torch.distributed.barrier()
+    x_mixed = f.download("DELTA_ER")
+    total_ms = float(sum(times))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_solve = total_ms / args.steps / ws
+    r_l1, b_l1 = f.true_residual()
+    err = float(np.linalg.norm((x_mixed - x_ref).ravel()) / np.linalg.norm(x_ref.ravel()))
+
+    # the plain FP64 red-black SOR on the same GPU (same stopping rule as the
+    # reference, in-sweep L1 ratio <= 1e-10)
+    plain = {}
+    for solver in ("sor64_exact", "sor64_fast"):
+        ms_list, st = [], None
+        for _ in range(2):
+            ms, st = solve_timed(solver)
+            ms_list.append(ms)
+        xs = f.download("DELTA_ER")
+        plain[solver] = {"ms": min(ms_list), "sweeps": st.sor_iter,
+                         "err_vs_fp64_1e-12": float(np.linalg.norm((xs - x_ref).ravel()) / np.linalg.norm(x_ref.ravel()))}
+
+    # roofline of the dominant kernel: FP32 sweep, timed live on the library stream
+    f.set_solver("mixed")
+    ms_sweep32 = f.time_sweeps("mixed", 50)
+    ms_sweep64 = f.time_sweeps("sor64_exact", 20)
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES_FP32_SWEEP * ncells / (ms_sweep32 * 1e-3) / 1e9   # GB/s per full sweep (2 launches)
+    traffic = load_traffic()
+
+    # e2e: the reference-facing SOLVE_WITH_SOR call with host (pinned) buffers:
+    # upload the EVAL arrays, RHS_ER and UPPERBND, fill + solve, download DELTA_ER
+    names = ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8", "EVAL_1_6", "RHS_ER")
+    host = {}
+    for n in names:
+        a = f.download(n)
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = a.ravel(order="F")
+        host[n] = t
+    ub = f.download("UPPERBND")
+    out = torch.empty(f.download("DELTA_ER").size, dtype=torch.float64, pin_memory=True)
+    h2d = sum(host[n].numel() * 8 for n in names) + ub.size * 4
+    d2h = out.numel() * 8
+    f.set_solver("mixed", tol=1e-10, inner_min=16, inner_max=512)
+    e2e = []
+    for it in range(args.warmup + args.steps):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for n in names:
+            _ffi.check(n, L.ttfld_upload(f.h, _ffi.FIELDS[n], host[n].data_ptr()))
+        _ffi.check("ub", L.ttfld_upload(f.h, _ffi.FIELDS["UPPERBND"], ub.ctypes.data))
+        st = _ffi.SolveStats()
+        import ctypes
+        _ffi.check("solve", L.ttfld_solve_with_sor(f.h, 1, ctypes.byref(st)), ok=(0, 1, 2))
+        _ffi.check("dl", L.ttfld_download(f.h, _ffi.FIELDS["DELTA_ER"], out.data_ptr()))
+        t1 = time.perf_counter()
+        if it >= args.warmup:
+            e2e.append((t1 - t0) * 1e3)
+    e2e_ms = float(sum(e2e) / len(e2e))
+
+    line = {
+        "metric": METRIC, "value": ms_per_solve, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 sweeps / fp64 residual",
+        "data": "synthetic (seeded analytic shell, no dataset)",
+        "config": {"workload": WORKLOAD, "cells": ncells, "solver": "mixed FP32/FP64 defect correction",
+                   "guess": "zero", "tol": 1e-10, "omega": sh.params["sorparam"],
+                   "l2": "flushed between timed solves (256 MB write)", "parallelism": "replicas"},
+        "sweeps_per_solve": stats[-1].sor_iter, "corrections_per_solve": stats[-1].corrections,
+        "true_rel_residual": r_l1 / b_l1,
+        "err_vs_fp64_1e-12": err, "fp64_1e-12_sweeps": st_ref.sor_iter,
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64_exact": plain["sor64_exact"]["ms"] / ms_per_solve,
+        "speedup_vs_plain_fp64_fast": plain["sor64_fast"]["ms"] / ms_per_solve,
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "call": "ttfld_upload x11 + ttfld_solve_with_sor + ttfld_download (pinned host)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "sweep32_kernel (both colours)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * ncells, "ms_per_sweep": ms_sweep32,
+                     "traffic": traffic},
+        "fp64_sweep": {"ms_per_sweep": ms_sweep64,
+                       "achieved_gbs": BYTES_FP64_SWEEP * ncells / (ms_sweep64 * 1e-3) / 1e9},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(f, sh, st_ref_sweeps=plain["sor64_exact"]["sweeps"])
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    f.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def oracle_system(sh, f=None):
+    """The same system in the CPU oracle: from the device context when given,
+    else assembled by the oracle itself (one COUPLED_ENERGY_EQS step)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as ormod
+    from ttcode_gb300.grid import full_1d
+    ormod.build()
+    o = ormod.Oracle(*sh.dims)
+    for n in sh.grid.m:
+        a = full_1d(sh.grid, n)
+        o.f(n)[:a.size] = a
+    for n, a in sh.fields.items():
+        o.f(n)[...] = a
+    for k, v in sh.params.items():
+        if k != "kappa_model":
+            o.set(k, v)
+    o.set("epsmat", 1e-10)
+    o.set("itmax", 200000)
+    assembly_ms = None
+    if f is not None:
+        for n in ("SOR_A", "SOR_B", "SOR_C", "SOR_D", "SOR_E", "SOR_F", "SOR_G", "RHS_ER"):
+            o.f(n)[...] = f.download(n)
+    else:
+        o.set("iii", 0)
+        o.call("bounds")
+        o.call("kappa")
+        o.set("iii", 1)
+        t0 = time.perf_counter()
+        o.call("coupled_energy_eqs", 1)
+        assembly_ms = (time.perf_counter() - t0) * 1e3
+    return o, assembly_ms
+
+
+def time_oracle_sweeps(o, target_s=10.0):
+    o.f("DELTA_ER")[...] = 0.0
+    t0 = time.perf_counter()
+    o.call("sor_sweeps", 5)
+    per = (time.perf_counter() - t0) / 5
+    n = max(5, int(target_s / max(per, 1e-6)))
+    o.f("DELTA_ER")[...] = 0.0
+    t0 = time.perf_counter()
+    o.call("sor_sweeps", n)
+    return (time.perf_counter() - t0) / n * 1e3, n
+
+
+def cpu_baseline(f, sh, st_ref_sweeps):
+    o, _ = oracle_system(sh, f)
+    ms_sweep, n = time_oracle_sweeps(o, 10.0)
+    return {"value": ms_sweep * st_ref_sweeps, "unit": "ms", "cores": 1, "kind": "port",
+            "sample": f"{n} FP64 red-black sweeps of the same 100x256x128 system by the C oracle "
+                      f"(gcc -O2, 1 core), {ms_sweep:.3f} ms/sweep x {st_ref_sweeps} sweeps per solve"}
+
+
+def run_reference(args):
+    """The reference's CPU path (the C restatement of ppsor.f, one core, as
+    the reference runs one serial rank per core): each step times a bounded
+    sample of red-black sweeps of the shell256 system and scales it by the
+    sweep count of a full solve to 1e-10."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from ttcode_gb300.synthetic import shell
+    sh = shell(SHELL, seed=1)
+    o, asm_ms = oracle_system(sh, None)         # one full step: assembly + solve
+    sweeps = int(o.get("sor_total"))
+    vals = []
+    for it in range(args.warmup + args.steps):
+        ms_sweep, n = time_oracle_sweeps(o, 4.0)
+        if it >= args.warmup:
+            vals.append(ms_sweep * sweeps)
+    v = float(sum(vals) / len(vals))
+    line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded analytic shell, no dataset)",
+            "config": {"workload": WORKLOAD, "cells": int(np.prod(sh.dims)), "solver": "FP64 red-black SOR",
+                       "guess": "zero", "tol": 1e-10, "omega": sh.params["sorparam"]},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": f"per step: ~4 s of FP64 red-black sweeps by the C oracle scaled by "
+                                       f"{sweeps} sweeps per solve; one step (assembly+solve) took {asm_ms:.0f} ms"},
+            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,265 @@
+/*
+ * ttfld.h -- C ABI of libttfld, the GB300 (sm_103a) implementation of
+ * ttcode's implicit flux-limited-diffusion radiation/gas energy step.
+ *
+ * The library holds the reference's module arrays on the device for the
+ * whole run; the host copies fields in and out only where the Fortran side
+ * reads or writes them.  One context = one device, one stream, one host
+ * thread (the reference is one serial MPI rank per core; the calls are not
+ * re-entrant).  Every entry point returns an int status:
+ *     0   success
+ *     1   an iteration limit (ITMAX) was reached; the reference prints and
+ *         continues (ppsor.f:161-174, ppenergy.f:750-775), so do the callers
+ *     2   the learned initial guess was rejected and the zero guess used
+ *    <0   error (see TTFLD_E_*); the reference's CLEAN_STOP cases map here
+ *
+ * Arrays cross the boundary in the reference's own Fortran layout
+ * (column-major, i = radius fastest) with the reference's bounds:
+ *     halo  (-1:NX+2,-1:NY+2,-1:NZ+2)  T RH CV ER ER_OLD DELTA_ER XKAP* KMUL ...
+ *     cell  (1:NX,1:NY,1:NZ)           EVAL1..8 EVAL_1_6 JACOB_ETA RHS_ER SOR_A..G
+ *     facex (1:NX+1,1:NY,1:NZ)         FLIMX DIFRX FLUX_X
+ *     facey (1:NX,1:NY+1,1:NZ)         FLIMY DIFRY FLUX_Y
+ *     facez (1:NX,1:NY,1:NZ+1)         FLIMZ DIFRZ FLUX_Z
+ *     plane (-1:NY+2,-1:NZ+2)          UPPERBND (int32) MU_STAR TINCIDENT
+ *     sinp  (1:NX,-1:NY+2,-1:NZ+2)     STELLARINPUT
+ *     stau  (1:NX+1,-1:NY+2,-1:NZ+2)   STELLARTAU DTAUS
+ * i.e. exactly what a Fortran caller passes with arr(lbound(arr,1),...).
+ */
+#ifndef TTFLD_H
+#define TTFLD_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TTFLD_ABI_VERSION 1
+
+enum ttfld_status {
+  TTFLD_OK = 0,
+  TTFLD_MAXITER = 1,
+  TTFLD_FALLBACK = 2,
+  TTFLD_E_ARGS = -1,        /* bad argument / unknown field id            */
+  TTFLD_E_CUDA = -2,        /* CUDA runtime error                         */
+  TTFLD_E_UNSUPPORTED = -3, /* configuration outside the implemented set  */
+  TTFLD_E_NONPOSITIVE_Q = -7, /* Q+conv*dQ <= 0, ppenergy.f:411-521       */
+  TTFLD_E_NONFINITE = -8,   /* NaN/Inf found in a solver norm             */
+  TTFLD_E_NOMODEL = -9      /* learned guess requested without a model    */
+};
+
+/* Fields addressable through ttfld_upload / ttfld_download. */
+enum ttfld_field {
+  /* halo (-1:NX+2,-1:NY+2,-1:NZ+2) */
+  TTFLD_T = 0, TTFLD_RH, TTFLD_CV, TTFLD_ER, TTFLD_ER_OLD, TTFLD_DELTA_ER,
+  TTFLD_XKAPR, TTFLD_XKAPP, TTFLD_XKAPA, TTFLD_DXKAPP_DT, TTFLD_DXKAPA_DT,
+  TTFLD_KMUL, TTFLD_Q, TTFLD_SCALAR,
+  /* cell (1:NX,1:NY,1:NZ) */
+  TTFLD_EVAL1 = 32, TTFLD_EVAL2, TTFLD_EVAL3, TTFLD_EVAL4, TTFLD_EVAL5,
+  TTFLD_EVAL6, TTFLD_EVAL7, TTFLD_EVAL8, TTFLD_EVAL_1_6, TTFLD_JACOB_ETA,
+  TTFLD_RHS_ER, TTFLD_SOR_A, TTFLD_SOR_B, TTFLD_SOR_C, TTFLD_SOR_D,
+  TTFLD_SOR_E, TTFLD_SOR_F, TTFLD_SOR_G, TTFLD_FQ, TTFLD_FR, TTFLD_DIVF,
+  TTFLD_DELTA_Q,
+  /* faces */
+  TTFLD_FLIMX = 64, TTFLD_FLIMY, TTFLD_FLIMZ, TTFLD_DIFRX, TTFLD_DIFRY,
+  TTFLD_DIFRZ, TTFLD_FLUX_X, TTFLD_FLUX_Y, TTFLD_FLUX_Z,
+  /* planes (-1:NY+2,-1:NZ+2) */
+  TTFLD_UPPERBND = 96, /* int32 */
+  TTFLD_MU_STAR, TTFLD_TINCIDENT,
+  /* stellar heating arrays */
+  TTFLD_STELLARINPUT = 112, TTFLD_STELLARTAU, TTFLD_DTAUS
+};
+
+/* Grid sizes of the one subdomain (the reference's locNX/locNY/locNZ). */
+typedef struct {
+  int32_t nx, ny, nz;
+  int32_t poles;  /* inc_poles (ipp:20); only 0 is implemented */
+} ttfld_dims;
+
+/* 1-D metric arrays of GITTER (ppinit.f:1028-1406), each passed with the
+ * reference's bounds: xxa(0:NX+2) xxb(-1:NX+2) dxa(1:NX+2) dxb(0:NX+2),
+ * the same pattern for y and z, ddx0/ddx1 (0:NX+2) ..., surxa/surxb,
+ * surza/surzb, geoxga/geoxha, geozga (0:N+2), geoxg/geoxh, geozg (-1:N+2). */
+typedef struct {
+  const double *xxa, *xxb, *dxa, *dxb;
+  const double *xya, *xyb, *dya, *dyb;
+  const double *xza, *xzb, *dza, *dzb;
+  const double *ddx0, *ddx1, *ddy0, *ddy1, *ddz0, *ddz1;
+  const double *surxa, *surxb, *surza, *surzb;
+  const double *geoxg, *geoxh, *geoxga, *geoxha, *geozg, *geozga;
+} ttfld_metrics;
+
+/* The input_init switches and constants the step reads (ppmod.f:2-33) plus
+ * the opacity model. */
+typedef struct {
+  double delt;      /* DELT                                               */
+  double sorparam;  /* SORPARAM (omega), ipp:13                           */
+  double epsmat;    /* EPSMAT, ipp:13                                     */
+  double fbottom;   /* Fbottom, ipp:12                                    */
+  double tirr;      /* TIRR, ipp:22                                       */
+  double xnue;      /* XNUE, ipp:8 (ieta=5 floor and DIFFUSION)           */
+  double pr_num;    /* PR_NUM, ipp:8                                      */
+  double kap0;      /* synthetic opacity scale, kappa_R = kap0*sqrt(rho)*(T/1000)^1.5*KMUL */
+  int32_t itmax;    /* ITMAX (shared by SOR and the outer loop), ipp:13   */
+  int32_t bcxmin;   /* BCXMIN, ipp:12 (9 implemented)                     */
+  int32_t ibdrad;   /* IBDRAD, ipp:12 (4, 7, 9 implemented)               */
+  int32_t iflimtyp; /* IFLIMTYP, ipp:12 (1, 2)                            */
+  int32_t f_incident; /* F_INCIDENT, ipp:12 (0..5)                        */
+  int32_t ieta;     /* IETA, ipp:8                                        */
+  int32_t isigtyp;  /* ISIGTYP, ipp:10 (0, 1)                             */
+  int32_t iii;      /* the driver's step counter III                      */
+  int32_t adjust_sor; /* call ADJUST_SOR_PARAM where the reference would  */
+  int32_t kappa_model; /* 0 = synthetic analytic (stand-in for the tables) */
+                       /* 1 = prescribed: XKAP* are uploaded, KAPPA no-op  */
+} ttfld_params;
+
+/* How SOLVE_WITH_SOR's linear system is solved on the device. */
+enum ttfld_solver {
+  TTFLD_SOLVER_SOR64_EXACT = 0, /* red-black SOR in FP64, same rounding as the
+                                   reference loop (bitwise per sweep)      */
+  TTFLD_SOLVER_SOR64_FAST = 1,  /* red-black SOR in FP64 on Jacobi-scaled
+                                   coefficients with FMA (same iteration,
+                                   different rounding)                     */
+  TTFLD_SOLVER_MIXED = 2        /* FP32 red-black sweeps inside FP64 defect
+                                   correction, stopped on the true FP64
+                                   residual ||b-Ax||_1/||b||_1            */
+};
+
+enum ttfld_guess {
+  TTFLD_GUESS_ZERO = 0,     /* delta_ER = 0 (ppsor.f:29)                   */
+  TTFLD_GUESS_PREVIOUS = 1, /* (1-conv_parm) * previous outer solution      */
+  TTFLD_GUESS_LEARNED = 2   /* 3-D conv net prediction, zero-guess fallback  */
+};
+
+typedef struct {
+  int32_t solver;      /* enum ttfld_solver                                */
+  int32_t guess;       /* enum ttfld_guess                                 */
+  double tol;          /* mixed solver: stop at ||b-Ax||_1/||b||_1 <= tol  */
+  int32_t inner_min;   /* mixed solver: FP32 sweeps per correction, bounds */
+  int32_t inner_max;
+  int32_t max_sweeps;  /* mixed solver sweep budget (0 = 100*ITMAX)        */
+  int32_t reserved;
+} ttfld_solve_opts;
+
+typedef struct {
+  int32_t sor_iter;        /* sweeps of the last solve (SOR_ITER)          */
+  int32_t corrections;     /* FP64 defect-correction passes (mixed)        */
+  int32_t fallback;        /* 1 if the learned guess was rejected          */
+  int32_t status;
+  double rnorm;            /* global_RNORM of the last sweep               */
+  double rhsnorm;          /* global_RHSNORM                               */
+  double true_resid_l1;    /* ||b - A x||_1 at exit (mixed solver)         */
+  double guess_resid_l1;   /* ||b - A x0||_1 of the initial guess          */
+  double solve_ms;         /* device time of the solve (CUDA events on the
+                              library's stream, guess included)           */
+} ttfld_solve_stats;
+
+typedef struct {
+  int32_t energy_iter;     /* outer Newton iterations (energy_ITER)        */
+  int32_t sor_total;       /* sweeps summed over the step's solves         */
+  int32_t solves;          /* linear solves in the step                    */
+  int32_t fallbacks;       /* learned-guess rejections                     */
+  int32_t status;
+  int32_t reserved;
+  double global_deltaq;    /* max |dQ/Q| of the last outer iteration       */
+  double global_deltaer;   /* max |dER/ER| of the last outer iteration     */
+  double solve_ms;         /* device time in the linear solves             */
+  double step_ms;          /* device time of the whole step                */
+} ttfld_step_stats;
+
+typedef struct ttfld_ctx ttfld_ctx;
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- lifetime (replaces the allocate* routines of ppmod.f for the
+ *      arrays the step touches, and MPI_INIT's one-rank decomposition) ---- */
+int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims,
+                 const ttfld_metrics* metrics, const ttfld_params* params,
+                 int device);
+int ttfld_destroy(ttfld_ctx* ctx);
+int ttfld_set_params(ttfld_ctx* ctx, const ttfld_params* params);
+int ttfld_get_params(const ttfld_ctx* ctx, ttfld_params* params);
+int ttfld_set_solver(ttfld_ctx* ctx, const ttfld_solve_opts* opts);
+const char* ttfld_status_string(int status);
+int ttfld_abi_version(void);
+
+/* ---- field transfer (module array <-> device) ------------------------- */
+int ttfld_upload(ttfld_ctx* ctx, int field, const void* host);
+int ttfld_download(ttfld_ctx* ctx, int field, void* host);
+/* Element count of a field in its reference bounds (0 if unknown). */
+size_t ttfld_field_size(const ttfld_ctx* ctx, int field);
+/* Device pointer of a field (for callers that keep data on the GPU). */
+void* ttfld_device_ptr(ttfld_ctx* ctx, int field);
+/* Device copies inside the context: dst <- src (same storage class). */
+int ttfld_copy_field(ttfld_ctx* ctx, int dst_field, int src_field);
+int ttfld_synchronize(ttfld_ctx* ctx);
+/* The cudaStream_t every call of this context is issued on (for callers
+ * that order their own work or CUDA events against the library's). */
+void* ttfld_stream(ttfld_ctx* ctx);
+
+/* ---- the reference subroutines, device-resident ------------------------ */
+/* BOUNDS, ppbou.f:1-92 (MODTYP=2) restricted to T, RH and UPPERBND. */
+int ttfld_bounds(ttfld_ctx* ctx);
+/* KAPPA, pprphy.f:1-360 (synthetic analytic opacity with the IKAPTYP
+ * 20:25 extents, pprphy.f:321-351) and SUBSIG, pprphy.f:567-583. */
+int ttfld_kappa(ttfld_ctx* ctx);
+/* CALCMUSTAR ppsub.f:156-179 and CALC_TINCIDENT pprad.f:296-405 are
+ * evaluated by the caller and uploaded as MU_STAR / TINCIDENT. */
+/* STELLARINPUT_HEATING, pprad.f:408-516 (grey branch, :490-502). */
+int ttfld_stellarinput_heating(ttfld_ctx* ctx);
+/* DIFF, pprad.f:74-156, including FLIM pprphy.f:362-565; energy_iter <= 1
+ * also re-evaluates KAPPA, SUBSIG and QDENS (pprphy.f:396-402). */
+int ttfld_diff(ttfld_ctx* ctx, int energy_iter);
+/* CALCULATEFLUX + FLUX_BC, ppenergy.f:880-982. */
+int ttfld_calculateflux(ttfld_ctx* ctx, int energy_iter);
+/* FILL_EVALUES(theta_param), ppenergy.f:984-1030. */
+int ttfld_fill_evalues(ttfld_ctx* ctx, double theta);
+/* FILL_SOR_MATRIX + B_VECTOR_BOUNDARIES, ppsor.f:189-329. */
+int ttfld_fill_sor_matrix(ttfld_ctx* ctx);
+/* SOLVE_WITH_SOR(print_max_values), ppsor.f:2-187: fills the matrix from the
+ * device EVAL arrays and RHS_ER, solves for DELTA_ER with the configured
+ * solver and guess.  stats may be NULL. */
+int ttfld_solve_with_sor(ttfld_ctx* ctx, int print_max_values,
+                         ttfld_solve_stats* stats);
+/* As above on SOR_A..G / RHS_ER already on the device (no refill). */
+int ttfld_solve_system(ttfld_ctx* ctx, ttfld_solve_stats* stats);
+/* Exactly n red-black sweeps on the current system from the current
+ * DELTA_ER, FP64, reference rounding (for sweep-by-sweep parity tests). */
+int ttfld_sor_sweeps(ttfld_ctx* ctx, int n, double* rnorm, double* rhsnorm);
+/* ||b - A x||_1 (FP64) of the current system with x = DELTA_ER. */
+int ttfld_true_residual(ttfld_ctx* ctx, double* l1, double* rhs_l1);
+/* ADJUST_SOR_PARAM, ppsor.f:332-354 (50 solves, omega = 1.01 + 0.02 n). */
+int ttfld_adjust_sor_param(ttfld_ctx* ctx, double* sorparam);
+/* COUPLED_ENERGY_EQS, ppenergy.f:2-791 (IRAD=3).  do_bounds=1 runs the
+ * device BOUNDS first, as ppenergy.f:63 does; a Fortran caller that keeps
+ * BOUNDS on the host passes 0 after uploading T, RH and UPPERBND. */
+int ttfld_coupled_energy_eqs(ttfld_ctx* ctx, int do_bounds,
+                             ttfld_step_stats* stats);
+/* DIFFUSION(scalar), ppdif.f:1-167, on the SCALAR field (the pass_sc
+ * module array) with diffusion constant xnue/pr_num. */
+int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
+
+/* ---- measurement (no reference counterpart) --------------------------- */
+/* Runs n back-to-back sweeps of a solver's sweep kernels on the current
+ * system (TTFLD_SOLVER_SOR64_EXACT: DELTA_ER is iterated in place;
+ * SOR64_FAST / MIXED: only their private iterate is touched) and returns
+ * the mean device time of one full sweep (both colours), CUDA events on the
+ * library's stream. */
+int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
+/* Number of kernels this process has launched through libttfld. */
+uint64_t ttfld_kernel_launches(void);
+
+/* ---- learned initial guess (no reference counterpart) ----------------- */
+/* Load / export the conv-net weights (flat BF16 blob, see ttfld_unet.h). */
+int ttfld_guess_load(ttfld_ctx* ctx, const void* blob, size_t bytes);
+int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TTFLD_H */

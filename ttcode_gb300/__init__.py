@@ -1,0 +1,10 @@
+"""GB300 (sm_103a) implementation of ttcode's implicit flux-limited-diffusion
+radiation/gas energy step (COUPLED_ENERGY_EQS + SOLVE_WITH_SOR) behind a C ABI.
+
+The compute lives in ``_lib/libttfld.so`` (CUDA, built by ``build.py``); this
+package holds the host-side mirror of the reference interface (``fld``), the
+grid metrics (``grid``) and the seeded synthetic shells (``synthetic``).
+"""
+from .grid import Grid, gitter  # noqa: F401
+
+__all__ = ["Grid", "gitter"]

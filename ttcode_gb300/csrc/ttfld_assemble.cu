@@ -1,0 +1,457 @@
+// ttfld_assemble.cu -- FP64 coefficient assembly of the implicit FLD step:
+// KAPPA/SUBSIG/QDENS, FLIM, DIFF, CALCULATEFLUX, FLUX_BC, FILL_EVALUES,
+// CALCULATEDIVF_WITHF, the grey stellar heating, BOUNDS for the planet set-up
+// and the one-rank PLANETSHIFT.  Each kernel body is one reference loop nest
+// (cited), launched over the same index box, with the same operand order.
+#include "ttfld_internal.cuh"
+
+namespace ttfld {
+
+// ---- PLANETSHIFT ppshift.f:1009-1214, one rank --------------------------
+// Only the "from lower" (:1096-1107) and "from upper" (:1164-1173) copies
+// act with one rank; z and corner partners are MPI_PROC_NULL.
+int halo_shift(ttfld_ctx* c, double* a) {
+  Dev d = c->d;
+  launch_box(c->stream, box(-1, d.nx + 2, 0, 0, 1, d.nz), [=] __device__(int i, int, int k) {
+    a[hidx(d, i, 0, k)] = a[hidx(d, i, d.ny, k)];
+    a[hidx(d, i, -1, k)] = a[hidx(d, i, d.ny - 1, k)];
+    a[hidx(d, i, d.ny + 1, k)] = a[hidx(d, i, 1, k)];
+    a[hidx(d, i, d.ny + 2, k)] = a[hidx(d, i, 2, k)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// Synthetic analytic opacity in KAPPA's IKAPTYP 20:25 branch
+// (pprphy.f:321-351): evaluated for i = -1..UPPERBND, then i = UPPERBND..NX+2
+// copied from UPPERBND-1.  kappa_P = kappa_A = kappa_R, zero T-derivatives
+// (the IKAPTYP=3 convention, pprphy.f:84-87).
+__device__ __forceinline__ double kap_formula(const Dev& d, double t, double rh, double kmul) {
+  double th = t / 1000.0;
+  return ((d.kap0 * sqrt(rh)) * (th * sqrt(th))) * kmul;
+}
+
+static int kappa(ttfld_ctx* c) {
+  Dev d = c->d;
+  if (d.kappa_model == 1) return 0;  // prescribed opacities: KAPPA is the caller's
+  launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
+    int ub = PA(UB, j, k);
+    if (ub < 1 || ub > d.nx + 1) return;
+    for (int i = -1; i <= ub; ++i) {
+      size_t q = hidx(d, i, j, k);
+      double kr = kap_formula(d, d.T[q], d.RH[q], d.KMUL[q]);
+      d.XKAPR[q] = kr; d.XKAPP[q] = kr; d.XKAPA[q] = kr;
+      d.DXKAPP[q] = 0.0; d.DXKAPA[q] = 0.0;
+    }
+    size_t s = hidx(d, ub - 1, j, k);
+    for (int i = ub; i <= d.nx + 2; ++i) {
+      size_t q = hidx(d, i, j, k);
+      d.XKAPR[q] = d.XKAPR[s]; d.XKAPP[q] = d.XKAPP[s]; d.XKAPA[q] = d.XKAPA[s];
+      d.DXKAPP[q] = d.DXKAPP[s]; d.DXKAPA[q] = d.DXKAPA[s];
+    }
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// QDENS ppphy.f:47-76
+static int qdens(ttfld_ctx* c) {
+  Dev d = c->d;
+  launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    size_t q = hidx(d, i, j, k);
+    if (i >= 0) d.RHQX[q] = G(ddx1, i) * d.RH[q] + G(ddx0, i) * HA(RH, i - 1, j, k);
+    if (j >= 0) d.RHQY[q] = G(ddy1, j) * d.RH[q] + G(ddy0, j) * HA(RH, i, j - 1, k);
+    if (k >= 0) d.RHQZ[q] = G(ddz1, k) * d.RH[q] + G(ddz0, k) * HA(RH, i, j, k - 1);
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// FLIM pprphy.f:362-565 (IFLIMTYP 1 and 2, irad=3).
+static int flim(ttfld_ctx* c, int energy_iter) {
+  if (energy_iter <= 1) {  // :396-402
+    int rc = kappa(c);
+    if (rc) return rc;
+    if ((rc = qdens(c))) return rc;
+  }
+  Dev d = c->d;
+  const double sg = d.sigval;
+  if (d.iflimtyp == 1) {
+    launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+      size_t q = fidx(d, i, j, k);
+      d.FLIMX[q] = 1.0 / 3.0; d.FLIMY[q] = 1.0 / 3.0; d.FLIMZ[q] = 1.0 / 3.0;
+    });
+    TT_CHECK_LAUNCH();
+    return 0;
+  }
+  const double xdmin = 1.0e-50;
+  // x-direction :414-448, i = 1..UPPERBND(j,k)-1
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    if (i > PA(UB, j, k) - 1) return;
+    double gradx = (HA(ER, i, j, k) - HA(ER, i - 1, j, k)) / G(dxb, i);
+    double grady = (G(ddx1, i) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
+                    G(ddx0, i) * (HA(ER, i - 1, j + 1, k) - HA(ER, i - 1, j - 1, k))) /
+                   (G(geoxga, i) * G(geozg, k) * (G(xyb, j + 1) - G(xyb, j - 1)));
+    double gradz = (G(ddx1, i) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
+                    G(ddx0, i) * (HA(ER, i - 1, j, k + 1) - HA(ER, i - 1, j, k - 1))) /
+                   (G(geoxha, i) * (G(xzb, k + 1) - G(xzb, k - 1)));
+    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
+    double rrx = 2.0 * grad /
+                 (HA(RHQX, i, j, k) *
+                  (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)) *
+                  (HA(ER, i, j, k) + HA(ER, i - 1, j, k)));
+    FA(FLIMX, i, j, k) = (2.0 + rrx) / (6.0 + 3.0 * rrx + rrx * rrx);
+  });
+  TT_CHECK_LAUNCH();
+  // :449-454
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    int ub = PA(UB, j, k);
+    if (ub < 2 || ub > d.nx + 1) return;  // UPPERBND outside the grid: no copy
+    if (i >= ub) FA(FLIMX, i, j, k) = FA(FLIMX, ub - 1, j, k);
+  });
+  TT_CHECK_LAUNCH();
+  // y and z loops reuse the last x-loop xmax_index (pprphy.f:464, 495)
+  // y-direction :462-484
+  launch_box(c->stream, box(1, d.nx, 1, d.ny + 1, 1, d.nz), [=] __device__(int i, int j, int k) {
+    int xmax_index = PA(UB, d.ny, d.nz) - 1;
+    if (i > xmax_index) return;
+    double gradx = (G(ddy1, j) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
+                    G(ddy0, j) * (HA(ER, i + 1, j - 1, k) - HA(ER, i - 1, j - 1, k))) /
+                   (G(xxb, i + 1) - G(xxb, i - 1));
+    double grady = (HA(ER, i, j, k) - HA(ER, i, j - 1, k)) / (G(geoxg, i) * G(geozg, k) * G(dyb, j));
+    double gradz = (G(ddy1, j) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
+                    G(ddy0, j) * (HA(ER, i, j - 1, k + 1) - HA(ER, i, j - 1, k - 1))) /
+                   ((G(xzb, k + 1) - G(xzb, k - 1)) * G(geoxh, i));
+    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
+    double rry = 2.0 * grad /
+                 (HA(RHQY, i, j, k) *
+                  (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)) *
+                  (HA(ER, i, j, k) + HA(ER, i, j - 1, k)));
+    FA(FLIMY, i, j, k) = (2.0 + rry) / (6.0 + 3.0 * rry + rry * rry);
+  });
+  TT_CHECK_LAUNCH();
+  // z-direction :493-515
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+    int xmax_index = PA(UB, d.ny, d.nz) - 1;
+    if (i > xmax_index) return;
+    double gradx = (G(ddz1, k) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
+                    G(ddz0, k) * (HA(ER, i + 1, j, k - 1) - HA(ER, i - 1, j, k - 1))) /
+                   (G(xxb, i + 1) - G(xxb, i - 1));
+    double grady = (G(ddz1, k) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
+                    G(ddz0, k) * (HA(ER, i, j + 1, k - 1) - HA(ER, i, j - 1, k - 1))) /
+                   ((G(xyb, j + 1) - G(xyb, j - 1)) * G(geoxg, i) * G(geozga, k));
+    double gradz = (HA(ER, i, j, k) - HA(ER, i, j, k - 1)) / (G(geoxh, i) * G(dzb, k));
+    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
+    double rrz = 2.0 * grad /
+                 (HA(RHQZ, i, j, k) *
+                  (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)) *
+                  (HA(ER, i, j, k) + HA(ER, i, j, k - 1)));
+    FA(FLIMZ, i, j, k) = (2.0 + rrz) / (6.0 + 3.0 * rrz + rrz * rrz);
+  });
+  TT_CHECK_LAUNCH();
+  // :485-489 and :516-520 (the copies read only i = UPPERBND-1 values)
+  launch_box(c->stream, box(1, d.nx, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+    int ub = PA(UB, j, k);
+    if (ub < 2 || ub > d.nx + 1 || i < ub) return;
+    if (k <= d.nz) FA(FLIMY, i, j, k) = FA(FLIMY, ub - 1, j, k);
+    if (j <= d.ny) FA(FLIMZ, i, j, k) = FA(FLIMZ, ub - 1, j, k);
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// DIFF pprad.f:74-156
+static int diff(ttfld_ctx* c, int energy_iter) {
+  int rc = flim(c, energy_iter);
+  if (rc) return rc;
+  Dev d = c->d;
+  const double sg = d.sigval;
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+    if (j <= d.ny && k <= d.nz) {
+      double v = TT_FD * FA(FLIMX, i, j, k) /
+                 (G(dxb, i) * HA(RHQX, i, j, k) *
+                  (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)));
+      if (d.ieta == 5) {
+        double mn = HA(RHQX, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                    (G(dxb, i) * 4.0 * TT_ARAD *
+                     p3(G(ddx1, i) * HA(T, i, j, k) + G(ddx0, i) * HA(T, i - 1, j, k)) * d.pr_num);
+        v = fmax(v, mn);
+      }
+      FA(DIFRX, i, j, k) = v;
+    }
+    if (i <= d.nx && k <= d.nz) {
+      double v = TT_FD * FA(FLIMY, i, j, k) /
+                 (G(dyb, j) * G(geoxg, i) * G(geozg, k) * HA(RHQY, i, j, k) *
+                  (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)));
+      if (d.ieta == 5) {
+        double mn = HA(RHQY, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                    (G(dyb, j) * G(geoxg, i) * G(geozg, k) * 4.0 * TT_ARAD *
+                     p3(G(ddy1, j) * HA(T, i, j, k) + G(ddy0, j) * HA(T, i, j - 1, k)) * d.pr_num);
+        v = fmax(v, mn);
+      }
+      FA(DIFRY, i, j, k) = v;
+    }
+    if (i <= d.nx && j <= d.ny) {
+      double v = TT_FD * FA(FLIMZ, i, j, k) /
+                 (G(dzb, k) * G(geoxh, i) * HA(RHQZ, i, j, k) *
+                  (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)));
+      if (d.ieta == 5) {
+        double mn = HA(RHQZ, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                    (G(dzb, k) * G(geoxh, i) * 4.0 * TT_ARAD *
+                     p3(G(ddz1, k) * HA(T, i, j, k) + G(ddz0, k) * HA(T, i, j, k - 1)) * d.pr_num);
+        v = fmax(v, mn);
+      }
+      FA(DIFRZ, i, j, k) = v;
+    }
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// CALCULATEFLUX ppenergy.f:880-920 followed by FLUX_BC ppenergy.f:922-982.
+static int calculateflux(ttfld_ctx* c, int energy_iter) {
+  int rc = diff(c, energy_iter);
+  if (rc) return rc;
+  Dev d = c->d;
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+    if (j <= d.ny && k <= d.nz)
+      FA(FLUXX, i, j, k) = -FA(DIFRX, i, j, k) * (HA(ER, i, j, k) - HA(ER, i - 1, j, k));
+    if (i <= d.nx && k <= d.nz)
+      FA(FLUXY, i, j, k) = -FA(DIFRY, i, j, k) * (HA(ER, i, j, k) - HA(ER, i, j - 1, k));
+    if (i <= d.nx && j <= d.ny)
+      FA(FLUXZ, i, j, k) = -FA(DIFRZ, i, j, k) * (HA(ER, i, j, k) - HA(ER, i, j, k - 1));
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    int ub = PA(UB, j, k);
+    if (i >= ub && ub >= 1) {
+      FA(FLUXX, i, j, k) = TT_FD * HA(ER, ub - 1, j, k) / 2.0;
+      if (i != d.nx + 1) { FA(FLUXY, i, j, k) = 0.0; FA(FLUXZ, i, j, k) = 0.0; }
+    }
+    if (i == 1) FA(FLUXX, 1, j, k) = d.fbottom;
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// FILL_EVALUES ppenergy.f:984-1030
+static int fill_evalues(ttfld_ctx* c, double theta) {
+  Dev d = c->d;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    size_t q = cidx(d, i, j, k);
+    double e1 = -G(surxa, i + 1) * FA(DIFRX, i + 1, j, k) / (G(surxb, i) * G(dxa, i));
+    double e2 = -G(surxa, i) * FA(DIFRX, i, j, k) / (G(surxb, i) * G(dxa, i));
+    double e3 = -FA(DIFRY, i, j + 1, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
+    double e4 = -FA(DIFRY, i, j, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
+    double e5 = -FA(DIFRZ, i, j, k + 1) * G(surza, k + 1) / (G(xxb, i) * G(surzb, k) * G(dza, k));
+    double e6 = -FA(DIFRZ, i, j, k) * G(surza, k) / (G(xxb, i) * G(surzb, k) * G(dza, k));
+    double eta = d.ETA[q];
+    d.E1[q] = e1; d.E2[q] = e2; d.E3[q] = e3; d.E4[q] = e4; d.E5[q] = e5; d.E6[q] = e6;
+    d.E7[q] = 1.0 + (1.0 - eta) * d.delt * HA(RH, i, j, k) * HA(XKAPP, i, j, k) * TT_FD;
+    d.E8[q] = (eta * (1.0 - theta) - 1.0) * d.delt;
+    d.E16[q] = e1 + e2 + e3 + e4 + e5 + e6;
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// CALCULATEDIVF_WITHF ppenergy.f:825-878, NCOSYS=2 (:853-867).
+static int divf_withf(ttfld_ctx* c, double* out, double theta) {
+  Dev d = c->d;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    double xb = G(xxb, i), szb = G(surzb, k);
+    double v = ((G(surxa, i + 1) / (G(surxb, i) * G(dxa, i))) * FA(FLUXX, i + 1, j, k) -
+                (G(surxa, i) / (G(surxb, i) * G(dxa, i))) * FA(FLUXX, i, j, k)) +
+               ((1.0 / (xb * szb * G(dya, j))) * FA(FLUXY, i, j + 1, k) -
+                (1.0 / (xb * szb * G(dya, j))) * FA(FLUXY, i, j, k)) +
+               ((G(surza, k + 1) / (xb * szb * G(dza, k))) * FA(FLUXZ, i, j, k + 1) -
+                (G(surza, k) / (xb * szb * G(dza, k))) * FA(FLUXZ, i, j, k));
+    out[cidx(d, i, j, k)] = v;
+  });
+  TT_CHECK_LAUNCH();
+  return fill_evalues(c, theta);
+}
+
+// CALCSTELLARTAU pprad.f:191-221, STELLAR_DTAU :223-242 and the grey
+// STELLARINPUT of STELLARINPUT_HEATING :490-502.  STELLARINPUT is declared
+// (1:NX,-1:NY+2,-1:NZ+2) (ppmod.f:341); only i = 1..NX is formed.
+static int stellarinput_heating(ttfld_ctx* c) {
+  Dev d = c->d;
+  if (d.f_incident == 0) {
+    TT_CHECK(cudaMemsetAsync(d.SI, 0, nhalo(d) * 8, c->stream));
+    return 0;
+  }
+  launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
+    double dr = G(xxb, 2) - G(xxb, 1);
+    int ub = PA(UB, j, k);
+    if (ub > d.nx + 1) ub = d.nx + 1;
+    if (ub < d.nx)
+      for (int i = ub + 1; i <= d.nx + 1; ++i) HA(STAU, i, j, k) = 0.0;
+    double tot = 0.0;
+    for (int i = ub; i >= 1; --i) {
+      tot = tot + (HA(XKAPA, i, j, k) * HA(RH, i, j, k) * dr);
+      HA(STAU, i, j, k) = tot;
+    }
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(1, d.nx + 1, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    int is = i < 2 ? 2 : (i > d.nx ? d.nx : i);  // dtaus(1)=dtaus(2), dtaus(NX+1)=dtaus(NX)
+    HA(DTAUS, i, j, k) = (HA(STAU, is - 1, j, k) - HA(STAU, is + 1, j, k)) / 2.0;
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(1, d.nx, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    double tinc = PA(TINC, j, k), mu = PA(MU, j, k);
+    HA(SI, i, j, k) = TT_SBCONST * (p4(tinc) / mu) * (exp(-HA(STAU, i, j, k) / mu)) * HA(DTAUS, i, j, k) /
+                      G(dxb, i);
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// BOUNDS ppbou.f:1-92 for MODTYP=2 (MODVER 0,2-5), T/RH/UPPERBND only:
+// UPPERBND from density (ppbou.f:124-138), PASSUPPERBND one rank
+// (ppbou.f:522-682), BOUNDXMIN(9) (:1029-1049), BOUNDXMAX(2) (:1269-1384),
+// BOUNDZMIN(0)/BOUNDZMAX(0) (:1833-1846, :1946-1958), PLANETSHIFT(1..2).
+static int bounds(ttfld_ctx* c) {
+  Dev d = c->d;
+  int rc;
+  if (d.bcxmin != 9) return TTFLD_E_UNSUPPORTED;
+  if ((rc = halo_shift(c, d.T)) || (rc = halo_shift(c, d.RH))) return rc;
+  launch_box(c->stream, box(0, 0, 1, d.ny, 1, d.nz), [=] __device__(int, int j, int k) {
+    int ub = d.nx - 1;
+    for (int i = 1; i <= d.nx; ++i)
+      if (HA(RH, i, j, k) < (double)1.0e-9f) { ub = i; break; }
+    PA(UB, j, k) = ub;
+  });
+  TT_CHECK_LAUNCH();
+  // PASSUPPERBND one rank: j ghosts by wrap for k = 1..NZ, then edges.
+  launch_box(c->stream, box(0, 0, 0, 0, 1, d.nz), [=] __device__(int, int, int k) {
+    PA(UB, 0, k) = PA(UB, d.ny, k); PA(UB, -1, k) = PA(UB, d.ny - 1, k);
+    PA(UB, d.ny + 1, k) = PA(UB, 1, k); PA(UB, d.ny + 2, k) = PA(UB, 2, k);
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(0, 0, -1, d.ny + 2, 0, 0), [=] __device__(int, int j, int) {
+    const int nz = d.nz;
+    PA(UB, j, 0) = PA(UB, j, 1); PA(UB, j, -1) = PA(UB, j, 1);
+    PA(UB, j, nz + 1) = PA(UB, j, nz); PA(UB, j, nz + 2) = PA(UB, j, nz);
+  });
+  TT_CHECK_LAUNCH();
+  // BOUNDXMIN(9)
+  launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
+    double dtdr;
+    if (d.ieta == 5) {
+      dtdr = -d.fbottom / (HA(RH, 1, j, k) * HA(CV, 1, j, k) * (d.xnue / d.pr_num));
+    } else if (d.iii > 0) {
+      dtdr = -(3.0 * d.fbottom * HA(XKAPR, 1, j, k) * HA(RH, 1, j, k) /
+               (4.0 * TT_ARAD * TT_FD * p3(HA(T, 1, j, k))));
+    } else {
+      double k111 = kap_formula(d, HA(T, 1, 1, 1), HA(RH, 1, 1, 1), HA(KMUL, 1, 1, 1));
+      dtdr = -(3.0 * d.fbottom * k111 * HA(RH, 1, 1, 1) / (4.0 * TT_ARAD * TT_FD * p3(HA(T, 1, 1, 1))));
+    }
+    HA(T, 0, j, k) = HA(T, 1, j, k) - dtdr * (G(xxb, 1) - G(xxb, 0));
+    HA(T, -1, j, k) = HA(T, 1, j, k) - dtdr * (G(xxb, 1) - G(xxb, -1));
+  });
+  TT_CHECK_LAUNCH();
+  // BOUNDXMAX(2)
+  launch_box(c->stream, box(0, 0, 1, d.ny, 1, d.nz), [=] __device__(int, int j, int k) {
+    int ub = PA(UB, j, k);
+    double tj;
+    if (d.ibdrad == 9) {
+      if (d.iii <= 1)
+        tj = HA(T, ub - 1, j, k);
+      else
+        tj = pow((HA(ER, ub - 1, j, k) / TT_ARAD) +
+                     (HA(SI, ub - 1, j, k) / (4.0 * TT_SBCONST * HA(RH, ub - 1, j, k) * HA(XKAPP, ub - 1, j, k))),
+                 0.25);
+    } else if (d.ibdrad == 7) {
+      tj = HA(T, ub - 1, j, k);
+    } else {
+      tj = d.tirr;
+    }
+    HA(T, ub, j, k) = tj;
+    for (int i = ub + 1; i <= d.nx + 2; ++i) {
+      HA(T, i, j, k) = tj;
+      HA(RH, i, j, k) = (double)1.0e-10f;
+    }
+    if (ub == d.nx) { HA(RH, d.nx, j, k) = (double)1.0e-10f; HA(T, d.nx, j, k) = tj; }
+  });
+  TT_CHECK_LAUNCH();
+  // BOUNDZMIN(0) then BOUNDZMAX(0)
+  launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, 0, 0), [=] __device__(int i, int j, int) {
+    const int nz = d.nz;
+    HA(RH, i, j, 1) = HA(RH, i, j, 2); HA(RH, i, j, 0) = HA(RH, i, j, 1); HA(RH, i, j, -1) = HA(RH, i, j, 1);
+    HA(T, i, j, 1) = HA(T, i, j, 2); HA(T, i, j, 0) = HA(T, i, j, 1); HA(T, i, j, -1) = HA(T, i, j, 1);
+    HA(RH, i, j, nz) = HA(RH, i, j, nz - 1); HA(RH, i, j, nz + 1) = HA(RH, i, j, nz);
+    HA(RH, i, j, nz + 2) = HA(RH, i, j, nz);
+    HA(T, i, j, nz) = HA(T, i, j, nz - 1); HA(T, i, j, nz + 1) = HA(T, i, j, nz);
+    HA(T, i, j, nz + 2) = HA(T, i, j, nz);
+  });
+  TT_CHECK_LAUNCH();
+  if ((rc = halo_shift(c, d.T)) || (rc = halo_shift(c, d.RH))) return rc;
+  return 0;
+}
+
+// ---- exported to the step driver ---------------------------------------
+int asm_kappa(ttfld_ctx* c) { return kappa(c); }
+int asm_calculateflux(ttfld_ctx* c, int energy_iter) { return calculateflux(c, energy_iter); }
+int asm_fill_evalues(ttfld_ctx* c, double theta) { return fill_evalues(c, theta); }
+int asm_divf(ttfld_ctx* c, double* out, double theta) { return divf_withf(c, out, theta); }
+int asm_stellar(ttfld_ctx* c) { return stellarinput_heating(c); }
+int asm_bounds(ttfld_ctx* c) { return bounds(c); }
+int asm_diff(ttfld_ctx* c, int energy_iter) { return diff(c, energy_iter); }
+
+}  // namespace ttfld
+
+using namespace ttfld;
+
+extern "C" {
+
+int ttfld_bounds(ttfld_ctx* c) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = bounds(c);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_kappa(ttfld_ctx* c) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = kappa(c);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_stellarinput_heating(ttfld_ctx* c) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = stellarinput_heating(c);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_diff(ttfld_ctx* c, int energy_iter) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = diff(c, energy_iter);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_calculateflux(ttfld_ctx* c, int energy_iter) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = calculateflux(c, energy_iter);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_fill_evalues(ttfld_ctx* c, double theta) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = fill_evalues(c, theta);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,241 @@
+// ttfld_internal.cuh -- device-side state and helpers shared by the
+// libttfld translation units.  All FP64 arithmetic in this library is
+// compiled with --fmad=false, so an expression a*b+c is two rounded
+// operations exactly as in the reference loops; fused multiply-adds are
+// written out explicitly (fma / fmaf) where a kernel wants them.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/ttfld.h"
+
+// global_constants, ppmod.f:1074-1092: REAL*4 literals held in double.
+#define TT_FD ((double)2.99792458e10f)
+#define TT_ARAD ((double)7.56596e-15f)
+#define TT_SBCONST ((double)5.6705e-5f)
+
+namespace ttfld {
+
+constexpr int kThreads = 256;
+constexpr int kMaxPartials = 4096;   // per-colour block partials of a sweep
+
+// Device-side solver bookkeeping (one per context), written by kernels.
+struct SolverDev {
+  double rhsnorm;      // global_RHSNORM
+  double rnorm;        // global_RNORM of the last completed sweep
+  double ratio;        // rnorm / rhsnorm
+  double true_l1;      // ||b - A x||_1 of the last residual pass
+  double scratch[4];
+  int iter;            // SOR_ITER
+  int done;            // 1 once the stopping rule fired
+  int maxit;           // 1 if ITMAX ended the loop
+  int nonfinite;       // 1 if a norm was NaN/Inf
+  unsigned int ticket; // last-block-done counter
+  unsigned int ticket2;
+  int pad[2];
+};
+
+// Reduction targets of the outer Newton loop.
+struct StepDev {
+  unsigned long long maxq_bits;   // max |dQ/Q| as IEEE bits (non-negative)
+  unsigned long long maxer_bits;  // max |dER/ER|
+  int nonpositive_q;              // ppenergy.f:411 guard fired
+  int dfq_zero;                   // ppenergy.f:334-340 (eta forced to 0)
+  int pad[2];
+};
+
+// Every array the step touches, in the reference's Fortran layout.
+// 1-D metrics are stored on (-1:N+2) and addressed with G(a, i) = a[i+1].
+struct Dev {
+  int nx, ny, nz;
+  // 1-D grid metrics
+  const double *xxa, *xxb, *dxa, *dxb, *xya, *xyb, *dya, *dyb, *xza, *xzb, *dza, *dzb;
+  const double *ddx0, *ddx1, *ddy0, *ddy1, *ddz0, *ddz1;
+  const double *surxa, *surxb, *surza, *surzb, *geoxg, *geoxh, *geoxga, *geoxha, *geozg, *geozga;
+  // halo (-1:NX+2,-1:NY+2,-1:NZ+2)
+  double *T, *RH, *CV, *ER, *ER_OLD, *Q, *Q_OLD, *DELTA_ER, *XKAPR, *XKAPP, *XKAPA;
+  double *DXKAPP, *DXKAPA, *KMUL, *RHQX, *RHQY, *RHQZ, *STAU, *DTAUS, *SI, *SCALAR;
+  // cell (1:NX,1:NY,1:NZ)
+  double *E1, *E2, *E3, *E4, *E5, *E6, *E7, *E8, *E16, *ETA, *FQ, *FR, *RHS;
+  double *SA, *SB, *SC, *SD, *SE, *SF, *SG, *DIVF, *DIVF_OLD, *DFQ, *DFR, *DQ, *RHS_DIF;
+  // face (1:NX+1,1:NY+1,1:NZ+1) internal storage
+  double *FLIMX, *FLIMY, *FLIMZ, *DIFRX, *DIFRY, *DIFRZ, *FLUXX, *FLUXY, *FLUXZ;
+  // plane (-1:NY+2,-1:NZ+2)
+  int* UB;
+  double *MU, *TINC;
+  // scalars
+  double delt, sorparam, epsmat, fbottom, tirr, xnue, pr_num, kap0, sigval;
+  int itmax, bcxmin, ibdrad, iflimtyp, f_incident, ieta, isigtyp, iii, kappa_model;
+  SolverDev* sol;
+  StepDev* stp;
+};
+
+__host__ __device__ __forceinline__ size_t hidx(const Dev& d, int i, int j, int k) {
+  return (size_t)(i + 1) + (size_t)(d.nx + 4) * ((size_t)(j + 1) + (size_t)(d.ny + 4) * (size_t)(k + 1));
+}
+__host__ __device__ __forceinline__ size_t cidx(const Dev& d, int i, int j, int k) {
+  return (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
+}
+__host__ __device__ __forceinline__ size_t fidx(const Dev& d, int i, int j, int k) {
+  return (size_t)(i - 1) + (size_t)(d.nx + 1) * ((size_t)(j - 1) + (size_t)(d.ny + 1) * (size_t)(k - 1));
+}
+__host__ __device__ __forceinline__ size_t pidx(const Dev& d, int j, int k) {
+  return (size_t)(j + 1) + (size_t)(d.ny + 4) * (size_t)(k + 1);
+}
+__host__ __device__ __forceinline__ size_t nhalo(const Dev& d) {
+  return (size_t)(d.nx + 4) * (d.ny + 4) * (d.nz + 4);
+}
+__host__ __device__ __forceinline__ size_t ncell(const Dev& d) { return (size_t)d.nx * d.ny * d.nz; }
+__host__ __device__ __forceinline__ size_t nface(const Dev& d) {
+  return (size_t)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
+}
+__host__ __device__ __forceinline__ size_t nplane(const Dev& d) { return (size_t)(d.ny + 4) * (d.nz + 4); }
+
+#define G(a, i) (d.a[(i) + 1])
+#define HA(a, i, j, k) (d.a[hidx(d, i, j, k)])
+#define CA(a, i, j, k) (d.a[cidx(d, i, j, k)])
+#define FA(a, i, j, k) (d.a[fidx(d, i, j, k)])
+#define PA(a, j, k) (d.a[pidx(d, j, k)])
+
+__device__ __forceinline__ double p4(double x) { double x2 = x * x; return x2 * x2; }
+__device__ __forceinline__ double p3(double x) { return (x * x) * x; }
+
+// An inclusive index box [i0,i1]x[j0,j1]x[k0,k1] walked i fastest.
+struct Box {
+  int i0, j0, k0, ni, nj, nk;
+};
+inline Box box(int i0, int i1, int j0, int j1, int k0, int k1) {
+  Box b{i0, j0, k0, i1 - i0 + 1, j1 - j0 + 1, k1 - k0 + 1};
+  if (b.ni < 0) b.ni = 0;
+  if (b.nj < 0) b.nj = 0;
+  if (b.nk < 0) b.nk = 0;
+  return b;
+}
+
+template <class Fn>
+__global__ void __launch_bounds__(kThreads) box_kernel(Box b, Fn fn) {
+  const long long n = (long long)b.ni * b.nj * b.nk;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = b.i0 + (int)(t % b.ni);
+    long long r = t / b.ni;
+    int j = b.j0 + (int)(r % b.nj);
+    int k = b.k0 + (int)(r / b.nj);
+    fn(i, j, k);
+  }
+}
+
+int grid_for(long long n, int threads = kThreads);
+void count_launches(int n);
+
+template <class Fn>
+inline void launch_box(cudaStream_t s, Box b, Fn fn) {
+  long long n = (long long)b.ni * b.nj * b.nk;
+  if (n <= 0) return;
+  box_kernel<<<grid_for(n), kThreads, 0, s>>>(b, fn);
+  count_launches(1);
+}
+
+// Deterministic block sum: every thread passes its value, thread 0 gets the
+// block total (fixed shuffle tree, fixed order across warps).
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int q = 0; q < nw; ++q) t += sh[q];
+  }
+  __syncthreads();
+  return t;
+}
+
+// Fixed-order sum of n partials by one block (result valid in thread 0).
+__device__ __forceinline__ double block_sum_array(const double* p, int n, double* sh) {
+  double v = 0.0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) v += p[q];
+  return block_sum(v, sh);
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* a, double v) {
+  atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ bool solver_done(const Dev& d) {
+  return *(volatile int*)&d.sol->done != 0;
+}
+
+// Fixed-order finalisation of one sweep: sum the two colours' partials,
+// advance SOR_ITER, apply the stopping rule of ppsor.f:161-177.
+__device__ __forceinline__ void finalize_sweep(const Dev& d, const double* partials, int nblk, int itmin, int itmax,
+                               double eps, double* sh) {
+  double r0 = block_sum_array(partials, nblk, sh);
+  double r1 = block_sum_array(partials + kMaxPartials, nblk, sh);
+  if (threadIdx.x == 0) {
+    double rnorm = r0 + r1;
+    SolverDev* s = d.sol;
+    int it = s->iter + 1;
+    s->iter = it;
+    s->rnorm = rnorm;
+    double ratio = rnorm / s->rhsnorm;
+    s->ratio = ratio;
+    if (!isfinite(rnorm)) { s->nonfinite = 1; s->done = 1; }
+    else if (it == itmax) { s->maxit = 1; s->done = 1; }
+    else if (!(ratio > eps) && it >= itmin) { s->done = 1; }
+    s->ticket = 0;
+  }
+}
+
+}  // namespace ttfld
+
+// Host-side context (the library's one handle per device).
+struct ttfld_ctx {
+  ttfld::Dev d;              // device pointers + scalars (passed to kernels)
+  ttfld_dims dims;
+  ttfld_params params;
+  ttfld_solve_opts opts;
+  int device;
+  cudaStream_t stream;
+  cudaEvent_t ev0, ev1;
+  void* slab;                // one allocation holding every array
+  size_t slab_bytes;
+  double* staging;           // device staging for box-shaped transfers
+  double* partials;          // 2 * kMaxPartials sweep partials
+  ttfld::SolverDev* sol;
+  ttfld::StepDev* stp;
+  ttfld::SolverDev* host_sol;  // pinned mirror
+  // mixed-precision workspace (allocated on first use)
+  void* mix_slab;
+  size_t mix_bytes;
+  // learned guess
+  void* unet;
+  int have_model;
+  double prev_scale;        // (1-conv_parm) for the previous-solution guess
+  int have_prev;
+  double* prev_x;           // previous outer solution (halo)
+  double last_solve_ms;
+};
+
+namespace ttfld {
+int check_cuda(cudaError_t e, const char* what);
+#define TT_CHECK(call)                                   \
+  do {                                                   \
+    int _rc = ttfld::check_cuda((call), #call);          \
+    if (_rc) return _rc;                                 \
+  } while (0)
+#define TT_CHECK_LAUNCH() TT_CHECK(cudaGetLastError())
+
+// Internal entry points shared across translation units.
+int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st);
+int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st);
+int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st);
+int fill_sor_matrix(ttfld_ctx* c);
+int halo_shift(ttfld_ctx* c, double* a);
+int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);
+int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1);
+int unet_guess(ttfld_ctx* c, double* x_out, double* resid_l1);
+void unet_free(ttfld_ctx* c);
+}  // namespace ttfld

@@ -1,0 +1,564 @@
+// ttfld_mixed.cu -- the two fast solvers of SOLVE_WITH_SOR's system:
+//
+//  * TTFLD_SOLVER_MIXED: FP32 red-black SOR sweeps on the correction
+//    equation A e = r inside an FP64 defect-correction loop
+//    (x += e; r = b - A x in FP64).  Red-black SOR is a stationary iteration,
+//    so m sweeps on A e = r from e = 0 followed by x += e give the same
+//    iterate as m more sweeps on A x = b; the FP64 residual re-anchors the
+//    iterate so the FP32 rounding never accumulates.  It stops on the true
+//    residual ||b - A x||_1 / ||b||_1 <= tol.
+//  * TTFLD_SOLVER_SOR64_FAST: the reference's FP64 red-black SOR with its
+//    in-sweep stopping rule (ppsor.f:161-177), on Jacobi-scaled
+//    coefficients with fused multiply-adds.
+//
+// Both keep their working arrays colour-compacted: the cells of one colour
+// in a (j,k) row are stored contiguously along the radial index, padded to
+// a multiple of four, so a half-sweep reads and writes only its own colour
+// with 16-byte vector accesses.  For cell (i,j,k) (1-based) the colour is
+// (i+j+k)&1 (0 = the reference's first pass, ppsor.f:59-61), its slot is
+// h = (i-1)>>1 in row (k-1)*NY + (j-1).  In a row with q = (j+k)&1 (0-based
+// j,k) the colour-c cells have i0 = 2h + off, off = (1+q+c)&1; their radial
+// neighbours in the other colour sit at h+off-1 and h+off, the phi and
+// theta neighbours at the same h.
+#include <math.h>
+
+#include "ttfld_internal.cuh"
+
+namespace ttfld {
+
+struct Cmp {
+  int nx, ny, nz, nxp;  // nxp: padded slots per colour row (multiple of 4)
+  long long rows;       // ny * nz
+  size_t csz;           // slots per colour array (no ghost planes)
+  size_t gsz;           // slots per colour array with theta ghost planes
+};
+
+static Cmp make_cmp(const Dev& d) {
+  Cmp g;
+  g.nx = d.nx; g.ny = d.ny; g.nz = d.nz;
+  int nxh = (d.nx + 1) / 2;
+  g.nxp = (nxh + 3) / 4 * 4;
+  g.rows = (long long)d.ny * d.nz;
+  g.csz = (size_t)g.rows * g.nxp;
+  g.gsz = (size_t)(d.nz + 2) * d.ny * g.nxp;
+  return g;
+}
+
+struct Mix32 {
+  float* a[6][2];   // W E S N B T (xm xp jm jp km kp) over A, per colour
+  float* ainv[2];   // 1/A
+  float* rhat[2];   // r / A
+  float* e[2];      // correction, with theta ghost planes
+};
+
+struct Fast64 {
+  double* a[6][2];
+  double* bhat[2];  // (b - ghost couplings) / A
+  double* diag[2];  // A
+  double* x[2];     // iterate, with theta ghost planes
+};
+
+struct MixWork {
+  Cmp g;
+  int have32, have64;
+  void* mem32;
+  void* mem64;
+  Mix32 m32;
+  Fast64 m64;
+};
+
+__host__ __device__ __forceinline__ size_t cslot(const Cmp& g, int j0, int k0, int h) {
+  return ((size_t)k0 * g.ny + j0) * g.nxp + h;
+}
+__host__ __device__ __forceinline__ size_t gslot(const Cmp& g, int j0, int k0, int h) {
+  return ((size_t)(k0 + 1) * g.ny + j0) * g.nxp + h;
+}
+
+static MixWork* work(ttfld_ctx* c) {
+  if (!c->mix_slab) {
+    MixWork* w = (MixWork*)calloc(1, sizeof(MixWork));
+    w->g = make_cmp(c->d);
+    c->mix_slab = w;
+  }
+  return (MixWork*)c->mix_slab;
+}
+
+static int ensure32(ttfld_ctx* c) {
+  MixWork* w = work(c);
+  if (w->have32) return 0;
+  const Cmp& g = w->g;
+  size_t n = 2 * (6 + 2) * g.csz + 2 * g.gsz;
+  float* p = nullptr;
+  TT_CHECK(cudaMalloc((void**)&p, n * sizeof(float)));
+  TT_CHECK(cudaMemset(p, 0, n * sizeof(float)));
+  w->mem32 = p;
+  for (int q = 0; q < 6; ++q)
+    for (int col = 0; col < 2; ++col) { w->m32.a[q][col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m32.ainv[col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m32.rhat[col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m32.e[col] = p; p += g.gsz; }
+  w->have32 = 1;
+  return 0;
+}
+
+static int ensure64(ttfld_ctx* c) {
+  MixWork* w = work(c);
+  if (w->have64) return 0;
+  const Cmp& g = w->g;
+  size_t n = 2 * (6 + 2) * g.csz + 2 * g.gsz;
+  double* p = nullptr;
+  TT_CHECK(cudaMalloc((void**)&p, n * sizeof(double)));
+  TT_CHECK(cudaMemset(p, 0, n * sizeof(double)));
+  w->mem64 = p;
+  for (int q = 0; q < 6; ++q)
+    for (int col = 0; col < 2; ++col) { w->m64.a[q][col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m64.bhat[col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m64.diag[col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m64.x[col] = p; p += g.gsz; }
+  w->have64 = 1;
+  return 0;
+}
+
+void mix_free(ttfld_ctx* c) {
+  MixWork* w = (MixWork*)c->mix_slab;
+  if (!w) return;
+  if (w->mem32) cudaFree(w->mem32);
+  if (w->mem64) cudaFree(w->mem64);
+  free(w);
+  c->mix_slab = nullptr;
+}
+
+// ---- FP32 path ----------------------------------------------------------
+
+// Jacobi-scaled FP32 coefficients of the current SOR_A..G.
+static int prep32(ttfld_ctx* c) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  Mix32 m = w->m32;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    size_t q = cidx(d, i, j, k);
+    int col = (i + j + k) & 1;
+    size_t s = cslot(g, j - 1, k - 1, (i - 1) >> 1);
+    double inv = 1.0 / d.SA[q];
+    m.a[0][col][s] = (float)(d.SB[q] * inv);
+    m.a[1][col][s] = (float)(d.SC[q] * inv);
+    m.a[2][col][s] = (float)(d.SD[q] * inv);
+    m.a[3][col][s] = (float)(d.SE[q] * inv);
+    m.a[4][col][s] = (float)(d.SF[q] * inv);
+    m.a[5][col][s] = (float)(d.SG[q] * inv);
+    m.ainv[col][s] = (float)inv;
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+// One colour of FP32 red-black SOR on A e = r (Jacobi-scaled), 4 cells per
+// thread.  e_new = e + omega * ((rhat - sum a_nb e_nb) - e).
+template <int COL>
+__global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega) {
+  const int nv = g.nxp >> 2;
+  const long long n = g.rows * nv;
+  const float* __restrict__ eo = m.e[1 - COL];
+  float* __restrict__ es = m.e[COL];
+  const size_t plane = (size_t)g.ny * g.nxp;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int hv = (int)(t % nv);
+    const long long rr = t / nv;
+    const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
+    const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
+    const int h0 = hv * 4;
+    const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
+    const size_t cb = (size_t)rr * g.nxp + h0;
+    const size_t eb = gslot(g, j0, k0, h0);
+    const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
+    const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
+    const float4 o = ld4(eo + eb);
+    float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
+    if (off == 0) {
+      xm0 = h0 > 0 ? eo[eb - 1] : 0.f; xm1 = o.x; xm2 = o.y; xm3 = o.z;
+      xp0 = o.x; xp1 = o.y; xp2 = o.z; xp3 = o.w;
+    } else {
+      xm0 = o.x; xm1 = o.y; xm2 = o.z; xm3 = o.w;
+      xp0 = o.y; xp1 = o.z; xp2 = o.w; xp3 = (h0 + 4 < g.nxp) ? eo[eb + 4] : 0.f;
+    }
+    const float4 s = ld4(eo + gslot(g, jm, k0, h0));
+    const float4 nn = ld4(eo + gslot(g, jp, k0, h0));
+    const float4 b = ld4(eo + eb - plane);
+    const float4 tt = ld4(eo + eb + plane);
+    const float4 e = ld4(es + eb);
+    const float4 aw = ld4(m.a[0][COL] + cb), ae = ld4(m.a[1][COL] + cb);
+    const float4 as = ld4(m.a[2][COL] + cb), an = ld4(m.a[3][COL] + cb);
+    const float4 ab = ld4(m.a[4][COL] + cb), at = ld4(m.a[5][COL] + cb);
+    const float4 r = ld4(m.rhat[COL] + cb);
+    float4 out;
+#define UPD(L, XM, XP)                                                                 \
+  {                                                                                    \
+    float acc = fmaf(aw.L, XM, fmaf(ae.L, XP, fmaf(as.L, s.L, fmaf(an.L, nn.L,         \
+                fmaf(ab.L, b.L, at.L * tt.L)))));                                      \
+    float v = fmaf(omega, (r.L - acc) - e.L, e.L);                                     \
+    out.L = (h0 + L##_IDX < ncol) ? v : 0.f;                                           \
+  }
+#define x_IDX 0
+#define y_IDX 1
+#define z_IDX 2
+#define w_IDX 3
+    UPD(x, xm0, xp0) UPD(y, xm1, xp1) UPD(z, xm2, xp2) UPD(w, xm3, xp3)
+#undef UPD
+    st4(es + eb, out);
+  }
+}
+
+// x += e over the interior of a halo array (natural layout).
+static int add_correction(ttfld_ctx* c, double* x) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  const float* e0 = w->m32.e[0];
+  const float* e1 = w->m32.e[1];
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    int col = (i + j + k) & 1;
+    const float* e = col ? e1 : e0;
+    size_t q = hidx(d, i, j, k);
+    x[q] = x[q] + (double)e[gslot(g, j - 1, k - 1, (i - 1) >> 1)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// r = b - A x in FP64 (FMA), its L1 norm (fixed-order) and rhat = r/A in FP32.
+__global__ void __launch_bounds__(kThreads) resid32_kernel(Dev d, Cmp g, Mix32 m, const double* __restrict__ x,
+                                                           const double* __restrict__ b, double* partials) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long n = (long long)nx * ny * nz;
+  const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % nx) + 1;
+    long long r = t / nx;
+    int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    size_t q = hidx(d, i, j, k);
+    size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
+    size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
+    double ax = d.SA[t] * x[q];
+    ax = fma(d.SB[t], x[q - 1], ax);
+    ax = fma(d.SC[t], x[q + 1], ax);
+    ax = fma(d.SD[t], x[qjm], ax);
+    ax = fma(d.SE[t], x[qjp], ax);
+    ax = fma(d.SF[t], x[q - sk], ax);
+    ax = fma(d.SG[t], x[q + sk], ax);
+    double rr = b[t] - ax;
+    acc += fabs(rr);
+    int col = (i + j + k) & 1;
+    size_t s = cslot(g, j - 1, k - 1, (i - 1) >> 1);
+    m.rhat[col][s] = __double2float_rn(rr) * m.ainv[col][s];
+  }
+  double sblk = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = sblk;
+    __threadfence();
+    last = (atomicAdd(&d.sol->ticket2, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double tot = block_sum_array(partials, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      d.sol->true_l1 = tot;
+      d.sol->ticket2 = 0;
+    }
+  }
+}
+
+static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
+  MixWork* w = work(c);
+  int nb = grid_for((long long)ncell(c->d));
+  if (nb > kMaxPartials) nb = kMaxPartials;
+  resid32_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->g, w->m32, x, b, c->partials + kMaxPartials);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  *l1 = c->host_sol->true_l1;
+  return 0;
+}
+
+int launch_sweeps32(ttfld_ctx* c, int nsweeps) {
+  MixWork* w = work(c);
+  const Cmp& g = w->g;
+  long long nvec = g.rows * (g.nxp >> 2);
+  int nb = grid_for(nvec);
+  float omega = (float)c->d.sorparam;
+  for (int s = 0; s < nsweeps; ++s) {
+    sweep32_kernel<0><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega);
+    sweep32_kernel<1><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega);
+  }
+  count_launches(2 * nsweeps);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st) {
+  int rc;
+  if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
+  MixWork* w = work(c);
+  const Cmp& g = w->g;
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  double bl1 = 0.0, l1 = 0.0;
+  if ((rc = rhs_norm(c, b, &bl1))) return rc;
+  if ((rc = resid32(c, x, b, &l1))) return rc;
+  const double tol = c->opts.tol;
+  const int imin = c->opts.inner_min, imax = c->opts.inner_max;
+  const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : 100LL * c->d.itmax;
+  long long total = 0;
+  int corrections = 0, stall = 0, status = TTFLD_OK;
+  int m = imin;
+  double prev = l1;
+  while (l1 > tol * bl1) {
+    if (!isfinite(l1)) { status = TTFLD_E_NONFINITE; break; }
+    if (total >= budget || stall >= 3) { status = TTFLD_MAXITER; break; }
+    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
+    if ((rc = launch_sweeps32(c, m))) return rc;
+    total += m;
+    if ((rc = add_correction(c, x))) return rc;
+    if ((rc = resid32(c, x, b, &l1))) return rc;
+    ++corrections;
+    double rate = (prev > 0.0 && l1 > 0.0) ? pow(l1 / prev, 1.0 / m) : 0.0;
+    if (l1 < prev) {
+      stall = 0;
+      double need = (rate > 0.0 && rate < 1.0) ? log(tol * bl1 / l1) / log(rate) : (double)imin;
+      double nm = ceil(need * 1.05) + 1.0;
+      m = (int)(nm < imin ? imin : (nm > imax ? imax : nm));
+    } else {
+      ++stall;
+      m = imax;
+    }
+    prev = l1;
+  }
+  if ((rc = halo_shift(c, x))) return rc;
+  if (st) {
+    st->sor_iter = (int)total;
+    st->corrections = corrections;
+    st->rhsnorm = bl1;
+    st->rnorm = l1;
+    st->true_resid_l1 = l1;
+    st->status = status;
+  }
+  c->host_sol->iter = (int)total;
+  return status;
+}
+
+// ---- fast FP64 path -----------------------------------------------------
+
+// Scaled FP64 coefficients; couplings to non-zero ghost values of x (the
+// radial and theta ghosts, fixed during a solve) are folded into bhat.
+static int prep64(ttfld_ctx* c, const double* x, const double* b) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  Fast64 m = w->m64;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    size_t q = cidx(d, i, j, k);
+    int col = (i + j + k) & 1;
+    size_t s = cslot(g, j - 1, k - 1, (i - 1) >> 1);
+    double a = d.SA[q];
+    double inv = 1.0 / a;
+    double bb = b[q];
+    if (i == 1) bb = bb - d.SB[q] * x[hidx(d, 0, j, k)];
+    if (i == d.nx) bb = bb - d.SC[q] * x[hidx(d, d.nx + 1, j, k)];
+    if (k == 1) bb = bb - d.SF[q] * x[hidx(d, i, j, 0)];
+    if (k == d.nz) bb = bb - d.SG[q] * x[hidx(d, i, j, d.nz + 1)];
+    m.a[0][col][s] = d.SB[q] * inv;
+    m.a[1][col][s] = d.SC[q] * inv;
+    m.a[2][col][s] = d.SD[q] * inv;
+    m.a[3][col][s] = d.SE[q] * inv;
+    m.a[4][col][s] = d.SF[q] * inv;
+    m.a[5][col][s] = d.SG[q] * inv;
+    m.bhat[col][s] = bb * inv;
+    m.diag[col][s] = a;
+    m.x[col][gslot(g, j - 1, k - 1, (i - 1) >> 1)] = x[hidx(d, i, j, k)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+static int unpack64(ttfld_ctx* c, double* x) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  Fast64 m = w->m64;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    int col = (i + j + k) & 1;
+    x[hidx(d, i, j, k)] = m.x[col][gslot(g, j - 1, k - 1, (i - 1) >> 1)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+__device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
+__device__ __forceinline__ void st2(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
+
+// One colour of the FP64 red-black sweep on the scaled system, 2 cells per
+// thread: rh = x + sum a_nb x_nb - bhat; resid = A*rh (the reference's
+// in-sweep residual, ppsor.f:64-73); x -= omega*rh.
+template <int COL>
+__global__ void __launch_bounds__(kThreads) sweep64_kernel(Dev d, Cmp g, Fast64 m, double omega, double* partials,
+                                                           int itmin, int itmax, double eps) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (solver_done(d)) return;
+  const int nv = g.nxp >> 1;
+  const long long n = g.rows * nv;
+  const double* __restrict__ xo = m.x[1 - COL];
+  double* __restrict__ xs = m.x[COL];
+  const size_t plane = (size_t)g.ny * g.nxp;
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int hv = (int)(t % nv);
+    const long long rr = t / nv;
+    const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
+    const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
+    const int h0 = hv * 2;
+    const int ncol = (g.nx - off + 1) >> 1;
+    const size_t cb = (size_t)rr * g.nxp + h0;
+    const size_t eb = gslot(g, j0, k0, h0);
+    const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
+    const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
+    const double2 o = ld2(xo + eb);
+    double xm0, xm1, xp0, xp1;
+    if (off == 0) {
+      xm0 = h0 > 0 ? xo[eb - 1] : 0.0; xm1 = o.x; xp0 = o.x; xp1 = o.y;
+    } else {
+      xm0 = o.x; xm1 = o.y; xp0 = o.y; xp1 = (h0 + 2 < g.nxp) ? xo[eb + 2] : 0.0;
+    }
+    const double2 s = ld2(xo + gslot(g, jm, k0, h0));
+    const double2 nn = ld2(xo + gslot(g, jp, k0, h0));
+    const double2 bz = ld2(xo + eb - plane);
+    const double2 tz = ld2(xo + eb + plane);
+    const double2 xv = ld2(xs + eb);
+    const double2 aw = ld2(m.a[0][COL] + cb), ae = ld2(m.a[1][COL] + cb);
+    const double2 as = ld2(m.a[2][COL] + cb), an = ld2(m.a[3][COL] + cb);
+    const double2 ab = ld2(m.a[4][COL] + cb), at = ld2(m.a[5][COL] + cb);
+    const double2 bh = ld2(m.bhat[COL] + cb), dg = ld2(m.diag[COL] + cb);
+    double2 out;
+    {
+      double rh = fma(aw.x, xm0, fma(ae.x, xp0, fma(as.x, s.x, fma(an.x, nn.x, fma(ab.x, bz.x, fma(at.x, tz.x, xv.x - bh.x))))));
+      bool ok = h0 < ncol;
+      acc += ok ? fabs(dg.x * rh) : 0.0;
+      out.x = ok ? fma(-omega, rh, xv.x) : 0.0;
+    }
+    {
+      double rh = fma(aw.y, xm1, fma(ae.y, xp1, fma(as.y, s.y, fma(an.y, nn.y, fma(ab.y, bz.y, fma(at.y, tz.y, xv.y - bh.y))))));
+      bool ok = h0 + 1 < ncol;
+      acc += ok ? fabs(dg.y * rh) : 0.0;
+      out.y = ok ? fma(-omega, rh, xv.y) : 0.0;
+    }
+    st2(xs + eb, out);
+  }
+  double sb = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    partials[COL * kMaxPartials + blockIdx.x] = sb;
+    if (COL == 1) {
+      __threadfence();
+      last = (atomicAdd(&d.sol->ticket, 1u) == gridDim.x - 1);
+    }
+  }
+  if (COL == 1) {
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      finalize_sweep(d, partials, gridDim.x, itmin, itmax, eps, sh);
+    }
+  }
+}
+
+int launch_sweeps64(ttfld_ctx* c, int nsweeps, int itmin, int itmax, double eps) {
+  MixWork* w = work(c);
+  const Cmp& g = w->g;
+  long long nvec = g.rows * (g.nxp >> 1);
+  int nb = grid_for(nvec);
+  if (nb > kMaxPartials) nb = kMaxPartials;
+  double omega = c->d.sorparam;
+  for (int s = 0; s < nsweeps; ++s) {
+    sweep64_kernel<0><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
+    sweep64_kernel<1><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
+  }
+  count_launches(2 * nsweeps);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
+  int rc;
+  if ((rc = ensure64(c))) return rc;
+  MixWork* w = work(c);
+  TT_CHECK(cudaMemsetAsync(w->m64.x[0], 0, 2 * w->g.gsz * sizeof(double), c->stream));
+  if ((rc = prep64(c, x, b))) return rc;
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  if ((rc = rhs_norm(c, b, nullptr))) return rc;
+  int chunk = 4, launched = 0;
+  for (;;) {
+    if ((rc = launch_sweeps64(c, chunk, itmin, itmax, c->d.epsmat))) return rc;
+    launched += chunk;
+    TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    if (c->host_sol->done) break;
+    if (launched >= itmax + 2) return TTFLD_E_CUDA;
+    chunk = chunk < 128 ? chunk * 2 : 256;
+  }
+  if ((rc = unpack64(c, x)) || (rc = halo_shift(c, x))) return rc;
+  int status = c->host_sol->nonfinite ? TTFLD_E_NONFINITE : (c->host_sol->maxit ? TTFLD_MAXITER : TTFLD_OK);
+  if (st) {
+    st->sor_iter = c->host_sol->iter;
+    st->rnorm = c->host_sol->rnorm;
+    st->rhsnorm = c->host_sol->rhsnorm;
+    st->status = status;
+  }
+  return status;
+}
+
+}  // namespace ttfld
+
+namespace ttfld {
+int launch_exact_sweeps(ttfld_ctx* c, double* x, const double* b, int nsweeps, int itmin, int itmax, double eps);
+
+// Mean device time of one full sweep of a solver's kernels (measurement).
+int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
+  int rc;
+  if (n < 1) return TTFLD_E_ARGS;
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  if ((rc = rhs_norm(c, c->d.RHS, nullptr))) return rc;
+  if (solver == TTFLD_SOLVER_MIXED) {
+    if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
+    double l1;
+    if ((rc = resid32(c, c->d.DELTA_ER, c->d.RHS, &l1))) return rc;
+    if ((rc = launch_sweeps32(c, 1))) return rc;  // warm
+  } else if (solver == TTFLD_SOLVER_SOR64_FAST) {
+    if ((rc = ensure64(c)) || (rc = prep64(c, c->d.DELTA_ER, c->d.RHS))) return rc;
+    if ((rc = launch_sweeps64(c, 1, n + 8, n + 8, -1.0))) return rc;
+  } else {
+    if ((rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, 1, n + 8, n + 8, -1.0))) return rc;
+  }
+  TT_CHECK(cudaEventRecord(c->ev0, c->stream));
+  if (solver == TTFLD_SOLVER_MIXED) rc = launch_sweeps32(c, n);
+  else if (solver == TTFLD_SOLVER_SOR64_FAST) rc = launch_sweeps64(c, n, n + 8, n + 8, -1.0);
+  else rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, n, n + 8, n + 8, -1.0);
+  if (rc) return rc;
+  TT_CHECK(cudaEventRecord(c->ev1, c->stream));
+  TT_CHECK(cudaEventSynchronize(c->ev1));
+  float t = 0.f;
+  TT_CHECK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+  *ms = (double)t / n;
+  return 0;
+}
+}  // namespace ttfld
+
+extern "C" int ttfld_time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
+  if (!c || !ms) return TTFLD_E_ARGS;
+  return ttfld::time_sweeps(c, solver, n, ms);
+}

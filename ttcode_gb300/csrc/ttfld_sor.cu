@@ -1,0 +1,424 @@
+// ttfld_sor.cu -- FILL_SOR_MATRIX / B_VECTOR_BOUNDARIES and the FP64
+// red-black SOR of SOLVE_WITH_SOR (ppsor.f:2-329) on the device.
+//
+// The exact kernel evaluates each cell update with the reference's operand
+// order and no fused multiply-add, so every sweep leaves DELTA_ER bitwise
+// equal to the serial Fortran loop: within one colour no cell reads another
+// cell of the same colour, so the order of the updates inside a colour does
+// not change any value.  The periodic phi direction is read by wrapping the
+// j index, which equals the reference's halo copy (PLANETSHIFT(8)) after
+// each colour because NY is even (the two wrapped neighbours have the
+// other colour).  The L1 norm of the in-sweep residuals is reduced in a
+// fixed order (block partials, then one block), so the sweep count is
+// reproducible run to run.
+#include "ttfld_internal.cuh"
+
+namespace ttfld {
+
+// FILL_SOR_MATRIX ppsor.f:189-277 and B_VECTOR_BOUNDARIES ppsor.f:280-329,
+// one rank, poles=.false.
+int fill_sor_matrix(ttfld_ctx* c) {
+  Dev d = c->d;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    size_t q = cidx(d, i, j, k);
+    double e8 = d.E8[q];
+    double a = d.E7[q] + e8 * d.E16[q];
+    double b = -e8 * d.E2[q], cc = -e8 * d.E1[q], dd = -e8 * d.E4[q];
+    double e = -e8 * d.E3[q], f = -e8 * d.E6[q], g = -e8 * d.E5[q];
+    int ub = PA(UB, j, k);
+    bool ident = (i >= ub) || (i == d.nx) || (k == 1) || (k == d.nz);
+    if (ident) { a = 1.0; b = 0.0; cc = 0.0; dd = 0.0; e = 0.0; f = 0.0; g = 0.0; }
+    if (i == ub - 1) cc = 0.0;
+    if (i == d.nx - 1) cc = 0.0;
+    if (k == 2) f = 0.0;
+    if (k == d.nz - 1) g = 0.0;
+    d.SA[q] = a; d.SB[q] = b; d.SC[q] = cc; d.SD[q] = dd; d.SE[q] = e; d.SF[q] = f; d.SG[q] = g;
+    if (ident) d.RHS[q] = 0.0;
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// Sum |b| over the interior (RHSNORM, ppsor.f:33) and reset the solver state.
+__global__ void __launch_bounds__(kThreads) rhsnorm_kernel(Dev d, const double* b, double* partials) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const long long n = (long long)ncell(d);
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    acc += fabs(b[t]);
+  double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s;
+    __threadfence();
+    last = (atomicAdd(&d.sol->ticket2, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double tot = block_sum_array(partials, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      d.sol->rhsnorm = tot;
+      d.sol->ticket2 = 0;
+    }
+  }
+}
+
+// One colour of the red-black loop, ppsor.f:59-88 (COLOUR 0) and :107-136
+// (COLOUR 1), reference rounding.  x is a halo array.
+template <int COLOUR>
+__global__ void __launch_bounds__(kThreads) sor_exact_kernel(Dev d, double* __restrict__ x,
+                                                             const double* __restrict__ b, double omega,
+                                                             double* partials, int itmin, int itmax, double eps) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (solver_done(d)) return;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int nxh = (nx + 1) >> 1;
+  const long long n = (long long)nxh * ny * nz;
+  const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int h = (int)(t % nxh);
+    long long r = t / nxh;
+    int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    int i = 2 - ((j + k + COLOUR) & 1) + 2 * h;
+    if (i > nx) continue;
+    size_t c = cidx(d, i, j, k);
+    size_t q = hidx(d, i, j, k);
+    size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
+    size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
+    double xc = x[q];
+    double resid = d.SA[c] * xc + d.SB[c] * x[q - 1] + d.SC[c] * x[q + 1] + d.SD[c] * x[qjm] +
+                   d.SE[c] * x[qjp] + d.SF[c] * x[q - sk] + d.SG[c] * x[q + sk] - b[c];
+    acc = acc + fabs(resid);
+    x[q] = xc - omega * resid / d.SA[c];
+  }
+  double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    partials[COLOUR * kMaxPartials + blockIdx.x] = s;
+    if (COLOUR == 1) {
+      __threadfence();
+      last = (atomicAdd(&d.sol->ticket, 1u) == gridDim.x - 1);
+    }
+  }
+  if (COLOUR == 1) {
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      finalize_sweep(d, partials, gridDim.x, itmin, itmax, eps, sh);
+    }
+  }
+}
+
+// ||b - A x||_1 (FP64, reference operand order) into sol->true_l1.
+__global__ void __launch_bounds__(kThreads) resid_l1_kernel(Dev d, const double* __restrict__ x,
+                                                            const double* __restrict__ b, double* partials) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long n = (long long)nx * ny * nz;
+  const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % nx) + 1;
+    long long r = t / nx;
+    int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    size_t q = hidx(d, i, j, k);
+    size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
+    size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
+    double rr = d.SA[t] * x[q] + d.SB[t] * x[q - 1] + d.SC[t] * x[q + 1] + d.SD[t] * x[qjm] +
+                d.SE[t] * x[qjp] + d.SF[t] * x[q - sk] + d.SG[t] * x[q + sk] - b[t];
+    acc = acc + fabs(rr);
+  }
+  double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s;
+    __threadfence();
+    last = (atomicAdd(&d.sol->ticket2, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double tot = block_sum_array(partials, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      d.sol->true_l1 = tot;
+      d.sol->ticket2 = 0;
+    }
+  }
+}
+
+int rhs_norm(ttfld_ctx* c, const double* b, double* out_host) {
+  int nb = grid_for((long long)ncell(c->d));
+  if (nb > kMaxPartials) nb = kMaxPartials;
+  rhsnorm_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, b, c->partials);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  if (out_host) {
+    TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    *out_host = c->host_sol->rhsnorm;
+  }
+  return 0;
+}
+
+int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1) {
+  int nb = grid_for((long long)ncell(c->d));
+  if (nb > kMaxPartials) nb = kMaxPartials;
+  resid_l1_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, x, b, c->partials + kMaxPartials);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  if (l1) {
+    TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    *l1 = c->host_sol->true_l1;
+  }
+  return 0;
+}
+
+static int sweep_blocks(const Dev& d) {
+  long long n = (long long)((d.nx + 1) / 2) * d.ny * d.nz;
+  int nb = grid_for(n);
+  return nb > kMaxPartials ? kMaxPartials : nb;
+}
+
+int launch_exact_sweeps(ttfld_ctx* c, double* x, const double* b, int nsweeps, int itmin, int itmax,
+                               double eps) {
+  const int nb = sweep_blocks(c->d);
+  const double omega = c->d.sorparam;
+  for (int s = 0; s < nsweeps; ++s) {
+    sor_exact_kernel<0><<<nb, kThreads, 0, c->stream>>>(c->d, x, b, omega, c->partials, itmin, itmax, eps);
+    sor_exact_kernel<1><<<nb, kThreads, 0, c->stream>>>(c->d, x, b, omega, c->partials, itmin, itmax, eps);
+  }
+  count_launches(2 * nsweeps);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+static void fill_stats(ttfld_ctx* c, ttfld_solve_stats* st, int status) {
+  if (!st) return;
+  const SolverDev* h = c->host_sol;
+  st->sor_iter = h->iter;
+  st->rnorm = h->rnorm;
+  st->rhsnorm = h->rhsnorm;
+  st->status = status;
+}
+
+// Red-black SOR to the ppsor.f:161-177 rule.  The host checks the device
+// flag after chunks of sweeps; sweeps queued after the rule fired return at
+// once, so the iteration count is exactly the reference's.
+int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  int rc = rhs_norm(c, b, nullptr);
+  if (rc) return rc;
+  int chunk = 4, launched = 0;
+  for (;;) {
+    if ((rc = launch_exact_sweeps(c, x, b, chunk, itmin, itmax, c->d.epsmat))) return rc;
+    launched += chunk;
+    TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    if (c->host_sol->done) break;
+    if (launched >= itmax + 2) return TTFLD_E_CUDA;  // the rule must have fired by ITMAX
+    chunk = chunk < 128 ? chunk * 2 : 256;
+  }
+  if ((rc = halo_shift(c, x))) return rc;  // PLANETSHIFT(8) after the last colour
+  int status = c->host_sol->nonfinite ? TTFLD_E_NONFINITE : (c->host_sol->maxit ? TTFLD_MAXITER : TTFLD_OK);
+  fill_stats(c, st, status);
+  return status;
+}
+
+}  // namespace ttfld
+
+using namespace ttfld;
+
+namespace {
+
+int solve_current(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
+  switch (c->opts.solver) {
+    case TTFLD_SOLVER_SOR64_EXACT: return solve_exact64(c, x, b, itmin, itmax, st);
+    case TTFLD_SOLVER_SOR64_FAST: return solve_fast64(c, x, b, itmin, itmax, st);
+    case TTFLD_SOLVER_MIXED: return solve_mixed(c, x, b, st);
+  }
+  return TTFLD_E_ARGS;
+}
+
+}  // namespace
+
+namespace ttfld {
+// Solve A x = RHS_ER for DELTA_ER with the context's solver and guess.
+int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
+  Dev d = c->d;
+  ttfld_solve_stats local{};
+  if (!st) st = &local;
+  int fallback = 0;
+  TT_CHECK(cudaEventRecord(c->ev0, c->stream));
+  if (c->opts.guess == TTFLD_GUESS_ZERO || (c->opts.guess == TTFLD_GUESS_PREVIOUS && !c->have_prev) ||
+      (c->opts.guess == TTFLD_GUESS_LEARNED && !c->have_model)) {
+    if (c->opts.guess == TTFLD_GUESS_LEARNED && !c->have_model) return TTFLD_E_NOMODEL;
+    TT_CHECK(cudaMemsetAsync(d.DELTA_ER, 0, nhalo(d) * 8, c->stream));  // ppsor.f:29
+  } else {
+    // initial iterate in the interior; ghosts zero as in ppsor.f:29
+    double* x = d.DELTA_ER;
+    TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
+    double gl1 = 0.0, bl1 = 0.0;
+    if (c->opts.guess == TTFLD_GUESS_PREVIOUS) {
+      const double* px = c->prev_x;
+      const double sc = c->prev_scale;
+      launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+        size_t q = hidx(d, i, j, k);
+        x[q] = sc * px[q];
+      });
+      TT_CHECK_LAUNCH();
+    } else {
+      int rc = unet_guess(c, x, nullptr);
+      if (rc) return rc;
+    }
+    int rc = rhs_norm(c, d.RHS, &bl1);
+    if (rc) return rc;
+    if ((rc = true_residual(c, x, d.RHS, &gl1))) return rc;
+    st->guess_resid_l1 = gl1;
+    // fallback when the guess is no better than the zero guess (||b||_1)
+    if (!(gl1 < bl1)) {
+      TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
+      fallback = 1;
+    }
+  }
+  int rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
+  TT_CHECK(cudaEventRecord(c->ev1, c->stream));
+  TT_CHECK(cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_solve_ms = ms;
+  st->solve_ms = ms;
+  st->fallback = fallback;
+  if (rc < 0) return rc;
+  // keep this outer iteration's solution for the previous-solution guess
+  if (!c->prev_x) TT_CHECK(cudaMalloc((void**)&c->prev_x, nhalo(d) * 8));
+  TT_CHECK(cudaMemcpyAsync(c->prev_x, d.DELTA_ER, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
+  c->have_prev = 1;
+  if (fallback && rc == TTFLD_OK) rc = TTFLD_FALLBACK;
+  return rc;
+}
+}  // namespace ttfld
+
+extern "C" {
+
+int ttfld_fill_sor_matrix(ttfld_ctx* c) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = fill_sor_matrix(c);
+  if (rc) return rc;
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ttfld_sor_sweeps(ttfld_ctx* c, int n, double* rnorm, double* rhsnorm) {
+  if (!c || n < 0) return TTFLD_E_ARGS;
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  int rc = rhs_norm(c, c->d.RHS, nullptr);
+  if (rc) return rc;
+  // itmax beyond n so the rule never stops the requested sweeps
+  if ((rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, n, n + 1, n + 2, -1.0))) return rc;
+  if ((rc = halo_shift(c, c->d.DELTA_ER))) return rc;
+  TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  if (rnorm) *rnorm = c->host_sol->rnorm;
+  if (rhsnorm) *rhsnorm = c->host_sol->rhsnorm;
+  return c->host_sol->iter == n ? 0 : TTFLD_E_CUDA;
+}
+
+int ttfld_true_residual(ttfld_ctx* c, double* l1, double* rhs_l1) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = rhs_norm(c, c->d.RHS, rhs_l1);
+  if (rc) return rc;
+  double v = 0.0;
+  if ((rc = true_residual(c, c->d.DELTA_ER, c->d.RHS, &v))) return rc;
+  if (l1) *l1 = v;
+  return 0;
+}
+
+int ttfld_solve_system(ttfld_ctx* c, ttfld_solve_stats* st) {
+  if (!c) return TTFLD_E_ARGS;
+  return solve_delta_er(c, st);
+}
+
+int ttfld_solve_with_sor(ttfld_ctx* c, int print_max_values, ttfld_solve_stats* st) {
+  if (!c) return TTFLD_E_ARGS;
+  int rc = fill_sor_matrix(c);
+  if (rc) return rc;
+  rc = solve_delta_er(c, st);
+  if (rc == TTFLD_MAXITER && print_max_values) {
+    const SolverDev* h = c->host_sol;
+    printf("MAX COUPLED SOR ITERATION %8d %12.6e %12.6e %12.6e %12.6e\n", h->iter, h->ratio, h->rnorm,
+           h->rhsnorm, c->d.epsmat);
+  }
+  return rc;
+}
+
+int ttfld_adjust_sor_param(ttfld_ctx* c, double* out) {
+  if (!c) return TTFLD_E_ARGS;
+  int save_it[50];
+  double save_p[50];
+  double omega = (double)1.01f;  // ppsor.f:341, REAL*4 literal
+  int rc = fill_sor_matrix(c);
+  if (rc) return rc;
+  for (int n = 0; n < 50; ++n) {
+    c->d.sorparam = omega;
+    TT_CHECK(cudaMemsetAsync(c->d.DELTA_ER, 0, nhalo(c->d) * 8, c->stream));
+    rc = solve_exact64(c, c->d.DELTA_ER, c->d.RHS, 1, c->d.itmax, nullptr);
+    if (rc < 0) return rc;
+    save_it[n] = c->host_sol->iter;
+    save_p[n] = omega;
+    omega = omega + (double)0.02f;  // ppsor.f:346
+  }
+  int best = 0;
+  for (int n = 1; n < 50; ++n)
+    if (save_it[n] < save_it[best]) best = n;
+  c->d.sorparam = save_p[best];
+  c->params.sorparam = save_p[best];
+  if (out) *out = save_p[best];
+  return 0;
+}
+
+}  // extern "C"
+
+namespace ttfld {
+// DIFFUSION ppdif.f:1-167 with DIFFUSION_MAT_ELEM (:169-223),
+// DIFFUSION_COEF (:226-275) and FILL_DVALUES (:278-308): implicit diffusion
+// of the SCALAR field with the constant xnue/Pr_num, the same red-black
+// SOR with ITMIN=5 and SORITMAX=500 (ppdif.f:14-15), in place on SCALAR.
+static int diffusion(ttfld_ctx* c, ttfld_solve_stats* st) {
+  Dev d = c->d;
+  if (!(d.pr_num != 0.0)) return TTFLD_E_ARGS;
+  const double dconst = d.xnue / d.pr_num;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    size_t q = cidx(d, i, j, k);
+    d.RHS_DIF[q] = HA(SCALAR, i, j, k);
+    double dx1 = dconst / G(dxb, i + 1), dx2 = dconst / G(dxb, i);
+    double dy1 = dconst / (G(dyb, j + 1) * G(geoxg, i) * G(geozg, k));
+    double dy2 = dconst / (G(dyb, j) * G(geoxg, i) * G(geozg, k));
+    double dz1 = dconst / (G(dzb, k + 1) * G(geoxh, i));
+    double dz2 = dconst / (G(dzb, k) * G(geoxh, i));
+    double d1 = d.delt * G(surxa, i + 1) * dx1 / (G(surxb, i) * G(dxa, i));
+    double d2 = d.delt * G(surxa, i) * dx2 / (G(surxb, i) * G(dxa, i));
+    double d3 = d.delt * dy1 / (G(geoxg, i) * G(surzb, k) * G(dya, j));
+    double d4 = d.delt * dy2 / (G(geoxg, i) * G(surzb, k) * G(dya, j));
+    double d5 = d.delt * dz1 * G(surza, k + 1) / (G(geoxg, i) * G(surzb, k) * G(dza, k));
+    double d6 = d.delt * dz2 * G(surza, k) / (G(geoxg, i) * G(surzb, k) * G(dza, k));
+    double d16 = d1 + d2 + d3 + d4 + d5 + d6;
+    if (i == d.nx) {  // XMAX zero-gradient row, ppdif.f:212-220
+      d.SA[q] = 1.0 + d2; d.SB[q] = -d2; d.SC[q] = 0.0; d.SD[q] = 0.0;
+      d.SE[q] = 0.0; d.SF[q] = 0.0; d.SG[q] = 0.0;
+    } else {
+      d.SA[q] = 1.0 + d16; d.SB[q] = -d2; d.SC[q] = -d1; d.SD[q] = -d4;
+      d.SE[q] = -d3; d.SF[q] = -d6; d.SG[q] = -d5;
+    }
+  });
+  TT_CHECK_LAUNCH();
+  return solve_exact64(c, d.SCALAR, d.RHS_DIF, 5, 500, st);
+}
+}  // namespace ttfld
+
+extern "C" int ttfld_diffusion(ttfld_ctx* c, ttfld_solve_stats* st) {
+  if (!c) return TTFLD_E_ARGS;
+  return ttfld::diffusion(c, st);
+}

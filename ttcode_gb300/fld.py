@@ -1,0 +1,201 @@
+"""Host-side mirror of the reference's FLD subroutine interface.
+
+``FLD`` owns one libttfld context: the module arrays of the step live on the
+GPU and the methods are named after the Fortran subroutines they replace
+(SOLVE_WITH_SOR, FILL_EVALUES, DIFF, COUPLED_ENERGY_EQS, DIFFUSION, ...).
+Every call goes through the C ABI in include/ttfld.h; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import FIELDS, GUESS, SOLVER, check, lib
+from .grid import Grid
+
+HALO = ("T", "RH", "CV", "ER", "ER_OLD", "DELTA_ER", "XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT",
+        "DXKAPA_DT", "KMUL", "Q", "SCALAR")
+CELL = ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8", "EVAL_1_6",
+        "JACOB_ETA", "RHS_ER", "SOR_A", "SOR_B", "SOR_C", "SOR_D", "SOR_E", "SOR_F", "SOR_G",
+        "FQ", "FR", "DIVF", "DELTA_Q")
+
+
+def field_shape(name: str, nx: int, ny: int, nz: int):
+    if name in HALO:
+        return (nx + 4, ny + 4, nz + 4)
+    if name in CELL:
+        return (nx, ny, nz)
+    if name in ("FLIMX", "DIFRX", "FLUX_X"):
+        return (nx + 1, ny, nz)
+    if name in ("FLIMY", "DIFRY", "FLUX_Y"):
+        return (nx, ny + 1, nz)
+    if name in ("FLIMZ", "DIFRZ", "FLUX_Z"):
+        return (nx, ny, nz + 1)
+    if name in ("UPPERBND", "MU_STAR", "TINCIDENT"):
+        return (ny + 4, nz + 4)
+    if name == "STELLARINPUT":
+        return (nx, ny + 4, nz + 4)
+    if name in ("STELLARTAU", "DTAUS"):
+        return (nx + 1, ny + 4, nz + 4)
+    raise KeyError(name)
+
+
+def make_params(p: dict) -> _ffi.Params:
+    out = _ffi.Params()
+    for k, _ in _ffi.Params._fields_:
+        setattr(out, k, p[k])
+    return out
+
+
+class FLD:
+    """One device-resident FLD step (one rank's module arrays)."""
+
+    def __init__(self, grid: Grid, params: dict, device: int = 0):
+        self.L = lib()
+        self.grid = grid
+        self.nx, self.ny, self.nz = grid.nx, grid.ny, grid.nz
+        self.params = dict(params)
+        dims = _ffi.Dims(self.nx, self.ny, self.nz, 0)
+        self._metric_keep = {}
+        m = _ffi.Metrics()
+        for n in _ffi.METRIC_NAMES:
+            a = np.ascontiguousarray(grid.m[n], dtype=np.float64)
+            self._metric_keep[n] = a
+            setattr(m, n, a.ctypes.data_as(_ffi.P_double))
+        h = ctypes.c_void_p()
+        check("ttfld_create", self.L.ttfld_create(ctypes.byref(h), ctypes.byref(dims), ctypes.byref(m),
+                                                  ctypes.byref(make_params(self.params)), device))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ttfld_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- parameters -----------------------------------------------------
+    def set_params(self, **kw):
+        self.params.update(kw)
+        check("ttfld_set_params", self.L.ttfld_set_params(self.h, ctypes.byref(make_params(self.params))))
+
+    def set_solver(self, solver: str = "sor64_exact", guess: str = "zero", tol: float = 1e-10,
+                   inner_min: int = 8, inner_max: int = 256, max_sweeps: int = 0):
+        o = _ffi.SolveOpts(SOLVER[solver], GUESS[guess], tol, inner_min, inner_max, max_sweeps, 0)
+        check("ttfld_set_solver", self.L.ttfld_set_solver(self.h, ctypes.byref(o)))
+
+    # ---- module arrays ----------------------------------------------------
+    def upload(self, name: str, arr):
+        shp = field_shape(name, self.nx, self.ny, self.nz)
+        dt = np.int32 if name == "UPPERBND" else np.float64
+        a = np.asfortranarray(np.asarray(arr, dtype=dt))
+        if a.shape != shp:
+            raise ValueError(f"{name}: shape {a.shape} != {shp}")
+        check(f"upload {name}", self.L.ttfld_upload(self.h, FIELDS[name], a.ctypes.data_as(ctypes.c_void_p)))
+
+    def download(self, name: str) -> np.ndarray:
+        shp = field_shape(name, self.nx, self.ny, self.nz)
+        dt = np.int32 if name == "UPPERBND" else np.float64
+        a = np.empty(shp, dtype=dt, order="F")
+        check(f"download {name}", self.L.ttfld_download(self.h, FIELDS[name], a.ctypes.data_as(ctypes.c_void_p)))
+        return a
+
+    def load_shell(self, shell):
+        for n, a in shell.fields.items():
+            self.upload(n, a)
+
+    # ---- the reference subroutines ---------------------------------------
+    def bounds(self):
+        check("BOUNDS", self.L.ttfld_bounds(self.h))
+
+    def kappa(self):
+        check("KAPPA", self.L.ttfld_kappa(self.h))
+
+    def stellarinput_heating(self):
+        check("STELLARINPUT_HEATING", self.L.ttfld_stellarinput_heating(self.h))
+
+    def diff(self, energy_iter: int = 0):
+        check("DIFF", self.L.ttfld_diff(self.h, energy_iter))
+
+    def calculateflux(self, energy_iter: int = 0):
+        check("CALCULATEFLUX", self.L.ttfld_calculateflux(self.h, energy_iter))
+
+    def fill_evalues(self, theta: float = 1.0):
+        check("FILL_EVALUES", self.L.ttfld_fill_evalues(self.h, theta))
+
+    def fill_sor_matrix(self):
+        check("FILL_SOR_MATRIX", self.L.ttfld_fill_sor_matrix(self.h))
+
+    def solve_with_sor(self, print_max_values: bool = True) -> _ffi.SolveStats:
+        st = _ffi.SolveStats()
+        check("SOLVE_WITH_SOR", self.L.ttfld_solve_with_sor(self.h, int(print_max_values), ctypes.byref(st)),
+              ok=(0, 1, 2))
+        return st
+
+    def solve_system(self) -> _ffi.SolveStats:
+        st = _ffi.SolveStats()
+        check("solve_system", self.L.ttfld_solve_system(self.h, ctypes.byref(st)), ok=(0, 1, 2))
+        return st
+
+    def sor_sweeps(self, n: int):
+        r, b = ctypes.c_double(), ctypes.c_double()
+        check("sor_sweeps", self.L.ttfld_sor_sweeps(self.h, n, ctypes.byref(r), ctypes.byref(b)))
+        return r.value, b.value
+
+    def true_residual(self):
+        r, b = ctypes.c_double(), ctypes.c_double()
+        check("true_residual", self.L.ttfld_true_residual(self.h, ctypes.byref(r), ctypes.byref(b)))
+        return r.value, b.value
+
+    def adjust_sor_param(self) -> float:
+        w = ctypes.c_double()
+        check("ADJUST_SOR_PARAM", self.L.ttfld_adjust_sor_param(self.h, ctypes.byref(w)))
+        self.params["sorparam"] = w.value
+        return w.value
+
+    def coupled_energy_eqs(self, do_bounds: bool = True) -> _ffi.StepStats:
+        st = _ffi.StepStats()
+        check("COUPLED_ENERGY_EQS", self.L.ttfld_coupled_energy_eqs(self.h, int(do_bounds), ctypes.byref(st)),
+              ok=(0, 1, 2))
+        return st
+
+    def diffusion(self) -> _ffi.SolveStats:
+        st = _ffi.SolveStats()
+        check("DIFFUSION", self.L.ttfld_diffusion(self.h, ctypes.byref(st)), ok=(0, 1))
+        return st
+
+    def stream_ptr(self) -> int:
+        """The cudaStream_t the library issues this context's work on."""
+        return int(self.L.ttfld_stream(self.h))
+
+    def time_sweeps(self, solver: str, n: int) -> float:
+        ms = ctypes.c_double()
+        check("time_sweeps", self.L.ttfld_time_sweeps(self.h, SOLVER[solver], n, ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        check("synchronize", self.L.ttfld_synchronize(self.h))
+
+
+def start_run(shell, device: int = 0) -> FLD:
+    """Context loaded with a synthetic shell and the initial BOUNDS/KAPPA of
+    the driver's set-up (pp.f:419-463): BOUNDS at III=0, then KAPPA."""
+    f = FLD(shell.grid, shell.params, device)
+    f.load_shell(shell)
+    f.set_params(iii=0)
+    f.bounds()
+    f.kappa()
+    f.set_params(iii=shell.params.get("iii", 1))
+    return f
