@@ -71,7 +71,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
         return self
@@ -130,6 +130,19 @@ def build_system(device):
 
 def flush_l2(torch, buf):
     buf.add_(1.0)  # 256 MB written: larger than the 126 MB L2
+
+
+def run_profile_solve(args):
+    """One product-path solve and one exact FP64 solve of the shell256
+    system, nothing else (the command the ncu summaries under profiles/ use)."""
+    import torch
+    torch.cuda.set_device(0)
+    sh, f = build_system(0)
+    for solver in ("mixed", "sor64_exact"):
+        f.set_solver(solver, tol=1e-10, inner_min=16, inner_max=512)
+        st = f.solve_system()
+        print(json.dumps({"solver": solver, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
+    f.close()
 
 
 def run_gpu(args):
@@ -366,11 +379,16 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="only build the system and run one mixed and one exact FP64 solve")
     args = ap.parse_args()
+    if args.profile_solve:
+        run_profile_solve(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -237,7 +237,8 @@ int ttfld_adjust_sor_param(ttfld_ctx* ctx, double* sorparam);
 int ttfld_coupled_energy_eqs(ttfld_ctx* ctx, int do_bounds,
                              ttfld_step_stats* stats);
 /* DIFFUSION(scalar), ppdif.f:1-167, on the SCALAR field (the pass_sc
- * module array) with diffusion constant xnue/pr_num. */
+ * module array) with diffusion constant xnue/pr_num.  As at the reference's
+ * call sites, SCALAR's phi halo must be current (PLANETSHIFT(10)) on entry. */
 int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
 
 /* ---- measurement (no reference counterpart) --------------------------- */

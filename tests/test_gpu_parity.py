@@ -188,6 +188,8 @@ def test_diffusion_parity(small):
     rng = np.random.default_rng(7)
     s = np.asfortranarray(1.0 + rng.random((nx + 4, ny + 4, nz + 4)))
     o.f("SCALAR")[...] = s
+    o.call("planetshift", "SCALAR")   # callers pass an exchanged phi halo
+    s = o.f("SCALAR").copy()
     o.set("pr_num", 1.0)
     o.set("xnue", 1.0e15)
     f.set_params(pr_num=1.0, xnue=1.0e15)

@@ -47,6 +47,7 @@ static Cmp make_cmp(const Dev& d) {
 struct Mix32 {
   float* a[6][2];   // W E S N B T (xm xp jm jp km kp) over A, per colour
   float* ainv[2];   // 1/A
+  float* diag[2];   // A (for the in-sweep residual norm)
   float* rhat[2];   // r / A
   float* e[2];      // correction, with theta ghost planes
 };
@@ -87,7 +88,7 @@ static int ensure32(ttfld_ctx* c) {
   MixWork* w = work(c);
   if (w->have32) return 0;
   const Cmp& g = w->g;
-  size_t n = 2 * (6 + 2) * g.csz + 2 * g.gsz;
+  size_t n = 2 * (6 + 3) * g.csz + 2 * g.gsz;
   float* p = nullptr;
   TT_CHECK(cudaMalloc((void**)&p, n * sizeof(float)));
   TT_CHECK(cudaMemset(p, 0, n * sizeof(float)));
@@ -95,6 +96,7 @@ static int ensure32(ttfld_ctx* c) {
   for (int q = 0; q < 6; ++q)
     for (int col = 0; col < 2; ++col) { w->m32.a[q][col] = p; p += g.csz; }
   for (int col = 0; col < 2; ++col) { w->m32.ainv[col] = p; p += g.csz; }
+  for (int col = 0; col < 2; ++col) { w->m32.diag[col] = p; p += g.csz; }
   for (int col = 0; col < 2; ++col) { w->m32.rhat[col] = p; p += g.csz; }
   for (int col = 0; col < 2; ++col) { w->m32.e[col] = p; p += g.gsz; }
   w->have32 = 1;
@@ -148,6 +150,7 @@ static int prep32(ttfld_ctx* c) {
     m.a[4][col][s] = (float)(d.SF[q] * inv);
     m.a[5][col][s] = (float)(d.SG[q] * inv);
     m.ainv[col][s] = (float)inv;
+    m.diag[col][s] = (float)d.SA[q];
   });
   TT_CHECK_LAUNCH();
   return 0;
@@ -157,14 +160,23 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
 // One colour of FP32 red-black SOR on A e = r (Jacobi-scaled), 4 cells per
-// thread.  e_new = e + omega * ((rhat - sum a_nb e_nb) - e).
-template <int COL>
-__global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega) {
+// thread: res = (e + sum a_nb e_nb) - rhat (the reference's in-sweep residual
+// divided by A, ppsor.f:64-71), e -= omega * res.  NORM sweeps also sum
+// |A * res| in FP64, i.e. the reference's RNORM (ppsor.f:73) of the iterate
+// x + e, and the last block of the second colour stops the inner loop once
+// RNORM / RHSNORM <= stop_ratio.  Sweeps queued after that return at once.
+template <int COL, bool NORM>
+__global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                           double* partials, double stop_ratio) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (*(volatile int*)&sol->done) return;
   const int nv = g.nxp >> 2;
   const long long n = g.rows * nv;
   const float* __restrict__ eo = m.e[1 - COL];
   float* __restrict__ es = m.e[COL];
   const size_t plane = (size_t)g.ny * g.nxp;
+  double nacc = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int hv = (int)(t % nv);
     const long long rr = t / nv;
@@ -194,21 +206,49 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
     const float4 as = ld4(m.a[2][COL] + cb), an = ld4(m.a[3][COL] + cb);
     const float4 ab = ld4(m.a[4][COL] + cb), at = ld4(m.a[5][COL] + cb);
     const float4 r = ld4(m.rhat[COL] + cb);
+    float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (NORM) dg = ld4(m.diag[COL] + cb);
     float4 out;
-#define UPD(L, XM, XP)                                                                 \
-  {                                                                                    \
-    float acc = fmaf(aw.L, XM, fmaf(ae.L, XP, fmaf(as.L, s.L, fmaf(an.L, nn.L,         \
-                fmaf(ab.L, b.L, at.L * tt.L)))));                                      \
-    float v = fmaf(omega, (r.L - acc) - e.L, e.L);                                     \
-    out.L = (h0 + L##_IDX < ncol) ? v : 0.f;                                           \
+#define UPD(L, IDX, XM, XP)                                                                \
+  {                                                                                        \
+    float acc = fmaf(aw.L, XM, fmaf(ae.L, XP, fmaf(as.L, s.L, fmaf(an.L, nn.L,             \
+                fmaf(ab.L, b.L, at.L * tt.L)))));                                          \
+    float res = (e.L + acc) - r.L;                                                         \
+    bool ok = h0 + IDX < ncol;                                                             \
+    out.L = ok ? fmaf(-omega, res, e.L) : 0.f;                                             \
+    if (NORM && ok) nacc += fabs((double)(dg.L * res));                                    \
   }
-#define x_IDX 0
-#define y_IDX 1
-#define z_IDX 2
-#define w_IDX 3
-    UPD(x, xm0, xp0) UPD(y, xm1, xp1) UPD(z, xm2, xp2) UPD(w, xm3, xp3)
+    UPD(x, 0, xm0, xp0) UPD(y, 1, xm1, xp1) UPD(z, 2, xm2, xp2) UPD(w, 3, xm3, xp3)
 #undef UPD
     st4(es + eb, out);
+  }
+  if (COL == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&sol->iter, 1);
+  if (NORM) {
+    double sb = block_sum(nacc, sh);
+    if (threadIdx.x == 0) {
+      partials[COL * kMaxPartials + blockIdx.x] = sb;
+      if (COL == 1) {
+        __threadfence();
+        last = (atomicAdd(&sol->ticket, 1u) == gridDim.x - 1);
+      }
+    }
+    if (COL == 1) {
+      __syncthreads();
+      if (last) {
+        __threadfence();
+        double r0 = block_sum_array(partials, gridDim.x, sh);
+        double r1 = block_sum_array(partials + kMaxPartials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+          double rnorm = r0 + r1;
+          double ratio = rnorm / sol->rhsnorm;
+          sol->rnorm = rnorm;
+          sol->ratio = ratio;
+          if (!isfinite(rnorm)) { sol->nonfinite = 1; sol->done = 1; }
+          else if (!(ratio > stop_ratio)) sol->done = 1;
+          sol->ticket = 0;
+        }
+      }
+    }
   }
 }
 
@@ -288,21 +328,40 @@ static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
   return 0;
 }
 
-int launch_sweeps32(ttfld_ctx* c, int nsweeps) {
+// Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
+// evaluates the in-sweep norm against stop_ratio.
+int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0) {
   MixWork* w = work(c);
   const Cmp& g = w->g;
   long long nvec = g.rows * (g.nxp >> 2);
   int nb = grid_for(nvec);
+  if (nb > kMaxPartials) nb = kMaxPartials;
   float omega = (float)c->d.sorparam;
-  for (int s = 0; s < nsweeps; ++s) {
-    sweep32_kernel<0><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega);
-    sweep32_kernel<1><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega);
+  for (int s = 1; s <= nsweeps; ++s) {
+    bool norm = norm_every > 0 && (s % norm_every == 0 || s == nsweeps);
+    if (norm) {
+      sweep32_kernel<0, true><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, true><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+    } else {
+      sweep32_kernel<0, false><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, false><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+    }
   }
   count_launches(2 * nsweeps);
   TT_CHECK_LAUNCH();
   return 0;
 }
 
+static int poll(ttfld_ctx* c) {
+  TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// Defect correction: anchor r = b - A x in FP64, run FP32 sweeps on
+// A e = r until the in-sweep norm of x + e has dropped by 1e-5 relative to
+// the anchor (well inside FP32 precision) or reached tol, x += e, repeat;
+// stop when the FP64 ||b - A x||_1 / ||b||_1 <= tol.
 int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st) {
   int rc;
   if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
@@ -311,45 +370,58 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st)
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   double bl1 = 0.0, l1 = 0.0;
   if ((rc = rhs_norm(c, b, &bl1))) return rc;
-  if ((rc = resid32(c, x, b, &l1))) return rc;
   const double tol = c->opts.tol;
-  const int imin = c->opts.inner_min, imax = c->opts.inner_max;
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : 100LL * c->d.itmax;
-  long long total = 0;
-  int corrections = 0, stall = 0, status = TTFLD_OK;
-  int m = imin;
-  double prev = l1;
-  while (l1 > tol * bl1) {
-    if (!isfinite(l1)) { status = TTFLD_E_NONFINITE; break; }
-    if (total >= budget || stall >= 3) { status = TTFLD_MAXITER; break; }
-    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
-    if ((rc = launch_sweeps32(c, m))) return rc;
-    total += m;
-    if ((rc = add_correction(c, x))) return rc;
+  const int period = 8;
+  int corrections = 0, status = TTFLD_OK;
+  double tight = 1.0;  // halved each time the in-sweep norm met tol but the FP64 residual did not
+  bool hit_tol = false;
+  for (;;) {
     if ((rc = resid32(c, x, b, &l1))) return rc;
     ++corrections;
-    double rate = (prev > 0.0 && l1 > 0.0) ? pow(l1 / prev, 1.0 / m) : 0.0;
-    if (l1 < prev) {
-      stall = 0;
-      double need = (rate > 0.0 && rate < 1.0) ? log(tol * bl1 / l1) / log(rate) : (double)imin;
-      double nm = ceil(need * 1.05) + 1.0;
-      m = (int)(nm < imin ? imin : (nm > imax ? imax : nm));
-    } else {
-      ++stall;
-      m = imax;
+    if (!isfinite(l1)) { status = TTFLD_E_NONFINITE; break; }
+    if (!(l1 > tol * bl1)) break;
+    if (hit_tol) tight *= 0.5;
+    if (c->host_sol->iter >= budget) { status = TTFLD_MAXITER; break; }
+    const double anchor = l1 / bl1;
+    const double stop = fmax(tol * tight, anchor * 1e-5);
+    hit_tol = stop <= tol;
+    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
+    TT_CHECK(cudaMemsetAsync(&c->sol->done, 0, sizeof(int), c->stream));
+    int it0 = c->host_sol->iter;
+    double r_prev = anchor;
+    int it_prev = it0;
+    int chunk = 32;
+    for (;;) {
+      if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop))) return rc;
+      if ((rc = poll(c))) return rc;
+      const SolverDev* h = c->host_sol;
+      if (h->nonfinite) { status = TTFLD_E_NONFINITE; break; }
+      if (h->done || h->iter >= budget) break;
+      // predict the sweeps left from the last two norms; queue about that many
+      double rate = (h->iter > it_prev && h->ratio > 0.0 && r_prev > 0.0)
+                        ? pow(h->ratio / r_prev, 1.0 / (h->iter - it_prev)) : 0.0;
+      double left = (rate > 0.0 && rate < 1.0) ? log(stop / h->ratio) / log(rate) : 64.0;
+      r_prev = h->ratio;
+      it_prev = h->iter;
+      if (left <= period) chunk = (int)ceil(left) < 1 ? 1 : (int)ceil(left);
+      else if (left < 64) chunk = ((int)left / period) * period;
+      else chunk = left < 512 ? ((int)(0.75 * left) / period) * period : 384;
+      if (chunk < 1) chunk = 1;
     }
-    prev = l1;
+    if (status < 0) break;
+    if (c->host_sol->iter == it0) { status = TTFLD_MAXITER; break; }  // no progress possible
+    if ((rc = add_correction(c, x))) return rc;
   }
   if ((rc = halo_shift(c, x))) return rc;
   if (st) {
-    st->sor_iter = (int)total;
+    st->sor_iter = c->host_sol->iter;
     st->corrections = corrections;
     st->rhsnorm = bl1;
     st->rnorm = l1;
     st->true_resid_l1 = l1;
     st->status = status;
   }
-  c->host_sol->iter = (int)total;
   return status;
 }
 
