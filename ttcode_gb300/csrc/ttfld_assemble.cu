@@ -34,21 +34,16 @@ __device__ __forceinline__ double kap_formula(const Dev& d, double t, double rh,
 static int kappa(ttfld_ctx* c) {
   Dev d = c->d;
   if (d.kappa_model == 1) return 0;  // prescribed opacities: KAPPA is the caller's
-  launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
+  // One thread per cell: the cells from UPPERBND up end with the value of
+  // UPPERBND-1, which each of them evaluates itself (same inputs, same bits).
+  launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
     int ub = PA(UB, j, k);
     if (ub < 1 || ub > d.nx + 1) return;
-    for (int i = -1; i <= ub; ++i) {
-      size_t q = hidx(d, i, j, k);
-      double kr = kap_formula(d, d.T[q], d.RH[q], d.KMUL[q]);
-      d.XKAPR[q] = kr; d.XKAPP[q] = kr; d.XKAPA[q] = kr;
-      d.DXKAPP[q] = 0.0; d.DXKAPA[q] = 0.0;
-    }
-    size_t s = hidx(d, ub - 1, j, k);
-    for (int i = ub; i <= d.nx + 2; ++i) {
-      size_t q = hidx(d, i, j, k);
-      d.XKAPR[q] = d.XKAPR[s]; d.XKAPP[q] = d.XKAPP[s]; d.XKAPA[q] = d.XKAPA[s];
-      d.DXKAPP[q] = d.DXKAPP[s]; d.DXKAPA[q] = d.DXKAPA[s];
-    }
+    size_t s = hidx(d, i < ub ? i : ub - 1, j, k);
+    size_t q = hidx(d, i, j, k);
+    double kr = kap_formula(d, d.T[s], d.RH[s], d.KMUL[s]);
+    d.XKAPR[q] = kr; d.XKAPP[q] = kr; d.XKAPA[q] = kr;
+    d.DXKAPP[q] = 0.0; d.DXKAPA[q] = 0.0;
   });
   TT_CHECK_LAUNCH();
   return 0;

@@ -162,7 +162,8 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 // One colour of FP32 red-black SOR on A e = r (Jacobi-scaled), 4 cells per
 // thread: res = (e + sum a_nb e_nb) - rhat (the reference's in-sweep residual
 // divided by A, ppsor.f:64-71), e -= omega * res.  NORM sweeps also sum
-// |A * res| in FP64, i.e. the reference's RNORM (ppsor.f:73) of the iterate
+// |A * res| (per thread in FP32, per block and grid in FP64 in a fixed
+// order), i.e. the reference's RNORM (ppsor.f:73) of the iterate
 // x + e, and the last block of the second colour stops the inner loop once
 // RNORM / RHSNORM <= stop_ratio.  Sweeps queued after that return at once.
 template <int COL, bool NORM>
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
   const float* __restrict__ eo = m.e[1 - COL];
   float* __restrict__ es = m.e[COL];
   const size_t plane = (size_t)g.ny * g.nxp;
-  double nacc = 0.0;
+  float nacc = 0.f;  // per-thread partial (a few cells): FP32, widened once below
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int hv = (int)(t % nv);
     const long long rr = t / nv;
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
     float res = (e.L + acc) - r.L;                                                         \
     bool ok = h0 + IDX < ncol;                                                             \
     out.L = ok ? fmaf(-omega, res, e.L) : 0.f;                                             \
-    if (NORM && ok) nacc += fabs((double)(dg.L * res));                                    \
+    if (NORM && ok) nacc += fabsf(dg.L * res);                                            \
   }
     UPD(x, 0, xm0, xp0) UPD(y, 1, xm1, xp1) UPD(z, 2, xm2, xp2) UPD(w, 3, xm3, xp3)
 #undef UPD
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
   }
   if (COL == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&sol->iter, 1);
   if (NORM) {
-    double sb = block_sum(nacc, sh);
+    double sb = block_sum((double)nacc, sh);
     if (threadIdx.x == 0) {
       partials[COL * kMaxPartials + blockIdx.x] = sb;
       if (COL == 1) {
@@ -328,14 +329,31 @@ static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
   return 0;
 }
 
+// Grid of whole waves: the blocks that fit on the SMs at once (occupancy of
+// the kernel), walking the rest of the items by grid stride, so the last
+// wave of a short streaming kernel is never a partial one.
+template <class K>
+static int wave_grid(K kernel, long long items) {
+  static int per_wave = 0;
+  if (per_wave == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+    per_wave = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 4);
+    if (per_wave > kMaxPartials) per_wave = kMaxPartials;
+  }
+  long long need = (items + kThreads - 1) / kThreads;
+  return (int)(need < per_wave ? (need < 1 ? 1 : need) : per_wave);
+}
+
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
 // evaluates the in-sweep norm against stop_ratio.
 int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0) {
   MixWork* w = work(c);
   const Cmp& g = w->g;
   long long nvec = g.rows * (g.nxp >> 2);
-  int nb = grid_for(nvec);
-  if (nb > kMaxPartials) nb = kMaxPartials;
+  int nb = wave_grid(sweep32_kernel<1, true>, nvec);
   float omega = (float)c->d.sorparam;
   for (int s = 1; s <= nsweeps; ++s) {
     bool norm = norm_every > 0 && (s % norm_every == 0 || s == nsweeps);

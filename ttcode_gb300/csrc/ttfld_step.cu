@@ -116,14 +116,20 @@ static int jacobian(ttfld_ctx* c, double theta) {
 // Algebraic delta Q with the positivity guard and the two max-norms
 // (ppenergy.f:379-541), fused with the damped update of :551-573 (each cell
 // reads only its own Q and E_R, which only it updates).
-static int delta_q_update(ttfld_ctx* c, double theta, double conv) {
-  Dev d = c->d;
-  launch_box(c->stream, box(2, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+__global__ void __launch_bounds__(kThreads) delta_q_kernel(Dev d, double theta, double conv) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long n = (long long)(nx - 1) * ny * nz;  // i = 2..NX
+  const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
+  const double* x = d.DELTA_ER;
+  double mq = 0.0, me = 0.0;
+  int bad = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i = 2 + (int)(t % (nx - 1));
+    long long r = t / (nx - 1);
+    int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
     int xmax_index = PA(UB, j, k) - 1;
-    if (i > xmax_index || xmax_index > d.nx) return;
+    if (i > xmax_index || xmax_index > nx) continue;
     size_t h = hidx(d, i, j, k), q = cidx(d, i, j, k);
-    const size_t sj = (size_t)(d.nx + 4), sk = (size_t)(d.nx + 4) * (d.ny + 4);
-    const double* x = d.DELTA_ER;
     double q1 = -d.delt * (1.0 - theta);
     double q2 = d.delt * d.RH[h] * d.XKAPP[h] * TT_FD;
     double dq = (1.0 / d.DFQ[q]) *
@@ -132,12 +138,29 @@ static int delta_q_update(ttfld_ctx* c, double theta, double conv) {
                  q1 * d.E6[q] * x[h - sk] + q2 * x[h] - d.FQ[q]);
     d.DQ[q] = dq;
     double qv = d.Q[h], erv = d.ER[h];
-    if ((qv + conv * dq) <= 0.0) d.stp->nonpositive_q = 1;
-    atomic_max_nonneg(&d.stp->maxq_bits, fabs(dq / qv));
-    atomic_max_nonneg(&d.stp->maxer_bits, fabs(x[h] / erv));
+    if ((qv + conv * dq) <= 0.0) bad = 1;
+    mq = fmax(mq, fabs(dq / qv));
+    me = fmax(me, fabs(x[h] / erv));
     d.ER[h] = erv + conv * x[h];
     d.Q[h] = qv + conv * dq;
-  });
+  }
+  // max is exact in any order: reduce in the warp, one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    mq = fmax(mq, __shfl_xor_sync(0xffffffffu, mq, o));
+    me = fmax(me, __shfl_xor_sync(0xffffffffu, me, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_nonneg(&d.stp->maxq_bits, mq);
+    atomic_max_nonneg(&d.stp->maxer_bits, me);
+    if (bad) d.stp->nonpositive_q = 1;
+  }
+}
+
+static int delta_q_update(ttfld_ctx* c, double theta, double conv) {
+  const Dev& d = c->d;
+  delta_q_kernel<<<grid_for((long long)(d.nx - 1) * d.ny * d.nz), kThreads, 0, c->stream>>>(d, theta, conv);
+  count_launches(1);
   TT_CHECK_LAUNCH();
   return 0;
 }
