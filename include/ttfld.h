@@ -256,6 +256,35 @@ uint64_t ttfld_kernel_launches(void);
 int ttfld_guess_load(ttfld_ctx* ctx, const void* blob, size_t bytes);
 int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
 
+/* ---- solve without any allocation ------------------------------------- */
+/* No counterpart in the reference.  The FP64 red-black SOR solve of
+ * SOLVE_WITH_SOR (the same iterate, bit for bit, and the same stopping rule
+ * as ttfld_solve_with_sor with TTFLD_SOLVER_SOR64_EXACT) on arrays the caller
+ * already holds on the device, with no context and no device allocation.
+ * It is for callers that cannot let a library call cudaMalloc: hosts whose
+ * device memory is all managed by their own pool or offload data region,
+ * jobs held to a fixed memory budget beside other work on the GPU, and codes
+ * that must not have a hidden allocation or free synchronise the device
+ * under their running kernels.
+ *   sor_a..sor_g, rhs : device pointers, cell layout (1:NX,1:NY,1:NZ)
+ *   x                 : device pointer, halo layout (-1:NX+2,-1:NY+2,-1:NZ+2);
+ *                       holds the initial iterate and the fixed ghost
+ *                       values, returns the solution with its phi halo
+ *                       refreshed as PLANETSHIFT(8) does
+ *   stream            : the cudaStream_t to run on (NULL = default stream)
+ * Its only working memory is one fixed __device__ array of 2 MiB + 256 B
+ * that every GPU loading the library keeps until the process exits; grids
+ * with NY*NZ > 131072 are rejected with TTFLD_E_ARGS.  All calls on a device
+ * share that array (each clears what it needs at its start), so calls whose
+ * GPU work overlaps race and must be serialised by the caller.  The first
+ * call on a device looks up the array's device address; make that first call
+ * before any stream capture.  NY must be even. */
+int ttfld_sor_solve_noalloc(const double* sor_a, const double* sor_b, const double* sor_c,
+                            const double* sor_d, const double* sor_e, const double* sor_f,
+                            const double* sor_g, const double* rhs, double* x, int nx, int ny,
+                            int nz, double omega, double epsmat, int itmin, int itmax,
+                            void* stream, int* sor_iter, double* rnorm, double* rhsnorm);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

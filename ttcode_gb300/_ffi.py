@@ -88,7 +88,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_solve_with_sor", "ttfld_solve_system", "ttfld_sor_sweeps",
            "ttfld_true_residual", "ttfld_adjust_sor_param", "ttfld_coupled_energy_eqs",
            "ttfld_diffusion", "ttfld_guess_load", "ttfld_guess_save", "ttfld_time_sweeps",
-           "ttfld_kernel_launches")
+           "ttfld_kernel_launches", "ttfld_sor_solve_noalloc")
 
 _lib = None
 
@@ -143,6 +143,8 @@ def lib():
     L.ttfld_time_sweeps.argtypes = [vp, ctypes.c_int, ctypes.c_int, P_double]
     L.ttfld_kernel_launches.restype = ctypes.c_uint64
     L.ttfld_kernel_launches.argtypes = []
+    L.ttfld_sor_solve_noalloc.argtypes = [vp] * 9 + [ctypes.c_int] * 3 + [ctypes.c_double] * 2 + \
+        [ctypes.c_int] * 2 + [vp, ctypes.POINTER(ctypes.c_int), P_double, P_double]
     L.ttfld_guess_load.argtypes = [vp, vp, ctypes.c_size_t]
     L.ttfld_guess_save.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     _lib = L
