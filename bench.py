@@ -107,10 +107,15 @@ class ClockSampler:
 
 
 def load_traffic():
-    p = os.path.join(ROOT, "profiles", "sweep32_shell256_traffic.json")
+    """DRAM bytes (read + write) of one sweep32 launch from the committed ncu
+    summary, doubled for the two colours of one sweep (the unit of
+    `achieved`)."""
+    p = os.path.join(ROOT, "profiles", "sweep32_shell256.md")
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f).get("bytes_per_launch")
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return 2 * int(line.split(":")[1])
     return None
 
 
