@@ -126,7 +126,9 @@ enum ttfld_solver {
 
 enum ttfld_guess {
   TTFLD_GUESS_ZERO = 0,     /* delta_ER = 0 (ppsor.f:29)                   */
-  TTFLD_GUESS_PREVIOUS = 1, /* (1-conv_parm) * previous outer solution      */
+  TTFLD_GUESS_PREVIOUS = 1, /* the previous solve's solution: times
+                               (1-conv_parm) inside a step, as is from one
+                               step to the next                           */
   TTFLD_GUESS_LEARNED = 2   /* 3-D conv net prediction, zero-guess fallback  */
 };
 
@@ -137,7 +139,12 @@ typedef struct {
   int32_t inner_min;   /* mixed solver: FP32 sweeps per correction, bounds */
   int32_t inner_max;
   int32_t max_sweeps;  /* mixed solver sweep budget (0 = 100*ITMAX)        */
-  int32_t reserved;
+  int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:
+                            0 = the residual ||b - A x||_1 after one
+                                red-black sweep from it is not below the
+                                residual after one sweep from zero;
+                            1 = never;
+                            2 = ||b - A x0||_1 >= ||b||_1                  */
 } ttfld_solve_opts;
 
 typedef struct {
@@ -151,6 +158,8 @@ typedef struct {
   double guess_resid_l1;   /* ||b - A x0||_1 of the initial guess          */
   double solve_ms;         /* device time of the solve (CUDA events on the
                               library's stream, guess included)           */
+  double guess_ms;         /* of which: making and checking the initial
+                              guess (network inference, fallback test)    */
 } ttfld_solve_stats;
 
 typedef struct {
@@ -252,7 +261,31 @@ int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 uint64_t ttfld_kernel_launches(void);
 
 /* ---- learned initial guess (no reference counterpart) ----------------- */
-/* Load / export the conv-net weights (flat BF16 blob, see ttfld_unet.h). */
+/* A 3-D U-Net (4 levels, 16-32-64-64 channels, 3x3x3 kernels, BF16 weights
+ * and activations, FP32 accumulation on the tensor cores) maps the state of
+ * a solve -- log E, log kappa_R, log rho, log dt and the heating -- to
+ * delta_ER / E, used as SOLVE_WITH_SOR's initial iterate (TTFLD_GUESS_LEARNED).
+ * It is trained on the GPU on pairs captured from this context's own solves. */
+/* Random (seeded, He-normal) weights for this context's grid. */
+int ttfld_guess_init(ttfld_ctx* ctx, uint64_t seed);
+/* Device storage for up to `capacity` training pairs (5 BF16 inputs, a BF16
+ * target and a mask per cell; about 13 B per cell and pair). */
+int ttfld_guess_dataset(ttfld_ctx* ctx, int capacity);
+/* Store the next solve of this context (its starting state and its answer)
+ * as a training pair. */
+int ttfld_guess_capture_next(ttfld_ctx* ctx);
+int ttfld_guess_dataset_count(ttfld_ctx* ctx);
+/* Adam (lr, beta 0.9/0.999) over the stored pairs, `epochs` seeded passes;
+ * mean masked MSE of the normalised target over the steps in *mean_loss. */
+int ttfld_guess_train(ttfld_ctx* ctx, int epochs, double lr, uint64_t seed, double* mean_loss);
+/* Loss and gradient of every parameter for one input (NX*NY*NZ cells x 5
+ * features, r fastest), target and mask -- the hook gradient checks use. */
+int ttfld_guess_gradients(ttfld_ctx* ctx, const float* feat, const float* target,
+                          const unsigned char* mask, double* loss, float* grads);
+/* Network output (normalised target units) for one input. */
+int ttfld_guess_predict(ttfld_ctx* ctx, const float* feat, float* pred);
+size_t ttfld_guess_num_params(void);
+/* Weights blob: "TTFLDNN1", uint64 parameter count, FP32 parameters. */
 int ttfld_guess_load(ttfld_ctx* ctx, const void* blob, size_t bytes);
 int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
 

@@ -43,13 +43,17 @@ class Params(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("solver", c_int32), ("guess", c_int32), ("tol", c_double),
                 ("inner_min", c_int32), ("inner_max", c_int32), ("max_sweeps", c_int32),
-                ("reserved", c_int32)]
+                ("fallback_rule", c_int32)]
+
+
+FALLBACK = {"first_sweep": 0, "never": 1, "residual": 2}
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("sor_iter", c_int32), ("corrections", c_int32), ("fallback", c_int32),
                 ("status", c_int32), ("rnorm", c_double), ("rhsnorm", c_double),
-                ("true_resid_l1", c_double), ("guess_resid_l1", c_double), ("solve_ms", c_double)]
+                ("true_resid_l1", c_double), ("guess_resid_l1", c_double), ("solve_ms", c_double),
+                ("guess_ms", c_double)]
 
 
 class StepStats(ctypes.Structure):
@@ -88,7 +92,10 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_solve_with_sor", "ttfld_solve_system", "ttfld_sor_sweeps",
            "ttfld_true_residual", "ttfld_adjust_sor_param", "ttfld_coupled_energy_eqs",
            "ttfld_diffusion", "ttfld_guess_load", "ttfld_guess_save", "ttfld_time_sweeps",
-           "ttfld_kernel_launches", "ttfld_sor_solve_noalloc")
+           "ttfld_kernel_launches", "ttfld_sor_solve_noalloc", "ttfld_guess_init",
+           "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
+           "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
+           "ttfld_guess_num_params")
 
 _lib = None
 
@@ -145,6 +152,15 @@ def lib():
     L.ttfld_kernel_launches.argtypes = []
     L.ttfld_sor_solve_noalloc.argtypes = [vp] * 9 + [ctypes.c_int] * 3 + [ctypes.c_double] * 2 + \
         [ctypes.c_int] * 2 + [vp, ctypes.POINTER(ctypes.c_int), P_double, P_double]
+    L.ttfld_guess_init.argtypes = [vp, ctypes.c_uint64]
+    L.ttfld_guess_dataset.argtypes = [vp, ctypes.c_int]
+    L.ttfld_guess_capture_next.argtypes = [vp]
+    L.ttfld_guess_dataset_count.argtypes = [vp]
+    L.ttfld_guess_train.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, P_double]
+    L.ttfld_guess_gradients.argtypes = [vp, vp, vp, vp, P_double, vp]
+    L.ttfld_guess_predict.argtypes = [vp, vp, vp]
+    L.ttfld_guess_num_params.restype = ctypes.c_size_t
+    L.ttfld_guess_num_params.argtypes = []
     L.ttfld_guess_load.argtypes = [vp, vp, ctypes.c_size_t]
     L.ttfld_guess_save.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     _lib = L

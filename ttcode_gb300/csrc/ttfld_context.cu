@@ -260,6 +260,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   }
   if (check_cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       check_cuda(cudaEventCreate(&c->ev0), "event") || check_cuda(cudaEventCreate(&c->ev1), "event") ||
+      check_cuda(cudaEventCreate(&c->evg), "event") ||
       check_cuda(cudaMallocHost((void**)&c->host_sol, sizeof(SolverDev)), "pinned")) {
     ttfld_destroy(c);
     return TTFLD_E_CUDA;
@@ -277,10 +278,12 @@ int ttfld_destroy(ttfld_ctx* c) {
   unet_free(c);
   mix_free(c);
   if (c->prev_x) cudaFree(c->prev_x);
+  if (c->guess_tmp) cudaFree(c->guess_tmp);
   if (c->slab) cudaFree(c->slab);
   if (c->host_sol) cudaFreeHost(c->host_sol);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->evg) cudaEventDestroy(c->evg);
   if (c->stream) cudaStreamDestroy(c->stream);
   free(c);
   return TTFLD_OK;

@@ -199,7 +199,7 @@ struct ttfld_ctx {
   ttfld_solve_opts opts;
   int device;
   cudaStream_t stream;
-  cudaEvent_t ev0, ev1;
+  cudaEvent_t ev0, ev1, evg;
   void* slab;                // one allocation holding every array
   size_t slab_bytes;
   double* staging;           // device staging for box-shaped transfers
@@ -213,9 +213,11 @@ struct ttfld_ctx {
   // learned guess
   void* unet;
   int have_model;
-  double prev_scale;        // (1-conv_parm) for the previous-solution guess
+  double prev_scale;        // scale of the previous-solution guess
   int have_prev;
-  double* prev_x;           // previous outer solution (halo)
+  int solve_idx;            // solves so far in the current step
+  double* prev_x;           // previous solution (halo)
+  double* guess_tmp;        // scratch halo array of the first-sweep guess test
   double last_solve_ms;
 };
 
@@ -237,5 +239,6 @@ int halo_shift(ttfld_ctx* c, double* a);
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);
 int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1);
 int unet_guess(ttfld_ctx* c, double* x_out, double* resid_l1);
+int unet_capture(ttfld_ctx* c);
 void unet_free(ttfld_ctx* c);
 }  // namespace ttfld

@@ -251,17 +251,20 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
   ttfld_solve_stats local{};
   if (!st) st = &local;
   int fallback = 0;
+  // the network is trained on a step's first solve; the later (outer
+  // iteration) solves of a step start from the previous solution
+  int guess = c->opts.guess;
+  if (guess == TTFLD_GUESS_LEARNED && !c->have_model) return TTFLD_E_NOMODEL;
+  if (guess == TTFLD_GUESS_LEARNED && c->solve_idx > 0) guess = TTFLD_GUESS_PREVIOUS;
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
-  if (c->opts.guess == TTFLD_GUESS_ZERO || (c->opts.guess == TTFLD_GUESS_PREVIOUS && !c->have_prev) ||
-      (c->opts.guess == TTFLD_GUESS_LEARNED && !c->have_model)) {
-    if (c->opts.guess == TTFLD_GUESS_LEARNED && !c->have_model) return TTFLD_E_NOMODEL;
+  if (guess == TTFLD_GUESS_ZERO || (guess == TTFLD_GUESS_PREVIOUS && !c->have_prev)) {
     TT_CHECK(cudaMemsetAsync(d.DELTA_ER, 0, nhalo(d) * 8, c->stream));  // ppsor.f:29
   } else {
     // initial iterate in the interior; ghosts zero as in ppsor.f:29
     double* x = d.DELTA_ER;
     TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
     double gl1 = 0.0, bl1 = 0.0;
-    if (c->opts.guess == TTFLD_GUESS_PREVIOUS) {
+    if (guess == TTFLD_GUESS_PREVIOUS) {
       const double* px = c->prev_x;
       const double sc = c->prev_scale;
       launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
@@ -277,25 +280,57 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
     if (rc) return rc;
     if ((rc = true_residual(c, x, d.RHS, &gl1))) return rc;
     st->guess_resid_l1 = gl1;
-    // fallback when the guess is no better than the zero guess (||b||_1)
-    if (!(gl1 < bl1)) {
+    bool reject = false;
+    if (c->opts.fallback_rule == 2) {
+      reject = !(gl1 < bl1);  // no better than the zero guess's residual ||b||_1
+    } else if (c->opts.fallback_rule == 0) {
+      // ||b - A x1||_1 after one FP64 red-black sweep from the guess and after
+      // one from zero, on a scratch copy: keep the guess if its first-sweep
+      // residual is the smaller.  (With over-relaxation the first sweep from
+      // zero itself leaves a residual above ||b||_1, so the comparison is
+      // made sweep for sweep.)
+      if (!c->guess_tmp) TT_CHECK(cudaMalloc((void**)&c->guess_tmp, nhalo(d) * 8));
+      double r1[2];
+      for (int q = 0; q < 2; ++q) {
+        if (q == 0) TT_CHECK(cudaMemcpyAsync(c->guess_tmp, x, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
+        else TT_CHECK(cudaMemsetAsync(c->guess_tmp, 0, nhalo(d) * 8, c->stream));
+        TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+        if ((rc = rhs_norm(c, d.RHS, nullptr))) return rc;
+        if ((rc = launch_exact_sweeps(c, c->guess_tmp, d.RHS, 1, 3, 3, -1.0))) return rc;
+        if ((rc = true_residual(c, c->guess_tmp, d.RHS, &r1[q]))) return rc;
+      }
+      reject = !(r1[0] < r1[1]);
+    }
+    if (reject) {
       TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
       fallback = 1;
     }
   }
+  TT_CHECK(cudaEventRecord(c->evg, c->stream));
   int rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));
-  float ms = 0.f;
+  float ms = 0.f, gms = 0.f;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  cudaEventElapsedTime(&gms, c->ev0, c->evg);
   c->last_solve_ms = ms;
   st->solve_ms = ms;
+  st->guess_ms = gms;
   st->fallback = fallback;
   if (rc < 0) return rc;
-  // keep this outer iteration's solution for the previous-solution guess
+  // a requested training pair: the state this solve started from and its answer
+  if (c->unet) {
+    int rc2 = unet_capture(c);
+    if (rc2) return rc2;
+  }
+  // keep this solution for the previous-solution guess of the next solve:
+  // scaled by (1 - conv_parm) inside a step (ER moved by conv_parm * delta_ER),
+  // as is from one step to the next
   if (!c->prev_x) TT_CHECK(cudaMalloc((void**)&c->prev_x, nhalo(d) * 8));
   TT_CHECK(cudaMemcpyAsync(c->prev_x, d.DELTA_ER, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
   c->have_prev = 1;
+  c->prev_scale = 0.9;
+  c->solve_idx += 1;
   if (fallback && rc == TTFLD_OK) rc = TTFLD_FALLBACK;
   return rc;
 }
@@ -338,6 +373,7 @@ int ttfld_true_residual(ttfld_ctx* c, double* l1, double* rhs_l1) {
 
 int ttfld_solve_system(ttfld_ctx* c, ttfld_solve_stats* st) {
   if (!c) return TTFLD_E_ARGS;
+  c->solve_idx = 0;  // a system solved on its own counts as a step's first solve
   return solve_delta_er(c, st);
 }
 

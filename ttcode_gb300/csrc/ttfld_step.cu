@@ -187,7 +187,8 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
   TT_CHECK(cudaEventRecord(t0, c->stream));
   TT_CHECK(cudaMemsetAsync(d.DELTA_ER, 0, nhalo(d) * 8, c->stream));  // :52-53
   TT_CHECK(cudaMemsetAsync(d.DQ, 0, ncell(d) * 8, c->stream));
-  c->have_prev = 0;
+  c->prev_scale = 1.0;  // the last step's solution guesses this step's first solve as is
+  c->solve_idx = 0;
   if (do_bounds && (rc = asm_bounds(c))) return rc;                     // :63
   launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
     size_t h = hidx(d, i, j, k);
