@@ -2,11 +2,15 @@
 residual 1e-10 on one GB300, through libttfld's C ABI.
 
 Workload (shell256): the 100 x 256 x 128 (r x phi x theta) synthetic shell
-(3,276,800 cells, dt = 100 s, seed 1) after the set-up BOUNDS/KAPPA and one
-implicit step; a "step" is one solve of that step's SOLVE_WITH_SOR system
-from delta_ER = 0 (ppsor.f:29).  The product path is the FP32 red-black
-sweeps inside FP64 defect correction; the plain FP64 red-black SOR (exact
-reference rounding, and Jacobi-scaled with FMA) are timed in the same run.
+(3,276,800 cells, dt = 100 s, seed 1) after the set-up BOUNDS/KAPPA; a
+"step" is one solve of the SOLVE_WITH_SOR system of its implicit step's
+first outer iteration (ppenergy.f:375).  The product path starts from the
+learned initial guess (trained before the timed region, on the GPU, on 16
+pairs the solver generates from other irradiations and time steps of the
+same shell), keeps it only if it beats the zero guess after its first
+sweep, and runs FP32 red-black sweeps inside FP64 defect correction.  The
+same system from zero, and the plain FP64 red-black SOR (exact reference
+rounding, and Jacobi-scaled with FMA), are timed in the same run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -31,8 +35,9 @@ sys.path.insert(0, ROOT)
 METRIC = "ms per FLD solve to rel. residual 1e-10: learned+FP32/FP64 vs plain FP64 SOR"
 SHELL = "shell256"
 WORKLOAD = ("shell256: 100x256x128 (r x phi x theta) synthetic spherical shell, 3276800 cells, "
-            "dt=100 s, seed 1; one SOLVE_WITH_SOR system of its implicit step, solved from zero "
-            "to ||b-Ax||_1/||b||_1 <= 1e-10")
+            "dt=100 s, seed 1; the SOLVE_WITH_SOR system of its implicit step's first outer "
+            "iteration, solved to ||b-Ax||_1/||b||_1 <= 1e-10")
+TRAIN_PAIRS, TRAIN_EPOCHS, TRAIN_LR = 16, 12, 5e-4
 # Algorithmic bytes per cell update of one sweep (both colours):
 #   FP32 scaled sweep: 6 coefficients + rhat + e read + e write  = 9 x 4 B
 #   FP64 exact sweep : 7 coefficients + b + x read + x write      = 10 x 8 B
@@ -119,18 +124,54 @@ def load_traffic():
     return None
 
 
-def build_system(device):
-    """One implicit step of the shell on the device; its last SOLVE_WITH_SOR
-    system stays in SOR_A..G / RHS_ER."""
+def first_system(f):
+    """Assemble the SOLVE_WITH_SOR system of an implicit step's first outer
+    iteration (one outer iteration of COUPLED_ENERGY_EQS leaves it in
+    SOR_A..G / RHS_ER) and put back the state the step started from, which
+    is what the learned guess reads."""
+    from ttcode_gb300 import _ffi
+    import ctypes
+    keep = {n: f.download(n) for n in ("T", "ER", "DELTA_ER")}
+    itmax = f.params["itmax"]
+    f.set_params(itmax=1)
+    f.set_solver("mixed", tol=1e-10, max_sweeps=64)
+    st = _ffi.StepStats()
+    f.L.ttfld_coupled_energy_eqs(f.h, 1, ctypes.byref(st))
+    for n, a in keep.items():
+        f.upload(n, a)
+    f.set_params(itmax=itmax)
+
+
+def build_system(device, train=True):
+    """The shell on the device with the learned guess trained (on pairs from
+    other irradiations and time steps) and the bench system assembled."""
+    from ttcode_gb300 import guess
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import shell
     sh = shell(SHELL, seed=1)
     sh.params["epsmat"] = 1e-10
     sh.params["itmax"] = 200000
     f = start_run(sh, device=device)
-    f.set_solver("mixed", tol=1e-10)
-    f.coupled_energy_eqs(True)
-    return sh, f
+    info = None
+    if train:
+        t0 = time.perf_counter()
+        guess.init(f, seed=1, capacity=TRAIN_PAIRS)
+        npairs = guess.capture_pairs(f, sh, guess.random_cases(TRAIN_PAIRS, seed=10))
+        t1 = time.perf_counter()
+        losses = [guess.train(f, epochs=1, lr=TRAIN_LR, seed=e) for e in range(TRAIN_EPOCHS)]
+        t2 = time.perf_counter()
+        info = {"pairs": npairs, "epochs": TRAIN_EPOCHS, "lr": TRAIN_LR, "capture_s": round(t1 - t0, 2),
+                "train_s": round(t2 - t1, 2), "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+                "pairs_from": "16 seeded irradiations (phi0, T_irr in [1500, 2500] K) and dt in [50, 500] s "
+                              "of the same shell; the timed system (T_irr 2048 K, dt 100 s) is not among them"}
+        # back to the bench case (start_run's set-up)
+        f.load_shell(sh)
+        f.set_params(iii=0, delt=sh.params["delt"])
+        f.bounds()
+        f.kappa()
+        f.set_params(iii=sh.params.get("iii", 1))
+    first_system(f)
+    return sh, f, info
 
 
 def flush_l2(torch, buf):
@@ -142,11 +183,11 @@ def run_profile_solve(args):
     system, nothing else (the command the ncu summaries under profiles/ use)."""
     import torch
     torch.cuda.set_device(0)
-    sh, f = build_system(0)
-    for solver in ("mixed", "sor64_exact"):
-        f.set_solver(solver, tol=1e-10, inner_min=16, inner_max=512)
+    sh, f, _ = build_system(0)
+    for solver, g in (("mixed", "learned"), ("sor64_exact", "zero")):
+        f.set_solver(solver, guess=g, tol=1e-10, inner_min=16, inner_max=512)
         st = f.solve_system()
-        print(json.dumps({"solver": solver, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
+        print(json.dumps({"solver": solver, "guess": g, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
     f.close()
 
 
@@ -159,7 +200,7 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     from ttcode_gb300 import _ffi
     L = _ffi.lib()
-    sh, f = build_system(local)
+    sh, f, train_info = build_system(local)
     nx, ny, nz = sh.dims
     ncells = nx * ny * nz
     stream = torch.cuda.ExternalStream(f.stream_ptr(), device=torch.device("cuda", local))
@@ -186,7 +227,7 @@ def run_gpu(args):
 
     # warm-up
     for _ in range(args.warmup):
-        solve_timed("mixed")
+        solve_timed("mixed", "learned")
     # timed region: K product-path solves
     if ws > 1:
         torch.distributed.barrier()
@@ -195,7 +236,7 @@ def run_gpu(args):
     times, stats = [], []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            ms, st = solve_timed("mixed")
+            ms, st = solve_timed("mixed", "learned")
             times.append(ms)
             stats.append(st)
     torch.cuda.synchronize()
@@ -212,6 +253,9 @@ def run_gpu(args):
     r_l1, b_l1 = f.true_residual()
     err = float(np.linalg.norm((x_mixed - x_ref).ravel()) / np.linalg.norm(x_ref.ravel()))
 
+    # the same mixed solver from the zero guess
+    zl = [solve_timed("mixed", "zero") for _ in range(3)]
+    zero_guess = {"ms": min(m for m, _ in zl), "sweeps": zl[-1][1].sor_iter}
     # the plain FP64 red-black SOR on the same GPU (same stopping rule as the
     # reference, in-sweep L1 ratio <= 1e-10)
     plain = {}
@@ -245,7 +289,7 @@ def run_gpu(args):
     out = torch.empty(f.download("DELTA_ER").size, dtype=torch.float64, pin_memory=True)
     h2d = sum(host[n].numel() * 8 for n in names) + ub.size * 4
     d2h = out.numel() * 8
-    f.set_solver("mixed", tol=1e-10, inner_min=16, inner_max=512)
+    f.set_solver("mixed", guess="learned", tol=1e-10, inner_min=16, inner_max=512)
     e2e = []
     for it in range(args.warmup + args.steps):
         flush_l2(torch, flush)
@@ -269,9 +313,12 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 sweeps / fp64 residual",
         "data": "synthetic (seeded analytic shell, no dataset)",
         "config": {"workload": WORKLOAD, "cells": ncells, "solver": "mixed FP32/FP64 defect correction",
-                   "guess": "zero", "tol": 1e-10, "omega": sh.params["sorparam"],
+                   "guess": "learned (half-resolution 3-D U-Net, BF16), first-sweep fallback to zero",
+                   "tol": 1e-10, "omega": sh.params["sorparam"],
                    "l2": "flushed between timed solves (256 MB write)", "parallelism": "replicas"},
         "sweeps_per_solve": stats[-1].sor_iter, "corrections_per_solve": stats[-1].corrections,
+        "fallbacks": int(sum(s.fallback for s in stats)), "guess_ms": stats[-1].guess_ms,
+        "guess_training": train_info, "zero_guess_mixed": zero_guess,
         "true_rel_residual": r_l1 / b_l1,
         "err_vs_fp64_1e-12": err, "fp64_1e-12_sweeps": st_ref.sor_iter,
         "plain_fp64": plain,
@@ -280,7 +327,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "call": "ttfld_upload x11 + ttfld_solve_with_sor + ttfld_download (pinned host)"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "sweep32_kernel (both colours)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "sweeps32_persistent (one full sweep)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * ncells, "ms_per_sweep": ms_sweep32,
                      "traffic": traffic},

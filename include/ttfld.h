@@ -140,9 +140,12 @@ typedef struct {
   int32_t inner_max;
   int32_t max_sweeps;  /* mixed solver sweep budget (0 = 100*ITMAX)        */
   int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:
-                            0 = the residual ||b - A x||_1 after one
-                                red-black sweep from it is not below the
-                                residual after one sweep from zero;
+                            0 = the residual its first red-black sweep
+                                leaves (the in-sweep norm RNORM of the
+                                second sweep) is not below the one the
+                                first sweep from zero leaves; the mixed
+                                solver runs this test with its own FP32
+                                sweeps and keeps the winner's two sweeps;
                             1 = never;
                             2 = ||b - A x0||_1 >= ||b||_1                  */
 } ttfld_solve_opts;
@@ -255,7 +258,9 @@ int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
  * system (TTFLD_SOLVER_SOR64_EXACT: DELTA_ER is iterated in place;
  * SOR64_FAST / MIXED: only their private iterate is touched) and returns
  * the mean device time of one full sweep (both colours), CUDA events on the
- * library's stream. */
+ * library's stream.  MIXED times the solver's own kernel (all n sweeps in
+ * one persistent launch, the in-sweep norm every 8th); solver = 3 times the
+ * same FP32 sweeps issued as two launches per sweep, for comparison. */
 int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 /* Number of kernels this process has launched through libttfld. */
 uint64_t ttfld_kernel_launches(void);

@@ -78,6 +78,7 @@ FIELDS = {
 }
 
 SOLVER = {"sor64_exact": 0, "sor64_fast": 1, "mixed": 2}
+TIMED_SWEEPS = dict(SOLVER, mixed_split=3)   # ttfld_time_sweeps also times the per-colour launches
 GUESS = {"zero": 0, "previous": 1, "learned": 2}
 
 STATUS = {0: "ok", 1: "iteration limit reached", 2: "learned guess rejected",

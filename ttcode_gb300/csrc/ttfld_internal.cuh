@@ -26,14 +26,17 @@ struct SolverDev {
   double rnorm;        // global_RNORM of the last completed sweep
   double ratio;        // rnorm / rhsnorm
   double true_l1;      // ||b - A x||_1 of the last residual pass
-  double scratch[4];
+  double scratch[3];
+  unsigned int bar_count;  // grid barrier of the persistent sweep kernel:
+  unsigned int bar_gen;    // arrivals and generation
   int iter;            // SOR_ITER
   int done;            // 1 once the stopping rule fired
   int maxit;           // 1 if ITMAX ended the loop
   int nonfinite;       // 1 if a norm was NaN/Inf
   unsigned int ticket; // last-block-done counter
   unsigned int ticket2;
-  int pad[2];
+  int bar_timeout;     // 1 if a grid barrier wait ran out (the kernel gave up)
+  int pad;
 };
 
 // Reduction targets of the outer Newton loop.
@@ -233,7 +236,8 @@ int check_cuda(cudaError_t e, const char* what);
 // Internal entry points shared across translation units.
 int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st);
 int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st);
-int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st);
+int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test = 0,
+                int* fallback = nullptr);
 int fill_sor_matrix(ttfld_ctx* c);
 int halo_shift(ttfld_ctx* c, double* a);
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);

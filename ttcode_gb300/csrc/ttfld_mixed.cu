@@ -163,53 +163,44 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 // thread: res = (e + sum a_nb e_nb) - rhat (the reference's in-sweep residual
 // divided by A, ppsor.f:64-71), e -= omega * res.  NORM sweeps also sum
 // |A * res| (per thread in FP32, per block and grid in FP64 in a fixed
-// order), i.e. the reference's RNORM (ppsor.f:73) of the iterate
-// x + e, and the last block of the second colour stops the inner loop once
-// RNORM / RHSNORM <= stop_ratio.  Sweeps queued after that return at once.
+// order), i.e. the reference's RNORM (ppsor.f:73) of the iterate x + e.
+// Item t is the t-th group of four colour slots (row-major over (k, j, h)).
 template <int COL, bool NORM>
-__global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega, SolverDev* sol,
-                                                           double* partials, double stop_ratio) {
-  __shared__ double sh[32];
-  __shared__ bool last;
-  if (*(volatile int*)&sol->done) return;
-  const int nv = g.nxp >> 2;
-  const long long n = g.rows * nv;
+__device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
+                                          size_t plane, float& nacc) {
   const float* __restrict__ eo = m.e[1 - COL];
   float* __restrict__ es = m.e[COL];
-  const size_t plane = (size_t)g.ny * g.nxp;
-  float nacc = 0.f;  // per-thread partial (a few cells): FP32, widened once below
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int hv = (int)(t % nv);
-    const long long rr = t / nv;
-    const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
-    const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
-    const int h0 = hv * 4;
-    const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
-    const size_t cb = (size_t)rr * g.nxp + h0;
-    const size_t eb = gslot(g, j0, k0, h0);
-    const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
-    const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
-    const float4 o = ld4(eo + eb);
-    float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
-    if (off == 0) {
-      xm0 = h0 > 0 ? eo[eb - 1] : 0.f; xm1 = o.x; xm2 = o.y; xm3 = o.z;
-      xp0 = o.x; xp1 = o.y; xp2 = o.z; xp3 = o.w;
-    } else {
-      xm0 = o.x; xm1 = o.y; xm2 = o.z; xm3 = o.w;
-      xp0 = o.y; xp1 = o.z; xp2 = o.w; xp3 = (h0 + 4 < g.nxp) ? eo[eb + 4] : 0.f;
-    }
-    const float4 s = ld4(eo + gslot(g, jm, k0, h0));
-    const float4 nn = ld4(eo + gslot(g, jp, k0, h0));
-    const float4 b = ld4(eo + eb - plane);
-    const float4 tt = ld4(eo + eb + plane);
-    const float4 e = ld4(es + eb);
-    const float4 aw = ld4(m.a[0][COL] + cb), ae = ld4(m.a[1][COL] + cb);
-    const float4 as = ld4(m.a[2][COL] + cb), an = ld4(m.a[3][COL] + cb);
-    const float4 ab = ld4(m.a[4][COL] + cb), at = ld4(m.a[5][COL] + cb);
-    const float4 r = ld4(m.rhat[COL] + cb);
-    float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (NORM) dg = ld4(m.diag[COL] + cb);
-    float4 out;
+  const int hv = (int)(t % nv);
+  const long long rr = t / nv;
+  const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
+  const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
+  const int h0 = hv * 4;
+  const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
+  const size_t cb = (size_t)rr * g.nxp + h0;
+  const size_t eb = gslot(g, j0, k0, h0);
+  const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
+  const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
+  const float4 o = ld4(eo + eb);
+  float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
+  if (off == 0) {
+    xm0 = h0 > 0 ? eo[eb - 1] : 0.f; xm1 = o.x; xm2 = o.y; xm3 = o.z;
+    xp0 = o.x; xp1 = o.y; xp2 = o.z; xp3 = o.w;
+  } else {
+    xm0 = o.x; xm1 = o.y; xm2 = o.z; xm3 = o.w;
+    xp0 = o.y; xp1 = o.z; xp2 = o.w; xp3 = (h0 + 4 < g.nxp) ? eo[eb + 4] : 0.f;
+  }
+  const float4 s = ld4(eo + gslot(g, jm, k0, h0));
+  const float4 nn = ld4(eo + gslot(g, jp, k0, h0));
+  const float4 b = ld4(eo + eb - plane);
+  const float4 tt = ld4(eo + eb + plane);
+  const float4 e = ld4(es + eb);
+  const float4 aw = ld4(m.a[0][COL] + cb), ae = ld4(m.a[1][COL] + cb);
+  const float4 as = ld4(m.a[2][COL] + cb), an = ld4(m.a[3][COL] + cb);
+  const float4 ab = ld4(m.a[4][COL] + cb), at = ld4(m.a[5][COL] + cb);
+  const float4 r = ld4(m.rhat[COL] + cb);
+  float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (NORM) dg = ld4(m.diag[COL] + cb);
+  float4 out;
 #define UPD(L, IDX, XM, XP)                                                                \
   {                                                                                        \
     float acc = fmaf(aw.L, XM, fmaf(ae.L, XP, fmaf(as.L, s.L, fmaf(an.L, nn.L,             \
@@ -219,10 +210,26 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
     out.L = ok ? fmaf(-omega, res, e.L) : 0.f;                                             \
     if (NORM && ok) nacc += fabsf(dg.L * res);                                            \
   }
-    UPD(x, 0, xm0, xp0) UPD(y, 1, xm1, xp1) UPD(z, 2, xm2, xp2) UPD(w, 3, xm3, xp3)
+  UPD(x, 0, xm0, xp0) UPD(y, 1, xm1, xp1) UPD(z, 2, xm2, xp2) UPD(w, 3, xm3, xp3)
 #undef UPD
-    st4(es + eb, out);
-  }
+  st4(es + eb, out);
+}
+
+// One colour per launch.  NORM launches of the second colour end with the
+// last block applying the stop rule: once RNORM / RHSNORM <= stop_ratio the
+// inner loop is done, and sweeps queued after that return at once.
+template <int COL, bool NORM>
+__global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                           double* partials, double stop_ratio) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  if (*(volatile int*)&sol->done) return;
+  const int nv = g.nxp >> 2;
+  const long long n = g.rows * nv;
+  const size_t plane = (size_t)g.ny * g.nxp;
+  float nacc = 0.f;  // per-thread partial (a few cells): FP32, widened once below
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    sweep_vec<COL, NORM>(g, m, omega, t, nv, plane, nacc);
   if (COL == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&sol->iter, 1);
   if (NORM) {
     double sb = block_sum((double)nacc, sh);
@@ -249,6 +256,100 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
           sol->ticket = 0;
         }
       }
+    }
+  }
+}
+
+// Grid-wide barrier of the persistent kernel (a cooperative launch, so all
+// blocks are resident).  Thread 0 of each block arrives on a counter; the
+// last arrival resets it and advances the generation the others wait on.
+// The wait is bounded: after kBarrierSpins polls (well over a second with
+// the back-off) or once another block has given up, the block records the
+// timeout and returns false, and the kernel returns without further work.
+constexpr long long kBarrierSpins = 1LL << 23;
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) {
+  __shared__ int ok_sh;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int g0 = ld_acquire(&sol->bar_gen);
+    __threadfence();
+    if (atomicAdd(&sol->bar_count, 1u) == nblocks - 1) {
+      atomicExch(&sol->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&sol->bar_gen, 1u);
+    } else {
+      long long polls = 0;
+      while (ld_acquire(&sol->bar_gen) == g0) {
+        if (++polls > kBarrierSpins || *(volatile int*)&sol->bar_timeout) {
+          atomicExch(&sol->bar_timeout, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok_sh = ok;
+  }
+  __syncthreads();
+  return ok_sh != 0;
+}
+
+// nsweeps FP32 sweeps in one launch: both colours of every sweep with a grid
+// barrier after each, every norm_every-th sweep (and the last) with the
+// in-sweep norm.  Each block reduces its partial of a norm sweep; after the
+// barrier every block adds all partials in the same fixed order, so all of
+// them reach the same stop decision and leave the loop together.  Every
+// thread keeps the same items from sweep to sweep.
+constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
+
+__global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                               double* partials, double stop_ratio, int nsweeps,
+                                                               int norm_every) {
+  __shared__ double sh[32];
+  __shared__ int stop_sh;
+  if (*(volatile int*)&sol->done) return;  // set before the launch, so the same for every block
+  const int nv = g.nxp >> 2;
+  const long long n = g.rows * nv;
+  const size_t plane = (size_t)g.ny * g.nxp;
+  const unsigned int nb = gridDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, ts = (long long)gridDim.x * blockDim.x;
+  for (int sw = 1; sw <= nsweeps; ++sw) {
+    const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
+    float nacc = 0.f;
+    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<0, true>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = t0; t < n; t += ts) sweep_vec<0, false>(g, m, omega, t, nv, plane, nacc); }
+    if (!grid_sync(sol, nb)) return;
+    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<1, true>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = t0; t < n; t += ts) sweep_vec<1, false>(g, m, omega, t, nv, plane, nacc); }
+    if (norm) {
+      const double sb = block_sum((double)nacc, sh);
+      if (threadIdx.x == 0) partials[blockIdx.x] = sb;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+    if (!grid_sync(sol, nb)) return;
+    if (norm) {
+      const double tot = block_sum_array(partials, nb, sh);
+      if (threadIdx.x == 0) {
+        const double ratio = tot / sol->rhsnorm;
+        const int stop = !isfinite(tot) || !(ratio > stop_ratio);
+        if (blockIdx.x == 0) {
+          sol->rnorm = tot;
+          sol->ratio = ratio;
+          if (!isfinite(tot)) sol->nonfinite = 1;
+          if (stop) sol->done = 1;
+        }
+        stop_sh = stop;
+      }
+      __syncthreads();
+      if (stop_sh) return;
     }
   }
 }
@@ -329,6 +430,21 @@ static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
   return 0;
 }
 
+// rhat = b / A: the correction equation of the zero initial guess.
+static int rhat_of_b(ttfld_ctx* c, const double* b) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  Mix32 m = w->m32;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    const int col = (i + j + k) & 1;
+    const size_t s = cslot(g, j - 1, k - 1, (i - 1) >> 1);
+    m.rhat[col][s] = __double2float_rn(b[cidx(d, i, j, k)]) * m.ainv[col][s];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
 // Grid of whole waves: the blocks that fit on the SMs at once (occupancy of
 // the kernel), walking the rest of the items by grid stride, so the last
 // wave of a short streaming kernel is never a partial one.
@@ -347,22 +463,53 @@ static int wave_grid(K kernel, long long items) {
   return (int)(need < per_wave ? (need < 1 ? 1 : need) : per_wave);
 }
 
+// Blocks of the persistent kernel: all resident at once (cooperative
+// launch), at most one wave.  0 if cooperative launch is unavailable.
+static int persistent_grid(long long items) {
+  static int coresident = -1;
+  if (coresident < 0) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweeps32_persistent, kPersistThreads, 0);
+    coresident = coop ? sms * per_sm : 0;
+    if (coresident > kMaxPartials) coresident = kMaxPartials;
+  }
+  if (coresident <= 0 || items <= 0) return 0;
+  const long long need = (items + kPersistThreads - 1) / kPersistThreads;
+  return (int)(need < coresident ? need : coresident);
+}
+
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
-// evaluates the in-sweep norm against stop_ratio.
-int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0) {
+// evaluates the in-sweep norm against stop_ratio.  One persistent launch
+// where cooperative launch is available, else two launches per sweep.
+int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0,
+                    bool split = false) {
   MixWork* w = work(c);
-  const Cmp& g = w->g;
+  Cmp g = w->g;
+  Mix32 m = w->m32;
   long long nvec = g.rows * (g.nxp >> 2);
-  int nb = wave_grid(sweep32_kernel<1, true>, nvec);
   float omega = (float)c->d.sorparam;
+  const int pb = split ? 0 : persistent_grid(nvec);
+  if (pb > 0) {
+    SolverDev* sol = c->sol;
+    double* partials = c->partials;
+    void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every};
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent, dim3(pb), dim3(kPersistThreads), args,
+                                         0, c->stream));
+    count_launches(1);
+    return 0;
+  }
+  int nb = wave_grid(sweep32_kernel<1, true>, nvec);
   for (int s = 1; s <= nsweeps; ++s) {
     bool norm = norm_every > 0 && (s % norm_every == 0 || s == nsweeps);
     if (norm) {
-      sweep32_kernel<0, true><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
-      sweep32_kernel<1, true><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<0, true><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, true><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
     } else {
-      sweep32_kernel<0, false><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
-      sweep32_kernel<1, false><<<nb, kThreads, 0, c->stream>>>(g, w->m32, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<0, false><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, false><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
     }
   }
   count_launches(2 * nsweeps);
@@ -373,6 +520,10 @@ int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_r
 static int poll(ttfld_ctx* c) {
   TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
   TT_CHECK(cudaStreamSynchronize(c->stream));
+  if (c->host_sol->bar_timeout) {
+    fprintf(stderr, "ttfld: a grid barrier of the persistent sweep kernel timed out\n");
+    return TTFLD_E_CUDA;
+  }
   return 0;
 }
 
@@ -380,7 +531,13 @@ static int poll(ttfld_ctx* c) {
 // A e = r until the in-sweep norm of x + e has dropped by 1e-5 relative to
 // the anchor (well inside FP32 precision) or reached tol, x += e, repeat;
 // stop when the FP64 ||b - A x||_1 / ||b||_1 <= tol.
-int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st) {
+//
+// With guess_test, x holds a previous or learned initial guess that must
+// beat the zero guess: two sweeps are run from zero and two from the guess,
+// and the in-sweep norm of each second sweep (the residual the first sweep
+// left) decides.  The guess keeps its two sweeps and its residual as the
+// first anchor; a rejected guess is replaced by zero (*fallback = 1).
+int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
   int rc;
   if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
   MixWork* w = work(c);
@@ -394,8 +551,32 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st)
   int corrections = 0, status = TTFLD_OK;
   double tight = 1.0;  // halved each time the in-sweep norm met tol but the FP64 residual did not
   bool hit_tol = false;
-  for (;;) {
+  bool resume = false;  // the first anchor and its first sweeps are done already
+  if (fallback) *fallback = 0;
+  if (guess_test) {
+    if ((rc = rhat_of_b(c, b))) return rc;
+    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
+    if ((rc = launch_sweeps32(c, 2, 2, -1.0)) || (rc = poll(c))) return rc;
+    const double r_zero = c->host_sol->rnorm;
+    TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
     if ((rc = resid32(c, x, b, &l1))) return rc;
+    if (st) st->guess_resid_l1 = l1;
+    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
+    if ((rc = launch_sweeps32(c, 2, 2, -1.0)) || (rc = poll(c))) return rc;
+    const double r_guess = c->host_sol->rnorm;
+    if (r_guess < r_zero) {
+      resume = true;
+    } else {
+      if (fallback) *fallback = 1;
+      TT_CHECK(cudaMemsetAsync(x, 0, nhalo(c->d) * 8, c->stream));
+      TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
+      if ((rc = poll(c))) return rc;
+    }
+  }
+  for (;;) {
+    if (!resume) {
+      if ((rc = resid32(c, x, b, &l1))) return rc;
+    }
     ++corrections;
     if (!isfinite(l1)) { status = TTFLD_E_NONFINITE; break; }
     if (!(l1 > tol * bl1)) break;
@@ -404,8 +585,9 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st)
     const double anchor = l1 / bl1;
     const double stop = fmax(tol * tight, anchor * 1e-5);
     hit_tol = stop <= tol;
-    TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
+    if (!resume) TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
     TT_CHECK(cudaMemsetAsync(&c->sol->done, 0, sizeof(int), c->stream));
+    resume = false;
     int it0 = c->host_sol->iter;
     double r_prev = anchor;
     int it_prev = it0;
@@ -623,11 +805,14 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   if (n < 1) return TTFLD_E_ARGS;
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   if ((rc = rhs_norm(c, c->d.RHS, nullptr))) return rc;
-  if (solver == TTFLD_SOLVER_MIXED) {
+  // TTFLD_SOLVER_MIXED times the solver's kernel (one persistent launch for
+  // the n sweeps); 3 times the same sweeps as two launches per sweep
+  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3;
+  if (mixed) {
     if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
     double l1;
     if ((rc = resid32(c, c->d.DELTA_ER, c->d.RHS, &l1))) return rc;
-    if ((rc = launch_sweeps32(c, 1))) return rc;  // warm
+    if ((rc = launch_sweeps32(c, 8, 8, -1.0, solver == 3))) return rc;  // warm
   } else if (solver == TTFLD_SOLVER_SOR64_FAST) {
     if ((rc = ensure64(c)) || (rc = prep64(c, c->d.DELTA_ER, c->d.RHS))) return rc;
     if ((rc = launch_sweeps64(c, 1, n + 8, n + 8, -1.0))) return rc;
@@ -635,7 +820,7 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
     if ((rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, 1, n + 8, n + 8, -1.0))) return rc;
   }
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
-  if (solver == TTFLD_SOLVER_MIXED) rc = launch_sweeps32(c, n);
+  if (mixed) rc = launch_sweeps32(c, n, 8, -1.0, solver == 3);
   else if (solver == TTFLD_SOLVER_SOR64_FAST) rc = launch_sweeps64(c, n, n + 8, n + 8, -1.0);
   else rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, n, n + 8, n + 8, -1.0);
   if (rc) return rc;
@@ -643,12 +828,13 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   TT_CHECK(cudaEventSynchronize(c->ev1));
   float t = 0.f;
   TT_CHECK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+  if ((rc = poll(c))) return rc;
   *ms = (double)t / n;
   return 0;
 }
 }  // namespace ttfld
 
 extern "C" int ttfld_time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
-  if (!c || !ms) return TTFLD_E_ARGS;
+  if (!c || !ms || solver < 0 || solver > 3) return TTFLD_E_ARGS;
   return ttfld::time_sweeps(c, solver, n, ms);
 }

@@ -251,6 +251,7 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
   ttfld_solve_stats local{};
   if (!st) st = &local;
   int fallback = 0;
+  bool race = false;
   // the network is trained on a step's first solve; the later (outer
   // iteration) solves of a step start from the previous solution
   int guess = c->opts.guess;
@@ -276,30 +277,35 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
       int rc = unet_guess(c, x, nullptr);
       if (rc) return rc;
     }
-    int rc = rhs_norm(c, d.RHS, &bl1);
-    if (rc) return rc;
-    if ((rc = true_residual(c, x, d.RHS, &gl1))) return rc;
-    st->guess_resid_l1 = gl1;
+    int rc;
     bool reject = false;
     if (c->opts.fallback_rule == 2) {
-      reject = !(gl1 < bl1);  // no better than the zero guess's residual ||b||_1
+      // no better than the zero guess's residual ||b||_1
+      if ((rc = rhs_norm(c, d.RHS, &bl1)) || (rc = true_residual(c, x, d.RHS, &gl1))) return rc;
+      st->guess_resid_l1 = gl1;
+      reject = !(gl1 < bl1);
+    } else if (c->opts.fallback_rule == 0 && c->opts.solver == TTFLD_SOLVER_MIXED) {
+      race = true;  // the mixed solver races the guess against zero itself
     } else if (c->opts.fallback_rule == 0) {
-      // ||b - A x1||_1 after one FP64 red-black sweep from the guess and after
-      // one from zero, on a scratch copy: keep the guess if its first-sweep
-      // residual is the smaller.  (With over-relaxation the first sweep from
-      // zero itself leaves a residual above ||b||_1, so the comparison is
-      // made sweep for sweep.)
+      // two FP64 red-black sweeps from the guess and two from zero, on a
+      // scratch copy: keep the guess if the in-sweep residual norm (RNORM)
+      // of its second sweep -- the residual its first sweep left -- is the
+      // smaller.  (With over-relaxation the first sweep from zero itself
+      // leaves a residual above ||b||_1, so the comparison is made sweep for
+      // sweep rather than against ||b||_1.)
       if (!c->guess_tmp) TT_CHECK(cudaMalloc((void**)&c->guess_tmp, nhalo(d) * 8));
-      double r1[2];
+      double r2[2];
       for (int q = 0; q < 2; ++q) {
         if (q == 0) TT_CHECK(cudaMemcpyAsync(c->guess_tmp, x, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
         else TT_CHECK(cudaMemsetAsync(c->guess_tmp, 0, nhalo(d) * 8, c->stream));
         TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
         if ((rc = rhs_norm(c, d.RHS, nullptr))) return rc;
-        if ((rc = launch_exact_sweeps(c, c->guess_tmp, d.RHS, 1, 3, 3, -1.0))) return rc;
-        if ((rc = true_residual(c, c->guess_tmp, d.RHS, &r1[q]))) return rc;
+        if ((rc = launch_exact_sweeps(c, c->guess_tmp, d.RHS, 2, 3, 3, -1.0))) return rc;
+        TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+        TT_CHECK(cudaStreamSynchronize(c->stream));
+        r2[q] = c->host_sol->rnorm;
       }
-      reject = !(r1[0] < r1[1]);
+      reject = !(r2[0] < r2[1]);
     }
     if (reject) {
       TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
@@ -307,7 +313,9 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
     }
   }
   TT_CHECK(cudaEventRecord(c->evg, c->stream));
-  int rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
+  int rc;
+  if (race) rc = solve_mixed(c, d.DELTA_ER, d.RHS, st, 1, &fallback);
+  else rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));
   float ms = 0.f, gms = 0.f;

@@ -184,7 +184,7 @@ class FLD:
 
     def time_sweeps(self, solver: str, n: int) -> float:
         ms = ctypes.c_double()
-        check("time_sweeps", self.L.ttfld_time_sweeps(self.h, SOLVER[solver], n, ctypes.byref(ms)))
+        check("time_sweeps", self.L.ttfld_time_sweeps(self.h, _ffi.TIMED_SWEEPS[solver], n, ctypes.byref(ms)))
         return ms.value
 
     def synchronize(self):
