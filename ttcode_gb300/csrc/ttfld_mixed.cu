@@ -158,6 +158,14 @@ static int prep32(ttfld_ctx* c) {
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+// Loads of the correction e are plain coherent loads, never the read-only
+// path: the persistent kernel writes e in one half-sweep and reads it, from
+// other SMs, in the next.  The barrier between them (a fence and an acquire
+// by one thread, then a block barrier) orders those loads after the other
+// blocks' writes, as the PTX memory model defines it.
+__device__ __forceinline__ float4 lde4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float lde(const float* p) { return *p; }
+__device__ __forceinline__ float4 ldc4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
 // One colour of FP32 red-black SOR on A e = r (Jacobi-scaled), 4 cells per
 // thread: res = (e + sum a_nb e_nb) - rhat (the reference's in-sweep residual
@@ -168,8 +176,8 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 template <int COL, bool NORM>
 __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
                                           size_t plane, float& nacc) {
-  const float* __restrict__ eo = m.e[1 - COL];
-  float* __restrict__ es = m.e[COL];
+  const float* eo = m.e[1 - COL];
+  float* es = m.e[COL];
   const int hv = (int)(t % nv);
   const long long rr = t / nv;
   const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
@@ -180,26 +188,26 @@ __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float om
   const size_t eb = gslot(g, j0, k0, h0);
   const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
   const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
-  const float4 o = ld4(eo + eb);
+  const float4 aw = ldc4(m.a[0][COL] + cb), ae = ldc4(m.a[1][COL] + cb);
+  const float4 as = ldc4(m.a[2][COL] + cb), an = ldc4(m.a[3][COL] + cb);
+  const float4 ab = ldc4(m.a[4][COL] + cb), at = ldc4(m.a[5][COL] + cb);
+  const float4 r = ldc4(m.rhat[COL] + cb);
+  float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (NORM) dg = ldc4(m.diag[COL] + cb);
+  const float4 o = lde4(eo + eb);
   float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
   if (off == 0) {
-    xm0 = h0 > 0 ? eo[eb - 1] : 0.f; xm1 = o.x; xm2 = o.y; xm3 = o.z;
+    xm0 = h0 > 0 ? lde(eo + eb - 1) : 0.f; xm1 = o.x; xm2 = o.y; xm3 = o.z;
     xp0 = o.x; xp1 = o.y; xp2 = o.z; xp3 = o.w;
   } else {
     xm0 = o.x; xm1 = o.y; xm2 = o.z; xm3 = o.w;
-    xp0 = o.y; xp1 = o.z; xp2 = o.w; xp3 = (h0 + 4 < g.nxp) ? eo[eb + 4] : 0.f;
+    xp0 = o.y; xp1 = o.z; xp2 = o.w; xp3 = (h0 + 4 < g.nxp) ? lde(eo + eb + 4) : 0.f;
   }
-  const float4 s = ld4(eo + gslot(g, jm, k0, h0));
-  const float4 nn = ld4(eo + gslot(g, jp, k0, h0));
-  const float4 b = ld4(eo + eb - plane);
-  const float4 tt = ld4(eo + eb + plane);
-  const float4 e = ld4(es + eb);
-  const float4 aw = ld4(m.a[0][COL] + cb), ae = ld4(m.a[1][COL] + cb);
-  const float4 as = ld4(m.a[2][COL] + cb), an = ld4(m.a[3][COL] + cb);
-  const float4 ab = ld4(m.a[4][COL] + cb), at = ld4(m.a[5][COL] + cb);
-  const float4 r = ld4(m.rhat[COL] + cb);
-  float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (NORM) dg = ld4(m.diag[COL] + cb);
+  const float4 s = lde4(eo + gslot(g, jm, k0, h0));
+  const float4 nn = lde4(eo + gslot(g, jp, k0, h0));
+  const float4 b = lde4(eo + eb - plane);
+  const float4 tt = lde4(eo + eb + plane);
+  const float4 e = lde4(es + eb);
   float4 out;
 #define UPD(L, IDX, XM, XP)                                                                \
   {                                                                                        \
@@ -302,20 +310,20 @@ __device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) 
   return ok_sh != 0;
 }
 
+constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
+
 // nsweeps FP32 sweeps in one launch: both colours of every sweep with a grid
 // barrier after each, every norm_every-th sweep (and the last) with the
 // in-sweep norm.  Each block reduces its partial of a norm sweep; after the
 // barrier every block adds all partials in the same fixed order, so all of
 // them reach the same stop decision and leave the loop together.  Every
 // thread keeps the same items from sweep to sweep.
-constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
-
 __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mix32 m, float omega, SolverDev* sol,
-                                                               double* partials, double stop_ratio, int nsweeps,
-                                                               int norm_every) {
+                                                                      double* partials, double stop_ratio,
+                                                                      int nsweeps, int norm_every) {
   __shared__ double sh[32];
   __shared__ int stop_sh;
-  if (*(volatile int*)&sol->done) return;  // set before the launch, so the same for every block
+  if (*(volatile int*)&sol->done) return;
   const int nv = g.nxp >> 2;
   const long long n = g.rows * nv;
   const size_t plane = (size_t)g.ny * g.nxp;
