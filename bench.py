@@ -112,15 +112,15 @@ class ClockSampler:
 
 
 def load_traffic():
-    """DRAM bytes (read + write) of one sweep32 launch from the committed ncu
-    summary, doubled for the two colours of one sweep (the unit of
+    """DRAM bytes (read + write) per sweep of the persistent FP32 sweep
+    kernel, from the committed ncu summary (one full sweep is the unit of
     `achieved`)."""
-    p = os.path.join(ROOT, "profiles", "sweep32_shell256.md")
+    p = os.path.join(ROOT, "profiles", "sweeps32_persistent_shell256.md")
     if os.path.exists(p):
         with open(p) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return 2 * int(line.split(":")[1])
+                if line.startswith("traffic_bytes_per_sweep:"):
+                    return int(line.split(":")[1])
     return None
 
 
@@ -179,15 +179,37 @@ def flush_l2(torch, buf):
 
 
 def run_profile_solve(args):
-    """One product-path solve and one exact FP64 solve of the shell256
-    system, nothing else (the command the ncu summaries under profiles/ use)."""
+    """For the ncu summaries under profiles/: after the set-up (training
+    included), one product-path solve and one exact FP64 solve of the
+    shell256 system inside cudaProfilerStart/Stop, so that
+    `ncu --profile-from-start off` lists exactly their launches."""
     import torch
     torch.cuda.set_device(0)
     sh, f, _ = build_system(0)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
     for solver, g in (("mixed", "learned"), ("sor64_exact", "zero")):
         f.set_solver(solver, guess=g, tol=1e-10, inner_min=16, inner_max=512)
         st = f.solve_system()
         print(json.dumps({"solver": solver, "guess": g, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    f.close()
+
+
+def run_profile_sweeps(args):
+    """For the ncu capture of the dominant kernel: the shell256 system, then
+    inside cudaProfilerStart/Stop one launch of 8 FP32 sweeps (the warm-up of
+    ttfld_time_sweeps) and one of 16 (in-sweep norm every 8th)."""
+    import torch
+    torch.cuda.set_device(0)
+    sh, f, _ = build_system(0, train=False)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    ms = f.time_sweeps("mixed", 16)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({"ms_per_sweep": ms}), flush=True)
     f.close()
 
 
@@ -437,9 +459,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--profile-solve", action="store_true",
                     help="only build the system and run one mixed and one exact FP64 solve")
+    ap.add_argument("--profile-sweeps", action="store_true",
+                    help="only build the system and run 8 + 16 FP32 sweeps")
     args = ap.parse_args()
     if args.profile_solve:
         run_profile_solve(args)
+        return
+    if args.profile_sweeps:
+        run_profile_sweeps(args)
         return
     if args.warmup < 3:
         args.warmup = 3
