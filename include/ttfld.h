@@ -138,7 +138,7 @@ typedef struct {
   double tol;          /* mixed solver: stop at ||b-Ax||_1/||b||_1 <= tol  */
   int32_t inner_min;   /* mixed solver: FP32 sweeps per correction, bounds */
   int32_t inner_max;
-  int32_t max_sweeps;  /* mixed solver sweep budget (0 = 100*ITMAX)        */
+  int32_t max_sweeps;  /* mixed solver sweep budget (0 = ITMAX)            */
   int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:
                             0 = the residual its first red-black sweep
                                 leaves (the in-sweep norm RNORM of the

@@ -554,7 +554,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   double bl1 = 0.0, l1 = 0.0;
   if ((rc = rhs_norm(c, b, &bl1))) return rc;
   const double tol = c->opts.tol;
-  const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : 100LL * c->d.itmax;
+  const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
   const int period = 8;
   int corrections = 0, status = TTFLD_OK;
   double tight = 1.0;  // halved each time the in-sweep norm met tol but the FP64 residual did not
@@ -600,18 +600,25 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     double r_prev = anchor;
     int it_prev = it0;
     int chunk = 32;
+    bool have_norm = false;  // r_prev is an in-sweep norm (the anchor is a true residual)
     for (;;) {
       if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop))) return rc;
       if ((rc = poll(c))) return rc;
       const SolverDev* h = c->host_sol;
       if (h->nonfinite) { status = TTFLD_E_NONFINITE; break; }
       if (h->done || h->iter >= budget) break;
+      // the in-sweep norm stopped falling over a whole chunk: the FP32
+      // iteration has reached its rounding floor relative to this anchor
+      // (stiff, high-contrast systems put it well above 1e-5), so re-anchor
+      // in FP64; restarting from e = 0 continues the same iteration
+      if (have_norm && h->iter - it_prev >= 16 && !(h->ratio < 0.999 * r_prev)) break;
       // predict the sweeps left from the last two norms; queue about that many
       double rate = (h->iter > it_prev && h->ratio > 0.0 && r_prev > 0.0)
                         ? pow(h->ratio / r_prev, 1.0 / (h->iter - it_prev)) : 0.0;
       double left = (rate > 0.0 && rate < 1.0) ? log(stop / h->ratio) / log(rate) : 64.0;
       r_prev = h->ratio;
       it_prev = h->iter;
+      have_norm = true;
       if (left <= period) chunk = (int)ceil(left) < 1 ? 1 : (int)ceil(left);
       else if (left < 64) chunk = ((int)left / period) * period;
       else chunk = left < 512 ? ((int)(0.75 * left) / period) * period : 384;
