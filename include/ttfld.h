@@ -253,28 +253,43 @@ int ttfld_coupled_energy_eqs(ttfld_ctx* ctx, int do_bounds,
  * call sites, SCALAR's phi halo must be current (PLANETSHIFT(10)) on entry. */
 int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
 
+/* Marks the next solve as the first of an implicit step: with
+ * TTFLD_GUESS_LEARNED it starts from the network's guess, with
+ * TTFLD_GUESS_PREVIOUS from the previous solution unscaled.
+ * ttfld_coupled_energy_eqs does this itself; a caller that runs its own
+ * step loop around ttfld_solve_with_sor calls it at the top of each step.
+ * new_run = 1 also forgets the previous solution (a new run, or a state the
+ * previous solution does not belong to).  No reference counterpart. */
+int ttfld_begin_step(ttfld_ctx* ctx, int new_run);
+
 /* ---- measurement (no reference counterpart) --------------------------- */
 /* Runs n back-to-back sweeps of a solver's sweep kernels on the current
  * system (TTFLD_SOLVER_SOR64_EXACT: DELTA_ER is iterated in place;
  * SOR64_FAST / MIXED: only their private iterate is touched) and returns
  * the mean device time of one full sweep (both colours), CUDA events on the
  * library's stream.  MIXED times the solver's own kernel (all n sweeps in
- * one persistent launch, the in-sweep norm every 8th); solver = 3 times the
- * same FP32 sweeps issued as two launches per sweep, for comparison. */
+ * one persistent launch, the in-sweep norm every 8th); for comparison,
+ * solver = 3 times the same FP32 sweeps issued as two launches per sweep
+ * and solver = 4 as one launch of the TMA-staged persistent kernel. */
 int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 /* Number of kernels this process has launched through libttfld. */
 uint64_t ttfld_kernel_launches(void);
 
 /* ---- learned initial guess (no reference counterpart) ----------------- */
 /* A 3-D U-Net (4 levels, 16-32-64-64 channels, 3x3x3 kernels, BF16 weights
- * and activations, FP32 accumulation on the tensor cores) maps the state of
- * a solve -- log E, log kappa_R, log rho, log dt and the heating -- to
- * delta_ER / E, used as SOLVE_WITH_SOR's initial iterate (TTFLD_GUESS_LEARNED).
- * It is trained on the GPU on pairs captured from this context's own solves. */
+ * and activations, FP32 accumulation on the tensor cores, run at half the
+ * grid's resolution) maps the state of a solve -- log E, log kappa_R,
+ * log rho, log dt, the heating and the previous solve's solution -- to the
+ * correction delta_ER / E on top of that previous solution (zero at a run's
+ * first solve); the sum is SOLVE_WITH_SOR's initial iterate for the first
+ * solve of each implicit step (TTFLD_GUESS_LEARNED; the step's later solves
+ * start from the previous solution).  It is trained on the GPU on pairs
+ * captured from this context's own solves. */
 /* Random (seeded, He-normal) weights for this context's grid. */
 int ttfld_guess_init(ttfld_ctx* ctx, uint64_t seed);
-/* Device storage for up to `capacity` training pairs (5 BF16 inputs, a BF16
- * target and a mask per cell; about 13 B per cell and pair). */
+/* Device storage for up to `capacity` training pairs (16 BF16 inputs per
+ * 2x2x2 cells, a BF16 target and a mask per cell; about 7 B per cell and
+ * pair). */
 int ttfld_guess_dataset(ttfld_ctx* ctx, int capacity);
 /* Store the next solve of this context (its starting state and its answer)
  * as a training pair. */
@@ -283,14 +298,14 @@ int ttfld_guess_dataset_count(ttfld_ctx* ctx);
 /* Adam (lr, beta 0.9/0.999) over the stored pairs, `epochs` seeded passes;
  * mean masked MSE of the normalised target over the steps in *mean_loss. */
 int ttfld_guess_train(ttfld_ctx* ctx, int epochs, double lr, uint64_t seed, double* mean_loss);
-/* Loss and gradient of every parameter for one input (NX*NY*NZ cells x 5
+/* Loss and gradient of every parameter for one input (NX*NY*NZ cells x 6
  * features, r fastest), target and mask -- the hook gradient checks use. */
 int ttfld_guess_gradients(ttfld_ctx* ctx, const float* feat, const float* target,
                           const unsigned char* mask, double* loss, float* grads);
 /* Network output (normalised target units) for one input. */
 int ttfld_guess_predict(ttfld_ctx* ctx, const float* feat, float* pred);
 size_t ttfld_guess_num_params(void);
-/* Weights blob: "TTFLDNN1", uint64 parameter count, FP32 parameters. */
+/* Weights blob: "TTFLDNN2", uint64 parameter count, FP32 parameters. */
 int ttfld_guess_load(ttfld_ctx* ctx, const void* blob, size_t bytes);
 int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
 

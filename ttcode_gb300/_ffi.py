@@ -78,7 +78,7 @@ FIELDS = {
 }
 
 SOLVER = {"sor64_exact": 0, "sor64_fast": 1, "mixed": 2}
-TIMED_SWEEPS = dict(SOLVER, mixed_split=3)   # ttfld_time_sweeps also times the per-colour launches
+TIMED_SWEEPS = dict(SOLVER, mixed_split=3, mixed_tma=4)   # ttfld_time_sweeps also times the per-colour launches
 GUESS = {"zero": 0, "previous": 1, "learned": 2}
 
 STATUS = {0: "ok", 1: "iteration limit reached", 2: "learned guess rejected",
@@ -96,7 +96,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_kernel_launches", "ttfld_sor_solve_noalloc", "ttfld_guess_init",
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
-           "ttfld_guess_num_params")
+           "ttfld_guess_num_params", "ttfld_begin_step")
 
 _lib = None
 
@@ -160,6 +160,7 @@ def lib():
     L.ttfld_guess_train.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, P_double]
     L.ttfld_guess_gradients.argtypes = [vp, vp, vp, vp, P_double, vp]
     L.ttfld_guess_predict.argtypes = [vp, vp, vp]
+    L.ttfld_begin_step.argtypes = [vp, ctypes.c_int]
     L.ttfld_guess_num_params.restype = ctypes.c_size_t
     L.ttfld_guess_num_params.argtypes = []
     L.ttfld_guess_load.argtypes = [vp, vp, ctypes.c_size_t]

@@ -36,7 +36,7 @@ struct SolverDev {
   unsigned int ticket; // last-block-done counter
   unsigned int ticket2;
   int bar_timeout;     // 1 if a grid barrier wait ran out (the kernel gave up)
-  int pad;
+  int stalled;         // 1 if the FP32 inner loop stopped at its rounding floor
 };
 
 // Reduction targets of the outer Newton loop.

@@ -172,10 +172,13 @@ __device__ __forceinline__ float4 ldc4(const float* p) { return *reinterpret_cas
 // divided by A, ppsor.f:64-71), e -= omega * res.  NORM sweeps also sum
 // |A * res| (per thread in FP32, per block and grid in FP64 in a fixed
 // order), i.e. the reference's RNORM (ppsor.f:73) of the iterate x + e.
-// Item t is the t-th group of four colour slots (row-major over (k, j, h)).
+// Item t is the t-th group of four colour slots (row-major over (k, j, h));
+// its coefficients (aw..at: the W E S N B T couplings over A, r: rhat, dg:
+// A) come in as arguments, from global or from shared memory.
 template <int COL, bool NORM>
-__device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
-                                          size_t plane, float& nacc) {
+__device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
+                                           size_t plane, float4 aw, float4 ae, float4 as, float4 an, float4 ab,
+                                           float4 at, float4 r, float4 dg, float& nacc) {
   const float* eo = m.e[1 - COL];
   float* es = m.e[COL];
   const int hv = (int)(t % nv);
@@ -184,16 +187,9 @@ __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float om
   const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
   const int h0 = hv * 4;
   const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
-  const size_t cb = (size_t)rr * g.nxp + h0;
   const size_t eb = gslot(g, j0, k0, h0);
   const int jm = j0 == 0 ? g.ny - 1 : j0 - 1;
   const int jp = j0 == g.ny - 1 ? 0 : j0 + 1;
-  const float4 aw = ldc4(m.a[0][COL] + cb), ae = ldc4(m.a[1][COL] + cb);
-  const float4 as = ldc4(m.a[2][COL] + cb), an = ldc4(m.a[3][COL] + cb);
-  const float4 ab = ldc4(m.a[4][COL] + cb), at = ldc4(m.a[5][COL] + cb);
-  const float4 r = ldc4(m.rhat[COL] + cb);
-  float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (NORM) dg = ldc4(m.diag[COL] + cb);
   const float4 o = lde4(eo + eb);
   float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
   if (off == 0) {
@@ -221,6 +217,21 @@ __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float om
   UPD(x, 0, xm0, xp0) UPD(y, 1, xm1, xp1) UPD(z, 2, xm2, xp2) UPD(w, 3, xm3, xp3)
 #undef UPD
   st4(es + eb, out);
+}
+
+// The same with the coefficients loaded from global memory (item t's four
+// slots are floats 4t .. 4t+3 of each coefficient array).
+template <int COL, bool NORM>
+__device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
+                                          size_t plane, float& nacc) {
+  const size_t cb = (size_t)t * 4;
+  const float4 aw = ldc4(m.a[0][COL] + cb), ae = ldc4(m.a[1][COL] + cb);
+  const float4 as = ldc4(m.a[2][COL] + cb), an = ldc4(m.a[3][COL] + cb);
+  const float4 ab = ldc4(m.a[4][COL] + cb), at = ldc4(m.a[5][COL] + cb);
+  const float4 r = ldc4(m.rhat[COL] + cb);
+  float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (NORM) dg = ldc4(m.diag[COL] + cb);
+  update_vec<COL, NORM>(g, m, omega, t, nv, plane, aw, ae, as, an, ab, at, r, dg, nacc);
 }
 
 // One colour per launch.  NORM launches of the second colour end with the
@@ -275,6 +286,12 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
 // the back-off) or once another block has given up, the block records the
 // timeout and returns false, and the kernel returns without further work.
 constexpr long long kBarrierSpins = 1LL << 23;
+// A norm sweep whose in-sweep ratio is not below kStallFactor times the
+// previous one (8 sweeps earlier) ends the inner loop: the FP32 iteration
+// has reached its rounding floor relative to the anchor (on stiff,
+// high-contrast systems after one or two decades), and re-anchoring in FP64
+// continues the same iteration.  A false alarm costs one FP64 residual.
+constexpr double kStallFactor = 0.999;
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
   unsigned int v;
@@ -320,7 +337,7 @@ constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
 // thread keeps the same items from sweep to sweep.
 __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mix32 m, float omega, SolverDev* sol,
                                                                       double* partials, double stop_ratio,
-                                                                      int nsweeps, int norm_every) {
+                                                                      int nsweeps, int norm_every, int stall_check) {
   __shared__ double sh[32];
   __shared__ int stop_sh;
   if (*(volatile int*)&sol->done) return;
@@ -329,6 +346,7 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
   const size_t plane = (size_t)g.ny * g.nxp;
   const unsigned int nb = gridDim.x;
   const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, ts = (long long)gridDim.x * blockDim.x;
+  double last_ratio = -1.0;  // in-sweep ratio of the previous norm sweep of this launch (thread 0)
   for (int sw = 1; sw <= nsweeps; ++sw) {
     const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
     float nacc = 0.f;
@@ -347,11 +365,15 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
       const double tot = block_sum_array(partials, nb, sh);
       if (threadIdx.x == 0) {
         const double ratio = tot / sol->rhsnorm;
-        const int stop = !isfinite(tot) || !(ratio > stop_ratio);
+        // every block holds the same tot, so all reach the same decision
+        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
+        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
+        last_ratio = ratio;
         if (blockIdx.x == 0) {
           sol->rnorm = tot;
           sol->ratio = ratio;
           if (!isfinite(tot)) sol->nonfinite = 1;
+          if (stall) sol->stalled = 1;
           if (stop) sol->done = 1;
         }
         stop_sh = stop;
@@ -360,6 +382,180 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
       if (stop_sh) return;
     }
   }
+}
+
+// ---- TMA-staged persistent sweeps (measured alternative) -------------------
+// The same sweeps as sweeps32_persistent, with each block's coefficients
+// streamed through shared memory by bulk asynchronous copies
+// (cp.async.bulk, completion on an mbarrier).  Block b owns a contiguous run
+// of items, processed per half-sweep in chunks of kTmaThreads items (one per
+// thread).  Thread 0 keeps kStages chunks in flight: the chunk's six
+// couplings and rhat (and A on norm sweeps) are contiguous spans of 16 bytes
+// per item in every array, one bulk copy each.  The coefficients do not
+// depend on the sweep, so the copies for the next half-sweep are issued
+// before the grid barrier and their latency hides behind it; only the
+// correction e is read through the cache after the barrier.
+constexpr int kTmaThreads = 512;
+constexpr int kStages = 3;
+constexpr int kStageArrays = 8;  // aw ae as an ab at rhat A
+constexpr size_t kStageBytes = (size_t)kStageArrays * kTmaThreads * 16;
+constexpr size_t kTmaSmem = 128 + kStages * kStageBytes;
+constexpr long long kMbarSpins = 1LL << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Bounded wait for phase `parity` of a stage barrier (all threads).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, SolverDev* sol) {
+  long long n = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++n > kMbarSpins) {
+      atomicExch(&sol->bar_timeout, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+struct TmaPlan {
+  long long t0, t1;  // this block's items
+  int nk;            // chunks per half-sweep
+  int per_sweep;     // chunks per sweep (2 nk)
+};
+
+// Thread 0: queue the copies of chunk gi (half-sweep gi / nk, chunk gi % nk)
+// into stage gi % kStages.
+__device__ __forceinline__ void issue_chunk(const Mix32& m, const TmaPlan& pl, long long gi, int norm_every,
+                                            int nsweeps, unsigned char* stages, uint64_t* bars) {
+  const int h = (int)(gi / pl.nk), k = (int)(gi % pl.nk);
+  const int col = h & 1, sw = h / 2 + 1;
+  const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
+  const long long ta = pl.t0 + (long long)k * kTmaThreads;
+  const long long tb = ta + kTmaThreads < pl.t1 ? ta + kTmaThreads : pl.t1;
+  const uint32_t bytes = (uint32_t)(tb - ta) * 16u;
+  const int st = (int)(gi % kStages);
+  unsigned char* base = stages + (size_t)st * kStageBytes;
+  const int na = norm ? 8 : 7;
+  mbar_expect_tx(bars + st, bytes * na);
+  const float* src[8] = {m.a[0][col], m.a[1][col], m.a[2][col], m.a[3][col],
+                         m.a[4][col], m.a[5][col], m.rhat[col], m.diag[col]};
+  for (int q = 0; q < na; ++q)
+    bulk_to_smem(base + (size_t)q * kTmaThreads * 16, src[q] + ta * 4, bytes, bars + st);
+}
+
+__global__ void __launch_bounds__(kTmaThreads) sweeps32_tma(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                            double* partials, double stop_ratio, int nsweeps,
+                                                            int norm_every, int stall_check) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  unsigned char* stages = smem + 128;
+  __shared__ double sh[32];
+  __shared__ int stop_sh;
+  if (*(volatile int*)&sol->done) return;  // set before the launch, so the same for every block
+  const int nv = g.nxp >> 2;
+  const long long n = g.rows * nv;
+  const size_t plane = (size_t)g.ny * g.nxp;
+  const int nb = (int)gridDim.x;
+  TmaPlan pl;
+  pl.t0 = n * blockIdx.x / nb;
+  pl.t1 = n * (blockIdx.x + 1) / nb;
+  pl.nk = (int)((pl.t1 - pl.t0 + kTmaThreads - 1) / kTmaThreads);
+  pl.per_sweep = 2 * pl.nk;
+  const long long total = (long long)pl.per_sweep * nsweeps;  // chunks of this launch
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < kStages; ++q) mbar_init(bars + q, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  long long issued = 0, done_chunks = 0;
+  if (threadIdx.x == 0)
+    for (; issued < kStages && issued < total; ++issued) issue_chunk(m, pl, issued, norm_every, nsweeps, stages, bars);
+  bool ok = true, synced = true;  // no barrier before the launch's first half-sweep
+  double last_ratio = -1.0;       // in-sweep ratio of the previous norm sweep of this launch (thread 0)
+  for (int sw = 1; sw <= nsweeps && ok; ++sw) {
+    const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
+    float nacc = 0.f;
+    for (int col = 0; col < 2 && ok; ++col) {
+      if (!synced && !grid_sync(sol, nb)) { ok = false; break; }
+      synced = false;
+      for (int k = 0; k < pl.nk; ++k) {
+        const int st = (int)(done_chunks % kStages);
+        if (!mbar_wait(bars + st, (uint32_t)((done_chunks / kStages) & 1), sol)) { ok = false; break; }
+        const long long t = pl.t0 + (long long)k * kTmaThreads + threadIdx.x;
+        if (t < pl.t1) {
+          const float4* sb = reinterpret_cast<const float4*>(stages + (size_t)st * kStageBytes) + threadIdx.x;
+          const float4 dg = norm ? sb[7 * kTmaThreads] : make_float4(0.f, 0.f, 0.f, 0.f);
+#define UPD_ARGS g, m, omega, t, nv, plane, sb[0], sb[kTmaThreads], sb[2 * kTmaThreads], sb[3 * kTmaThreads], \
+                 sb[4 * kTmaThreads], sb[5 * kTmaThreads], sb[6 * kTmaThreads], dg, nacc
+          if (col == 0) { if (norm) update_vec<0, true>(UPD_ARGS); else update_vec<0, false>(UPD_ARGS); }
+          else { if (norm) update_vec<1, true>(UPD_ARGS); else update_vec<1, false>(UPD_ARGS); }
+#undef UPD_ARGS
+        }
+        ++done_chunks;
+        __syncthreads();  // the stage is free again
+        if (threadIdx.x == 0 && issued < total) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue_chunk(m, pl, issued, norm_every, nsweeps, stages, bars);
+          ++issued;
+        }
+      }
+    }
+    if (!ok) break;
+    if (norm) {
+      const double sb = block_sum((double)nacc, sh);
+      if (threadIdx.x == 0) partials[blockIdx.x] = sb;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+    if (norm) {
+      if (!grid_sync(sol, nb)) { ok = false; break; }
+      synced = true;
+      const double tot = block_sum_array(partials, nb, sh);
+      if (threadIdx.x == 0) {
+        const double ratio = tot / sol->rhsnorm;
+        // every block holds the same tot, so all reach the same decision
+        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
+        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
+        last_ratio = ratio;
+        if (blockIdx.x == 0) {
+          sol->rnorm = tot;
+          sol->ratio = ratio;
+          if (!isfinite(tot)) sol->nonfinite = 1;
+          if (stall) sol->stalled = 1;
+          if (stop) sol->done = 1;
+        }
+        stop_sh = stop;
+      }
+      __syncthreads();
+      if (stop_sh) break;
+    }
+  }
+  // copies still in flight (issued for chunks that will not run) land before
+  // the block leaves; bounded like every other wait
+  __syncthreads();
+  for (long long c = done_chunks; c < issued; ++c)
+    if (!mbar_wait(bars + (int)(c % kStages), (uint32_t)((c / kStages) & 1), sol)) break;
 }
 
 // x += e over the interior of a halo array (natural layout).
@@ -471,41 +667,63 @@ static int wave_grid(K kernel, long long items) {
   return (int)(need < per_wave ? (need < 1 ? 1 : need) : per_wave);
 }
 
-// Blocks of the persistent kernel: all resident at once (cooperative
-// launch), at most one wave.  0 if cooperative launch is unavailable.
-static int persistent_grid(long long items) {
-  static int coresident = -1;
-  if (coresident < 0) {
-    int dev = 0, sms = 0, per_sm = 0, coop = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweeps32_persistent, kPersistThreads, 0);
-    coresident = coop ? sms * per_sm : 0;
-    if (coresident > kMaxPartials) coresident = kMaxPartials;
+// Blocks of a persistent kernel: all resident at once (cooperative launch),
+// at most one wave.  0 if cooperative launch is unavailable.
+template <class K>
+static int persistent_grid(K kernel, int threads, size_t smem, long long items) {
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
   }
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  long long coresident = coop ? (long long)sms * per_sm : 0;
+  if (coresident > kMaxPartials) coresident = kMaxPartials;
   if (coresident <= 0 || items <= 0) return 0;
-  const long long need = (items + kPersistThreads - 1) / kPersistThreads;
+  const long long need = (items + threads - 1) / threads;
   return (int)(need < coresident ? need : coresident);
 }
 
+enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2 };
+
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
-// evaluates the in-sweep norm against stop_ratio.  One persistent launch
-// where cooperative launch is available, else two launches per sweep.
+// evaluates the in-sweep norm against stop_ratio (and, with stall_check,
+// stops at the FP32 rounding floor).  The product form is one persistent
+// launch; two launches per sweep are the fallback where cooperative launch
+// is unavailable.  The TMA-staged persistent kernel is kept for comparison:
+// it is slower on this workload (the per-chunk block barriers and cache
+// latencies of e outweigh the staged coefficient traffic).
 int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0,
-                    bool split = false) {
+                    SweepForm form = kFormPersistent, bool stall_check = true) {
   MixWork* w = work(c);
   Cmp g = w->g;
   Mix32 m = w->m32;
   long long nvec = g.rows * (g.nxp >> 2);
   float omega = (float)c->d.sorparam;
-  const int pb = split ? 0 : persistent_grid(nvec);
-  if (pb > 0) {
-    SolverDev* sol = c->sol;
-    double* partials = c->partials;
-    void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every};
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent, dim3(pb), dim3(kPersistThreads), args,
-                                         0, c->stream));
+  SolverDev* sol = c->sol;
+  double* partials = c->partials;
+  int stall = stall_check ? 1 : 0;
+  void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall};
+  static int tma_blocks = -1, pers_blocks = -1;
+  static long long sized_for = -1;
+  if (sized_for != nvec) {
+    tma_blocks = persistent_grid(sweeps32_tma, kTmaThreads, kTmaSmem, nvec);
+    pers_blocks = persistent_grid(sweeps32_persistent, kPersistThreads, 0, nvec);
+    sized_for = nvec;
+  }
+  if (form == kFormTma && tma_blocks > 0) {
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma, dim3(tma_blocks), dim3(kTmaThreads), args,
+                                         kTmaSmem, c->stream));
+    count_launches(1);
+    return 0;
+  }
+  if (form != kFormSplit && pers_blocks > 0) {
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent, dim3(pers_blocks), dim3(kPersistThreads),
+                                         args, 0, c->stream));
     count_launches(1);
     return 0;
   }
@@ -821,13 +1039,15 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   if ((rc = rhs_norm(c, c->d.RHS, nullptr))) return rc;
   // TTFLD_SOLVER_MIXED times the solver's kernel (one persistent launch for
-  // the n sweeps); 3 times the same sweeps as two launches per sweep
-  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3;
+  // the n sweeps); 3 the same sweeps as two launches per sweep, 4 as one
+  // launch of the TMA-staged persistent kernel.  No stall test: all n run.
+  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3 || solver == 4;
+  const SweepForm form = solver == 3 ? kFormSplit : (solver == 4 ? kFormTma : kFormPersistent);
   if (mixed) {
     if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
     double l1;
     if ((rc = resid32(c, c->d.DELTA_ER, c->d.RHS, &l1))) return rc;
-    if ((rc = launch_sweeps32(c, 8, 8, -1.0, solver == 3))) return rc;  // warm
+    if ((rc = launch_sweeps32(c, 8, 8, -1.0, form, false))) return rc;  // warm
   } else if (solver == TTFLD_SOLVER_SOR64_FAST) {
     if ((rc = ensure64(c)) || (rc = prep64(c, c->d.DELTA_ER, c->d.RHS))) return rc;
     if ((rc = launch_sweeps64(c, 1, n + 8, n + 8, -1.0))) return rc;
@@ -835,7 +1055,7 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
     if ((rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, 1, n + 8, n + 8, -1.0))) return rc;
   }
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
-  if (mixed) rc = launch_sweeps32(c, n, 8, -1.0, solver == 3);
+  if (mixed) rc = launch_sweeps32(c, n, 8, -1.0, form, false);
   else if (solver == TTFLD_SOLVER_SOR64_FAST) rc = launch_sweeps64(c, n, n + 8, n + 8, -1.0);
   else rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, n, n + 8, n + 8, -1.0);
   if (rc) return rc;
@@ -850,6 +1070,6 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
 }  // namespace ttfld
 
 extern "C" int ttfld_time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
-  if (!c || !ms || solver < 0 || solver > 3) return TTFLD_E_ARGS;
+  if (!c || !ms || solver < 0 || solver > 4) return TTFLD_E_ARGS;
   return ttfld::time_sweeps(c, solver, n, ms);
 }

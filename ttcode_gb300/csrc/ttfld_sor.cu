@@ -379,6 +379,14 @@ int ttfld_true_residual(ttfld_ctx* c, double* l1, double* rhs_l1) {
   return 0;
 }
 
+int ttfld_begin_step(ttfld_ctx* c, int new_run) {
+  if (!c) return TTFLD_E_ARGS;
+  c->solve_idx = 0;
+  c->prev_scale = 1.0;
+  if (new_run) c->have_prev = 0;
+  return 0;
+}
+
 int ttfld_solve_system(ttfld_ctx* c, ttfld_solve_stats* st) {
   if (!c) return TTFLD_E_ARGS;
   c->solve_idx = 0;  // a system solved on its own counts as a step's first solve

@@ -211,7 +211,11 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
   for (;;) {
     ++energy_iter;                                                      // :260
     if ((rc = halo_shift(c, d.ER))) return rc;                          // :264-279
-    if ((rc = asm_calculateflux(c, energy_iter))) return rc;            // :283-285
+    // :283-285.  In the first iteration the fluxes are those of :253-255
+    // already in FLUX_X/Y/Z: E_R, T and rho are unchanged since, the halo
+    // shift just done repeats the one of :230-245, and FLIM at energy_iter
+    // 0 and 1 takes the same branch (:396-402) -- so they are not formed again.
+    if (energy_iter > 1 && (rc = asm_calculateflux(c, energy_iter))) return rc;
     if ((rc = asm_divf(c, d.DIVF, theta))) return rc;
     if ((rc = jacobian(c, theta))) return rc;                           // :287-345
     if ((rc = asm_fill_evalues(c, theta))) return rc;                   // :348

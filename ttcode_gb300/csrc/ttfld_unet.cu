@@ -1,11 +1,13 @@
 // ttfld_unet.cu -- the learned initial guess of SOLVE_WITH_SOR (no reference
 // counterpart): a 3-D U-Net (4 levels, 16-32-64-64 channels, 3x3x3 kernels,
 // periodic in phi, zero-padded in r and theta) that maps the state of a step
-// (log E^n, log kappa_R, log rho, log dt, heating) to the relative energy
-// increment delta_ER / E^n.  It is trained on the GPU by the kernels below on
-// pairs captured from the solver's own solves; SOLVE_WITH_SOR then starts
-// from its prediction instead of zero (ppsor.f:29) and iterates to the same
-// tolerance, falling back to zero when the prediction is not better.
+// (log E^n, log kappa_R, log rho, log dt, heating, previous solution) to the
+// relative energy increment delta_ER / E^n -- as a correction to the
+// previous solve's solution where the run has one.  It is trained on the
+// GPU by the kernels below on pairs captured from the solver's own solves;
+// SOLVE_WITH_SOR then starts from its prediction instead of zero
+// (ppsor.f:29) and iterates to the same tolerance, falling back to zero when
+// the prediction is not better.
 //
 // The network works at half the grid's resolution: the features are
 // averaged over 2x2x2 cells, its four levels are 1/2 .. 1/16 of the grid, and
@@ -36,7 +38,7 @@ namespace ttfld {
 typedef __nv_bfloat16 bf16;
 
 constexpr float kLeak = 0.1f;      // LeakyReLU slope
-constexpr int kFeat = 5;           // input channels
+constexpr int kFeat = 6;           // input channels
 constexpr int kFeatPad = 16;       // padded to one mma K step
 constexpr double kTargetScale = 0.01;  // target = delta_ER / E / 0.01
 
@@ -46,7 +48,7 @@ struct LayerSpec {
 };
 // 0-7 encoder, 8-13 decoder (their inputs are [upsampled | skip] concatenations)
 static const LayerSpec kLayers[14] = {
-    {5, 16, 16, 0},   {16, 16, 16, 0}, {16, 16, 32, 1}, {32, 32, 32, 1}, {32, 32, 64, 2},
+    {kFeat, 16, 16, 0}, {16, 16, 16, 0}, {16, 16, 32, 1}, {32, 32, 32, 1}, {32, 32, 64, 2},
     {64, 64, 64, 2},  {64, 64, 64, 3}, {64, 64, 64, 3}, {128, 128, 64, 2}, {64, 64, 64, 2},
     {96, 96, 32, 1},  {32, 32, 32, 1}, {48, 48, 16, 0}, {16, 16, 16, 0}};
 constexpr int kNumConv = 14;
@@ -607,8 +609,11 @@ __global__ void wgrad_fold_kernel(const float* gpad, int cin, int cin_pad, int c
 // L0 voxel (x,y,z) = interior cell (i,j,k) = (x+1, y+1, z+1)
 // In FP32: the features are rounded to BF16 anyway, and FP64 logarithms
 // would cost more than the network (FP64 is a small fraction of the SM's
-// FP32 rate on this part).
-__device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k, float* f) {
+// FP32 rate on this part).  prev (may be null) is the previous solve's
+// solution, scaled by psc as the previous-solution guess scales it; the
+// network predicts the correction to it, in the target's units.
+__device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k, const double* prev, double psc,
+                                              float* f) {
   const size_t h = hidx(d, i, j, k);
   const float er = fmaxf((float)d.ER[h], 1e-30f);
   f[0] = (log10f(er) + 1.3f) / 0.6f;
@@ -618,6 +623,8 @@ __device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k,
   const float s = (i <= d.nx) ? (float)d.SI[h] : 0.0f;
   const float q = fminf(fmaxf(s * (float)d.delt * 1e4f / er, -1e30f), 1e30f);
   f[4] = asinhf(q) / 5.0f;
+  const float pv = prev ? (float)(psc * prev[h] / d.ER[h] / kTargetScale) : 0.0f;
+  f[5] = fminf(fmaxf(pv, -1e4f), 1e4f);
 }
 
 __device__ __forceinline__ bool cell_active(const Dev& d, int i, int j, int k) {
@@ -897,10 +904,12 @@ size_t max_wpad(const Net* n) {
 }
 
 // Features of the current state averaged over the 2x2x2 cells of each
-// level-0 voxel (BF16, 16 channels, 5 used), and the grid's active-cell mask.
+// level-0 voxel (BF16, 16 channels, 6 used), and the grid's active-cell mask.
 int make_features(ttfld_ctx* c, bf16* feat0, unsigned char* mask) {
   Dev d = c->d;
   const Level l0 = net_of(c)->lv[0];
+  const double* prev = c->have_prev ? c->prev_x : nullptr;
+  const double psc = c->prev_scale;
   launch_box(c->stream, box(0, l0.X - 1, 0, l0.Y - 1, 0, l0.Z - 1), [=] __device__(int x, int y, int z) {
     float acc[kFeat];
     for (int q = 0; q < kFeat; ++q) acc[q] = 0.f;
@@ -909,7 +918,7 @@ int make_features(ttfld_ctx* c, bf16* feat0, unsigned char* mask) {
       const int i = 2 * x + 1 + (q & 1), j = 2 * y + 1 + ((q >> 1) & 1), k = 2 * z + 1 + (q >> 2);
       if (i > d.nx || j > d.ny || k > d.nz) continue;
       float f[kFeat];
-      cell_features(d, i, j, k, f);
+      cell_features(d, i, j, k, prev, psc, f);
       for (int t = 0; t < kFeat; ++t) acc[t] += f[t];
       ++cnt;
       mask[(size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1))] =
@@ -935,7 +944,7 @@ int upload_features(ttfld_ctx* c, const float* feat) {
   for (int z = 0; z < l0.Z; ++z)
     for (int y = 0; y < l0.Y; ++y)
       for (int x = 0; x < l0.X; ++x) {
-        float acc[kFeat] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        float acc[kFeat] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         int cnt = 0;
         for (int q = 0; q < 8; ++q) {
           const int xx = 2 * x + (q & 1), yy = 2 * y + ((q >> 1) & 1), zz = 2 * z + (q >> 2);
@@ -967,7 +976,8 @@ void unet_free(ttfld_ctx* c) {
 }
 
 // Learned initial guess into the interior of x (a halo array, zeroed by the
-// caller): delta_ER = pred * 0.01 * E on the active cells, 0 elsewhere.
+// caller): delta_ER = prev + pred * 0.01 * E on the active cells (prev: the
+// scaled previous solution, 0 at a run's first solve), 0 elsewhere.
 int unet_guess(ttfld_ctx* c, double* x, double* /*resid_l1*/) {
   Net* n = net_of(c);
   if (!n || !n->ready) return TTFLD_E_NOMODEL;
@@ -976,17 +986,21 @@ int unet_guess(ttfld_ctx* c, double* x, double* /*resid_l1*/) {
   Dev d = c->d;
   const float* pred = n->pred;
   const unsigned char* mask = n->mask;
+  const double* prev = c->have_prev ? c->prev_x : nullptr;
+  const double psc = c->prev_scale;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     const size_t v = (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
     const size_t h = hidx(d, i, j, k);
-    x[h] = mask[v] ? (double)pred[v] * kTargetScale * d.ER[h] : 0.0;
+    const double base = prev ? psc * prev[h] : 0.0;
+    x[h] = mask[v] ? base + (double)pred[v] * kTargetScale * d.ER[h] : 0.0;
   });
   TT_CHECK_LAUNCH();
   return 0;
 }
 
 // Called after a solve that should become a training pair: features of the
-// state the solve started from and its solution delta_ER / E as the target.
+// state the solve started from and, as the target, its solution minus the
+// scaled previous solution (0 at a run's first solve), over E.
 int unet_capture(ttfld_ctx* c) {
   Net* n = net_of(c);
   if (!n || !n->capture_next || !n->ds_feat) return 0;
@@ -999,10 +1013,13 @@ int unet_capture(ttfld_ctx* c) {
   int rc = make_features(c, feat, mask);
   if (rc) return rc;
   Dev d = c->d;
+  const double* prev = c->have_prev ? c->prev_x : nullptr;
+  const double psc = c->prev_scale;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     const size_t v = (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
     const size_t h = hidx(d, i, j, k);
-    tgt[v] = __float2bfloat16_rn((float)(d.DELTA_ER[h] / d.ER[h] / kTargetScale));
+    const double base = prev ? psc * prev[h] : 0.0;
+    tgt[v] = __float2bfloat16_rn((float)((d.DELTA_ER[h] - base) / d.ER[h] / kTargetScale));
   });
   TT_CHECK_LAUNCH();
   n->count += 1;
@@ -1149,7 +1166,7 @@ size_t ttfld_guess_num_params(void) {
   return tmp.nparams;
 }
 
-// Weights blob: "TTFLDNN1", uint64 nparams, float params[nparams].
+// Weights blob: "TTFLDNN2", uint64 nparams, float params[nparams].
 int ttfld_guess_save(ttfld_ctx* c, void* blob, size_t bytes, size_t* needed) {
   if (!c) return TTFLD_E_ARGS;
   const size_t np = ttfld_guess_num_params();
@@ -1159,7 +1176,7 @@ int ttfld_guess_save(ttfld_ctx* c, void* blob, size_t bytes, size_t* needed) {
   if (!n || !n->ready) return TTFLD_E_NOMODEL;
   if (!blob) return 0;
   if (bytes < need) return TTFLD_E_ARGS;
-  memcpy(blob, "TTFLDNN1", 8);
+  memcpy(blob, "TTFLDNN2", 8);
   uint64_t np64 = np;
   memcpy((char*)blob + 8, &np64, 8);
   TT_CHECK(cudaMemcpy((char*)blob + 16, n->p, np * 4, cudaMemcpyDeviceToHost));
@@ -1171,7 +1188,7 @@ int ttfld_guess_load(ttfld_ctx* c, const void* blob, size_t bytes) {
   const size_t np = ttfld_guess_num_params();
   uint64_t np64 = 0;
   memcpy(&np64, (const char*)blob + 8, 8);
-  if (memcmp(blob, "TTFLDNN1", 8) != 0 || np64 != np || bytes < 16 + np * 4) return TTFLD_E_ARGS;
+  if (memcmp(blob, "TTFLDNN2", 8) != 0 || np64 != np || bytes < 16 + np * 4) return TTFLD_E_ARGS;
   int rc = ensure_net(c);
   if (rc) return rc;
   Net* n = net_of(c);

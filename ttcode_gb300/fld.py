@@ -167,6 +167,10 @@ class FLD:
         self.params["sorparam"] = w.value
         return w.value
 
+    def begin_step(self, new_run: bool = False):
+        """The next solve is an implicit step's first (ttfld_begin_step)."""
+        check("begin_step", self.L.ttfld_begin_step(self.h, int(new_run)))
+
     def coupled_energy_eqs(self, do_bounds: bool = True) -> _ffi.StepStats:
         st = _ffi.StepStats()
         check("COUPLED_ENERGY_EQS", self.L.ttfld_coupled_energy_eqs(self.h, int(do_bounds), ctypes.byref(st)),

@@ -59,16 +59,31 @@ def reset_state(f: FLD, shell: Shell, case: Case):
     f.bounds()
     f.kappa()
     f.set_params(iii=1)
+    f.begin_step(new_run=True)   # no previous solution belongs to this state
 
 
-def capture_pairs(f: FLD, shell: Shell, cases, solver="mixed", tol=1e-10):
-    """One implicit step per case; the step's first solve becomes a pair."""
+def capture_pairs(f: FLD, shell: Shell, cases, solver="mixed", tol=1e-10, first_solve_only=False,
+                  steps_per_case=1):
+    """For each case, `steps_per_case` consecutive implicit steps from the
+    case's starting state; the first solve of every step becomes a pair (its
+    starting state, the previous step's solution, and its own solution).
+    With first_solve_only (one step per case) the step stops after its first
+    outer iteration: the pair is the same, the rest of the step is not
+    needed for it."""
     L = f.L
-    f.set_solver(solver, guess="zero", tol=tol)
+    itmax = f.params["itmax"]
+    f.set_solver(solver, guess="zero", tol=tol, max_sweeps=itmax if first_solve_only else 0)
     for case in cases:
         reset_state(f, shell, case)
-        check("capture", L.ttfld_guess_capture_next(f.h))
-        f.coupled_energy_eqs(True)
+        for _ in range(1 if first_solve_only else steps_per_case):
+            check("capture", L.ttfld_guess_capture_next(f.h))
+            if first_solve_only:
+                f.set_params(itmax=1)   # one outer iteration; the solve keeps its own budget
+                st = _ffi.StepStats()
+                check("capture step", L.ttfld_coupled_energy_eqs(f.h, 1, ctypes.byref(st)), ok=(0, 1, 2))
+                f.set_params(itmax=itmax)
+            else:
+                f.coupled_energy_eqs(True)
     return L.ttfld_guess_dataset_count(f.h)
 
 
