@@ -143,11 +143,15 @@ typedef struct {
                             0 = the residual its first red-black sweep
                                 leaves (the in-sweep norm RNORM of the
                                 second sweep) is not below the one the
-                                first sweep from zero leaves; the mixed
-                                solver runs this test with its own FP32
-                                sweeps and keeps the winner's two sweeps;
+                                first sweep from zero leaves;
                             1 = never;
-                            2 = ||b - A x0||_1 >= ||b||_1                  */
+                            2 = ||b - A x0||_1 >= ||b||_1;
+                            3 = (default) as 0 after four sweeps (RNORM of
+                                the fifth): robust to the cell-scale error
+                                of a good guess, which the first sweep has
+                                not yet removed.
+                            The mixed solver runs tests 0 and 3 with its own
+                            FP32 sweeps and keeps the winner's sweeps.   */
 } ttfld_solve_opts;
 
 typedef struct {
@@ -253,13 +257,13 @@ int ttfld_coupled_energy_eqs(ttfld_ctx* ctx, int do_bounds,
  * call sites, SCALAR's phi halo must be current (PLANETSHIFT(10)) on entry. */
 int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
 
-/* Marks the next solve as the first of an implicit step: with
- * TTFLD_GUESS_LEARNED it starts from the network's guess, with
- * TTFLD_GUESS_PREVIOUS from the previous solution unscaled.
- * ttfld_coupled_energy_eqs does this itself; a caller that runs its own
- * step loop around ttfld_solve_with_sor calls it at the top of each step.
- * new_run = 1 also forgets the previous solution (a new run, or a state the
- * previous solution does not belong to).  No reference counterpart. */
+/* Marks the next solve as the first of an implicit step: it starts from the
+ * previous solution unscaled (TTFLD_GUESS_PREVIOUS, and TTFLD_GUESS_LEARNED
+ * once the run has one).  ttfld_coupled_energy_eqs does this itself; a
+ * caller that runs its own step loop around ttfld_solve_with_sor calls it at
+ * the top of each step.  new_run = 1 also forgets the previous solution (a
+ * new run, or a state it does not belong to): the next solve then starts
+ * from the learned guess or zero.  No reference counterpart. */
 int ttfld_begin_step(ttfld_ctx* ctx, int new_run);
 
 /* ---- measurement (no reference counterpart) --------------------------- */
@@ -279,12 +283,12 @@ uint64_t ttfld_kernel_launches(void);
 /* A 3-D U-Net (4 levels, 16-32-64-64 channels, 3x3x3 kernels, BF16 weights
  * and activations, FP32 accumulation on the tensor cores, run at half the
  * grid's resolution) maps the state of a solve -- log E, log kappa_R,
- * log rho, log dt, the heating and the previous solve's solution -- to the
- * correction delta_ER / E on top of that previous solution (zero at a run's
- * first solve); the sum is SOLVE_WITH_SOR's initial iterate for the first
- * solve of each implicit step (TTFLD_GUESS_LEARNED; the step's later solves
- * start from the previous solution).  It is trained on the GPU on pairs
- * captured from this context's own solves. */
+ * log rho, log dt and the heating -- to delta_ER / E, SOLVE_WITH_SOR's
+ * initial iterate where the run has no previous solution yet (its first
+ * solve, or after ttfld_begin_step(ctx, 1)); with TTFLD_GUESS_LEARNED the
+ * solves after that start from the previous solution, which over a run is
+ * the better guess.  It is trained on the GPU on pairs captured from this
+ * context's own solves. */
 /* Random (seeded, He-normal) weights for this context's grid. */
 int ttfld_guess_init(ttfld_ctx* ctx, uint64_t seed);
 /* Device storage for up to `capacity` training pairs (16 BF16 inputs per
@@ -298,7 +302,7 @@ int ttfld_guess_dataset_count(ttfld_ctx* ctx);
 /* Adam (lr, beta 0.9/0.999) over the stored pairs, `epochs` seeded passes;
  * mean masked MSE of the normalised target over the steps in *mean_loss. */
 int ttfld_guess_train(ttfld_ctx* ctx, int epochs, double lr, uint64_t seed, double* mean_loss);
-/* Loss and gradient of every parameter for one input (NX*NY*NZ cells x 6
+/* Loss and gradient of every parameter for one input (NX*NY*NZ cells x 5
  * features, r fastest), target and mask -- the hook gradient checks use. */
 int ttfld_guess_gradients(ttfld_ctx* ctx, const float* feat, const float* target,
                           const unsigned char* mask, double* loss, float* grads);

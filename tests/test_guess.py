@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-LAYERS = [(6, 16), (16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (64, 64), (64, 64),
+LAYERS = [(5, 16), (16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (64, 64), (64, 64),
           (128, 64), (64, 64), (96, 32), (32, 32), (48, 16), (16, 16)]
 
 
@@ -90,7 +90,7 @@ def torch_reference(params, feat, target, mask, X, Y, Z):
         y = x.repeat_interleave(2, 2).repeat_interleave(2, 3).repeat_interleave(2, 4)
         return y[:, :, :like.shape[2], :like.shape[3], :like.shape[4]]
 
-    f = torch.tensor(feat.reshape(Z, Y, X, 6), dtype=torch.float64).permute(3, 0, 1, 2)[None]
+    f = torch.tensor(feat.reshape(Z, Y, X, 5), dtype=torch.float64).permute(3, 0, 1, 2)[None]
     f = pool(f)                     # averaged over 2x2x2 cells, then BF16: the network runs at half resolution
     s0 = conv(conv(f, 0), 1)
     s1 = conv(conv(pool(s0), 2), 3)
@@ -126,7 +126,7 @@ def test_gradients_match_cpu_reference():
     params = np.frombuffer(blob[16:], dtype=np.float32).astype(np.float64)
     rng = np.random.default_rng(0)
     V = X * Y * Z
-    feat = rng.uniform(-1, 1, (V, 6)).astype(np.float32)
+    feat = rng.uniform(-1, 1, (V, 5)).astype(np.float32)
     target = rng.normal(0, 1, V).astype(np.float32)
     mask = (rng.random(V) < 0.8).astype(np.uint8)
     n = guess.num_params()
@@ -155,7 +155,7 @@ def test_gradients_match_cpu_reference():
 def test_trained_guess_saves_sweeps():
     """Train on 16 solver-generated pairs (random irradiation, dt in [50,500] s)
     on the 100x256x128 shell; on 3 held-out cases the learned guess passes
-    the first-sweep test (no fallback) and needs fewer sweeps to
+    the fallback test (no fallback) and needs fewer sweeps to
     ||b-Ax||_1/||b||_1 <= 1e-10 than the zero guess, for the same answer."""
     from ttcode_gb300 import guess
     from ttcode_gb300.fld import start_run

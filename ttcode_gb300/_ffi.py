@@ -46,7 +46,7 @@ class SolveOpts(ctypes.Structure):
                 ("fallback_rule", c_int32)]
 
 
-FALLBACK = {"first_sweep": 0, "never": 1, "residual": 2}
+FALLBACK = {"first_sweep": 0, "never": 1, "residual": 2, "four_sweeps": 3}
 
 
 class SolveStats(ctypes.Structure):

@@ -186,6 +186,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   c->opts.tol = 1e-10;
   c->opts.inner_min = 8;
   c->opts.inner_max = 256;
+  c->opts.fallback_rule = 3;
   c->prev_scale = 0.9;
   Dev& d = c->d;
   d.nx = dims->nx; d.ny = dims->ny; d.nz = dims->nz;
@@ -308,6 +309,7 @@ int ttfld_set_solver(ttfld_ctx* c, const ttfld_solve_opts* o) {
   if (!c || !o) return TTFLD_E_ARGS;
   if (o->solver < 0 || o->solver > 2 || o->guess < 0 || o->guess > 2) return TTFLD_E_ARGS;
   if (o->solver == TTFLD_SOLVER_MIXED && !(o->tol > 0.0)) return TTFLD_E_ARGS;
+  if (o->fallback_rule < 0 || o->fallback_rule > 3) return TTFLD_E_ARGS;
   c->opts = *o;
   if (c->opts.inner_min < 1) c->opts.inner_min = 1;
   if (c->opts.inner_max < c->opts.inner_min) c->opts.inner_max = c->opts.inner_min;

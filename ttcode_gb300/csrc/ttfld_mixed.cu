@@ -758,10 +758,10 @@ static int poll(ttfld_ctx* c) {
 // the anchor (well inside FP32 precision) or reached tol, x += e, repeat;
 // stop when the FP64 ||b - A x||_1 / ||b||_1 <= tol.
 //
-// With guess_test, x holds a previous or learned initial guess that must
-// beat the zero guess: two sweeps are run from zero and two from the guess,
-// and the in-sweep norm of each second sweep (the residual the first sweep
-// left) decides.  The guess keeps its two sweeps and its residual as the
+// With guess_test = n > 0, x holds a previous or learned initial guess that
+// must beat the zero guess: n sweeps are run from zero and n from the guess,
+// and the in-sweep norm of each n-th sweep (the residual the sweeps before
+// it left) decides.  The guess keeps its n sweeps and its residual as the
 // first anchor; a rejected guess is replaced by zero (*fallback = 1).
 int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
   int rc;
@@ -782,13 +782,13 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   if (guess_test) {
     if ((rc = rhat_of_b(c, b))) return rc;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
-    if ((rc = launch_sweeps32(c, 2, 2, -1.0)) || (rc = poll(c))) return rc;
+    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0)) || (rc = poll(c))) return rc;
     const double r_zero = c->host_sol->rnorm;
     TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
     if ((rc = resid32(c, x, b, &l1))) return rc;
     if (st) st->guess_resid_l1 = l1;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
-    if ((rc = launch_sweeps32(c, 2, 2, -1.0)) || (rc = poll(c))) return rc;
+    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0)) || (rc = poll(c))) return rc;
     const double r_guess = c->host_sol->rnorm;
     if (r_guess < r_zero) {
       resume = true;

@@ -252,11 +252,13 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
   if (!st) st = &local;
   int fallback = 0;
   bool race = false;
-  // the network is trained on a step's first solve; the later (outer
-  // iteration) solves of a step start from the previous solution
+  // the network makes the guess where the run has no previous solution (its
+  // first solve, or after ttfld_begin_step(ctx, 1)); once there is one, the
+  // previous solution is the better guess (it beats the network's
+  // two-to-three-digit prediction over a run), so it is used instead
   int guess = c->opts.guess;
   if (guess == TTFLD_GUESS_LEARNED && !c->have_model) return TTFLD_E_NOMODEL;
-  if (guess == TTFLD_GUESS_LEARNED && c->solve_idx > 0) guess = TTFLD_GUESS_PREVIOUS;
+  if (guess == TTFLD_GUESS_LEARNED && (c->solve_idx > 0 || c->have_prev)) guess = TTFLD_GUESS_PREVIOUS;
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
   if (guess == TTFLD_GUESS_ZERO || (guess == TTFLD_GUESS_PREVIOUS && !c->have_prev)) {
     TT_CHECK(cudaMemsetAsync(d.DELTA_ER, 0, nhalo(d) * 8, c->stream));  // ppsor.f:29
@@ -279,20 +281,23 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
     }
     int rc;
     bool reject = false;
+    // rule 0: the residual the first sweep leaves (RNORM of sweep 2); rule 3:
+    // the residual four sweeps leave (RNORM of sweep 5)
+    const int race_sweeps = c->opts.fallback_rule == 0 ? 2 : (c->opts.fallback_rule == 3 ? 5 : 0);
     if (c->opts.fallback_rule == 2) {
       // no better than the zero guess's residual ||b||_1
       if ((rc = rhs_norm(c, d.RHS, &bl1)) || (rc = true_residual(c, x, d.RHS, &gl1))) return rc;
       st->guess_resid_l1 = gl1;
       reject = !(gl1 < bl1);
-    } else if (c->opts.fallback_rule == 0 && c->opts.solver == TTFLD_SOLVER_MIXED) {
+    } else if (race_sweeps > 0 && c->opts.solver == TTFLD_SOLVER_MIXED) {
       race = true;  // the mixed solver races the guess against zero itself
-    } else if (c->opts.fallback_rule == 0) {
-      // two FP64 red-black sweeps from the guess and two from zero, on a
-      // scratch copy: keep the guess if the in-sweep residual norm (RNORM)
-      // of its second sweep -- the residual its first sweep left -- is the
-      // smaller.  (With over-relaxation the first sweep from zero itself
-      // leaves a residual above ||b||_1, so the comparison is made sweep for
-      // sweep rather than against ||b||_1.)
+    } else if (race_sweeps > 0) {
+      // race_sweeps FP64 red-black sweeps from the guess and as many from
+      // zero, on a scratch copy: keep the guess if the in-sweep residual
+      // norm (RNORM) of its last sweep -- the residual the sweeps before it
+      // left -- is the smaller.  (With over-relaxation the first sweep from
+      // zero itself leaves a residual above ||b||_1, so the comparison is
+      // made sweep for sweep rather than against ||b||_1.)
       if (!c->guess_tmp) TT_CHECK(cudaMalloc((void**)&c->guess_tmp, nhalo(d) * 8));
       double r2[2];
       for (int q = 0; q < 2; ++q) {
@@ -300,7 +305,8 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
         else TT_CHECK(cudaMemsetAsync(c->guess_tmp, 0, nhalo(d) * 8, c->stream));
         TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
         if ((rc = rhs_norm(c, d.RHS, nullptr))) return rc;
-        if ((rc = launch_exact_sweeps(c, c->guess_tmp, d.RHS, 2, 3, 3, -1.0))) return rc;
+        if ((rc = launch_exact_sweeps(c, c->guess_tmp, d.RHS, race_sweeps, race_sweeps + 1, race_sweeps + 1, -1.0)))
+          return rc;
         TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
         TT_CHECK(cudaStreamSynchronize(c->stream));
         r2[q] = c->host_sol->rnorm;
@@ -314,7 +320,7 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
   }
   TT_CHECK(cudaEventRecord(c->evg, c->stream));
   int rc;
-  if (race) rc = solve_mixed(c, d.DELTA_ER, d.RHS, st, 1, &fallback);
+  if (race) rc = solve_mixed(c, d.DELTA_ER, d.RHS, st, c->opts.fallback_rule == 3 ? 5 : 2, &fallback);
   else rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));

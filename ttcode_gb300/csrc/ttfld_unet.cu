@@ -1,13 +1,12 @@
 // ttfld_unet.cu -- the learned initial guess of SOLVE_WITH_SOR (no reference
 // counterpart): a 3-D U-Net (4 levels, 16-32-64-64 channels, 3x3x3 kernels,
 // periodic in phi, zero-padded in r and theta) that maps the state of a step
-// (log E^n, log kappa_R, log rho, log dt, heating, previous solution) to the
-// relative energy increment delta_ER / E^n -- as a correction to the
-// previous solve's solution where the run has one.  It is trained on the
-// GPU by the kernels below on pairs captured from the solver's own solves;
-// SOLVE_WITH_SOR then starts from its prediction instead of zero
-// (ppsor.f:29) and iterates to the same tolerance, falling back to zero when
-// the prediction is not better.
+// (log E^n, log kappa_R, log rho, log dt, heating) to the relative energy
+// increment delta_ER / E^n.  It is trained on the GPU by the kernels below
+// on pairs captured from the solver's own solves; SOLVE_WITH_SOR then starts
+// a run's first solve from its prediction instead of zero (ppsor.f:29) and
+// iterates to the same tolerance, falling back to zero when the prediction
+// is not better.
 //
 // The network works at half the grid's resolution: the features are
 // averaged over 2x2x2 cells, its four levels are 1/2 .. 1/16 of the grid, and
@@ -38,7 +37,7 @@ namespace ttfld {
 typedef __nv_bfloat16 bf16;
 
 constexpr float kLeak = 0.1f;      // LeakyReLU slope
-constexpr int kFeat = 6;           // input channels
+constexpr int kFeat = 5;           // input channels
 constexpr int kFeatPad = 16;       // padded to one mma K step
 constexpr double kTargetScale = 0.01;  // target = delta_ER / E / 0.01
 
@@ -200,8 +199,132 @@ __global__ void __launch_bounds__(256) conv3_fwd_kernel(ConvArgs a) {
   }
 }
 
+// Shared-memory tiled form for the large levels (few channels, many
+// voxels): a CTA computes 16 (x) x 8 (y) x 2 (z) output voxels and all
+// output channels.  The input tile with its one-voxel halo (18 x 10 x 4
+// voxels) and, when they fit, the weights are staged in shared memory with
+// every voxel/weight row padded by 8 channels, so that the 8 rows an
+// A/B-fragment read touches fall in distinct banks.  Warp w computes rows
+// (y0 + w, z0) and (y0 + w, z0 + 1), reusing each weight fragment for both.
+// Each input voxel is then read from global memory about 2.8 times (the
+// halo) instead of once per tap through the caches.
+constexpr int kTX = 16, kTY = 8, kTZ = 2;
+constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2;
+constexpr int kHalo = kHX * kHY * kHZ;
+
+static size_t conv_smem_bytes(int cin, int cout, bool with_w) {
+  size_t b = (size_t)kHalo * (cin + 8) * 2;
+  if (with_w) b += (size_t)27 * cout * (cin + 8) * 2;
+  return b;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(256) conv3_smem_kernel(ConvArgs a, int w_in_smem) {
+  extern __shared__ __align__(16) unsigned char csm[];
+  const int cst = a.cin + 8;  // padded row, in bf16
+  bf16* tin = reinterpret_cast<bf16*>(csm);
+  bf16* tw = tin + (size_t)kHalo * cst;
+  const int XT = (a.X + kTX - 1) / kTX, YT = (a.Y + kTY - 1) / kTY;
+  const int bx = (int)(blockIdx.x % XT), by = (int)((blockIdx.x / XT) % YT), bz = (int)(blockIdx.x / (XT * YT));
+  const int x0 = bx * kTX, y0 = by * kTY, z0 = bz * kTZ;
+  const int c8n = a.cin >> 3;
+  for (int q = threadIdx.x; q < kHalo * c8n; q += blockDim.x) {
+    const int c8 = q % c8n, hv = q / c8n;
+    const int hx = hv % kHX, hy = (hv / kHX) % kHY, hz = hv / (kHX * kHY);
+    const int x = x0 + hx - 1, z = z0 + hz - 1;
+    const int y = ((y0 + hy - 1) % a.Y + a.Y) % a.Y;  // periodic phi
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (x >= 0 && x < a.X && z >= 0 && z < a.Z)
+      v = *reinterpret_cast<const uint4*>(a.in + (((size_t)z * a.Y + y) * a.X + x) * a.in_cs + a.in_co + c8 * 8);
+    *reinterpret_cast<uint4*>(tin + (size_t)hv * cst + c8 * 8) = v;
+  }
+  if (w_in_smem) {
+    const int rows = 27 * a.cout;
+    for (int q = threadIdx.x; q < rows * c8n; q += blockDim.x) {
+      const int c8 = q % c8n, row = q / c8n;
+      *reinterpret_cast<uint4*>(tw + (size_t)row * cst + c8 * 8) =
+          *reinterpret_cast<const uint4*>(a.w + (size_t)row * a.cin + c8 * 8);
+    }
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = lane >> 2, cq = (lane & 3) * 2;
+  const bf16* wbase = w_in_smem ? tw : a.w;
+  const int wst = w_in_smem ? cst : a.cin;
+  float acc[2][NB][4];
+#pragma unroll
+  for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+    for (int nb = 0; nb < NB; ++nb) acc[zz][nb][0] = acc[zz][nb][1] = acc[zz][nb][2] = acc[zz][nb][3] = 0.f;
+  for (int tap = 0; tap < 27; ++tap) {
+    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // 0..2: halo offsets
+    const bf16* p0 = tin + ((size_t)((0 + dz) * kHY + (w + dy)) * kHX + r + dx) * cst + cq;
+    const bf16* p1 = tin + ((size_t)((1 + dz) * kHY + (w + dy)) * kHX + r + dx) * cst + cq;
+    const bf16* wt = wbase + (size_t)tap * a.cout * wst;
+    for (int kc = 0; kc < a.cin; kc += 16) {
+      const uint32_t a00 = ld32(p0 + kc), a01 = ld32(p0 + 8 * cst + kc);
+      const uint32_t a02 = ld32(p0 + kc + 8), a03 = ld32(p0 + 8 * cst + kc + 8);
+      const uint32_t a10 = ld32(p1 + kc), a11 = ld32(p1 + 8 * cst + kc);
+      const uint32_t a12 = ld32(p1 + kc + 8), a13 = ld32(p1 + 8 * cst + kc + 8);
+#pragma unroll
+      for (int nb = 0; nb < NB; ++nb) {
+        const bf16* wp = wt + (size_t)(nb * 8 + r) * wst + kc + cq;
+        const uint32_t b0 = ld32(wp), b1 = ld32(wp + 8);
+        mma_bf16(acc[0][nb], a00, a01, a02, a03, b0, b1);
+        mma_bf16(acc[1][nb], a10, a11, a12, a13, b0, b1);
+      }
+    }
+  }
+  const int y = y0 + w;
+  if (y >= a.Y) return;
+#pragma unroll
+  for (int zz = 0; zz < 2; ++zz) {
+    const int z = z0 + zz;
+    if (z >= a.Z) continue;
+    const size_t rowo = ((size_t)z * a.Y + y) * a.X;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int x = x0 + r + half * 8;
+      if (x >= a.X) continue;
+      bf16* po = a.out + (rowo + x) * a.out_cs + a.out_co + cq;
+#pragma unroll
+      for (int nb = 0; nb < NB; ++nb) {
+        float v0 = acc[zz][nb][half * 2], v1 = acc[zz][nb][half * 2 + 1];
+        const int ch = nb * 8 + cq;
+        if (a.bias) { v0 += a.bias[ch]; v1 += a.bias[ch + 1]; }
+        if (a.act) { v0 = v0 > 0.f ? v0 : kLeak * v0; v1 = v1 > 0.f ? v1 : kLeak * v1; }
+        bf16* q = po + nb * 8;
+        if (a.accum) { v0 += __bfloat162float(q[0]); v1 += __bfloat162float(q[1]); }
+        *reinterpret_cast<uint32_t*>(q) = pack2(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
+      }
+    }
+  }
+}
+
+template <int NB>
+static int launch_conv_smem(cudaStream_t s, const ConvArgs& a) {
+  bool with_w = conv_smem_bytes(a.cin, a.cout, true) <= 100 * 1024;
+  const size_t smem = conv_smem_bytes(a.cin, a.cout, with_w);
+  static size_t opted = 0;
+  if (smem > 48 * 1024 && smem > opted) {
+    if (cudaFuncSetAttribute(conv3_smem_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024) !=
+        cudaSuccess)
+      return TTFLD_E_CUDA;
+    opted = 128 * 1024;
+  }
+  const long long blocks = (long long)((a.X + kTX - 1) / kTX) * ((a.Y + kTY - 1) / kTY) * ((a.Z + kTZ - 1) / kTZ);
+  conv3_smem_kernel<NB><<<(unsigned)blocks, 256, smem, s>>>(a, with_w ? 1 : 0);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
 static int conv_fwd(cudaStream_t s, const ConvArgs& a) {
   if (a.cin % 16 || a.cout % 16 || a.in_cs % 2 || a.in_co % 2 || a.out_cs % 2 || a.out_co % 2) return TTFLD_E_ARGS;
+  if (a.cin <= 48 && a.in_cs % 8 == 0 && a.in_co % 8 == 0) {
+    if (a.cout == 16) return launch_conv_smem<2>(s, a);
+    if (a.cout == 32) return launch_conv_smem<4>(s, a);
+  }
   const long long tiles = (long long)((a.X + 15) >> 4) * a.Y * a.Z * (a.cout / 16);
   // split the taps over more warps until about two waves of warps are busy
   int ks = 1;
@@ -609,11 +732,8 @@ __global__ void wgrad_fold_kernel(const float* gpad, int cin, int cin_pad, int c
 // L0 voxel (x,y,z) = interior cell (i,j,k) = (x+1, y+1, z+1)
 // In FP32: the features are rounded to BF16 anyway, and FP64 logarithms
 // would cost more than the network (FP64 is a small fraction of the SM's
-// FP32 rate on this part).  prev (may be null) is the previous solve's
-// solution, scaled by psc as the previous-solution guess scales it; the
-// network predicts the correction to it, in the target's units.
-__device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k, const double* prev, double psc,
-                                              float* f) {
+// FP32 rate on this part).
+__device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k, float* f) {
   const size_t h = hidx(d, i, j, k);
   const float er = fmaxf((float)d.ER[h], 1e-30f);
   f[0] = (log10f(er) + 1.3f) / 0.6f;
@@ -623,8 +743,6 @@ __device__ __forceinline__ void cell_features(const Dev& d, int i, int j, int k,
   const float s = (i <= d.nx) ? (float)d.SI[h] : 0.0f;
   const float q = fminf(fmaxf(s * (float)d.delt * 1e4f / er, -1e30f), 1e30f);
   f[4] = asinhf(q) / 5.0f;
-  const float pv = prev ? (float)(psc * prev[h] / d.ER[h] / kTargetScale) : 0.0f;
-  f[5] = fminf(fmaxf(pv, -1e4f), 1e4f);
 }
 
 __device__ __forceinline__ bool cell_active(const Dev& d, int i, int j, int k) {
@@ -904,12 +1022,10 @@ size_t max_wpad(const Net* n) {
 }
 
 // Features of the current state averaged over the 2x2x2 cells of each
-// level-0 voxel (BF16, 16 channels, 6 used), and the grid's active-cell mask.
+// level-0 voxel (BF16, 16 channels, 5 used), and the grid's active-cell mask.
 int make_features(ttfld_ctx* c, bf16* feat0, unsigned char* mask) {
   Dev d = c->d;
   const Level l0 = net_of(c)->lv[0];
-  const double* prev = c->have_prev ? c->prev_x : nullptr;
-  const double psc = c->prev_scale;
   launch_box(c->stream, box(0, l0.X - 1, 0, l0.Y - 1, 0, l0.Z - 1), [=] __device__(int x, int y, int z) {
     float acc[kFeat];
     for (int q = 0; q < kFeat; ++q) acc[q] = 0.f;
@@ -918,7 +1034,7 @@ int make_features(ttfld_ctx* c, bf16* feat0, unsigned char* mask) {
       const int i = 2 * x + 1 + (q & 1), j = 2 * y + 1 + ((q >> 1) & 1), k = 2 * z + 1 + (q >> 2);
       if (i > d.nx || j > d.ny || k > d.nz) continue;
       float f[kFeat];
-      cell_features(d, i, j, k, prev, psc, f);
+      cell_features(d, i, j, k, f);
       for (int t = 0; t < kFeat; ++t) acc[t] += f[t];
       ++cnt;
       mask[(size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1))] =
@@ -944,7 +1060,7 @@ int upload_features(ttfld_ctx* c, const float* feat) {
   for (int z = 0; z < l0.Z; ++z)
     for (int y = 0; y < l0.Y; ++y)
       for (int x = 0; x < l0.X; ++x) {
-        float acc[kFeat] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float acc[kFeat] = {0.f, 0.f, 0.f, 0.f, 0.f};
         int cnt = 0;
         for (int q = 0; q < 8; ++q) {
           const int xx = 2 * x + (q & 1), yy = 2 * y + ((q >> 1) & 1), zz = 2 * z + (q >> 2);
@@ -976,8 +1092,7 @@ void unet_free(ttfld_ctx* c) {
 }
 
 // Learned initial guess into the interior of x (a halo array, zeroed by the
-// caller): delta_ER = prev + pred * 0.01 * E on the active cells (prev: the
-// scaled previous solution, 0 at a run's first solve), 0 elsewhere.
+// caller): delta_ER = pred * 0.01 * E on the active cells, 0 elsewhere.
 int unet_guess(ttfld_ctx* c, double* x, double* /*resid_l1*/) {
   Net* n = net_of(c);
   if (!n || !n->ready) return TTFLD_E_NOMODEL;
@@ -986,21 +1101,17 @@ int unet_guess(ttfld_ctx* c, double* x, double* /*resid_l1*/) {
   Dev d = c->d;
   const float* pred = n->pred;
   const unsigned char* mask = n->mask;
-  const double* prev = c->have_prev ? c->prev_x : nullptr;
-  const double psc = c->prev_scale;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     const size_t v = (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
     const size_t h = hidx(d, i, j, k);
-    const double base = prev ? psc * prev[h] : 0.0;
-    x[h] = mask[v] ? base + (double)pred[v] * kTargetScale * d.ER[h] : 0.0;
+    x[h] = mask[v] ? (double)pred[v] * kTargetScale * d.ER[h] : 0.0;
   });
   TT_CHECK_LAUNCH();
   return 0;
 }
 
 // Called after a solve that should become a training pair: features of the
-// state the solve started from and, as the target, its solution minus the
-// scaled previous solution (0 at a run's first solve), over E.
+// state the solve started from and its solution delta_ER / E as the target.
 int unet_capture(ttfld_ctx* c) {
   Net* n = net_of(c);
   if (!n || !n->capture_next || !n->ds_feat) return 0;
@@ -1013,13 +1124,10 @@ int unet_capture(ttfld_ctx* c) {
   int rc = make_features(c, feat, mask);
   if (rc) return rc;
   Dev d = c->d;
-  const double* prev = c->have_prev ? c->prev_x : nullptr;
-  const double psc = c->prev_scale;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     const size_t v = (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
     const size_t h = hidx(d, i, j, k);
-    const double base = prev ? psc * prev[h] : 0.0;
-    tgt[v] = __float2bfloat16_rn((float)((d.DELTA_ER[h] - base) / d.ER[h] / kTargetScale));
+    tgt[v] = __float2bfloat16_rn((float)(d.DELTA_ER[h] / d.ER[h] / kTargetScale));
   });
   TT_CHECK_LAUNCH();
   n->count += 1;

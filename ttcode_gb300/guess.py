@@ -66,7 +66,7 @@ def capture_pairs(f: FLD, shell: Shell, cases, solver="mixed", tol=1e-10, first_
                   steps_per_case=1):
     """For each case, `steps_per_case` consecutive implicit steps from the
     case's starting state; the first solve of every step becomes a pair (its
-    starting state, the previous step's solution, and its own solution).
+    starting state and its solution).
     With first_solve_only (one step per case) the step stops after its first
     outer iteration: the pair is the same, the rest of the step is not
     needed for it."""

@@ -12,8 +12,9 @@ with its solver and initial guess:
     fp64_fast       the same iteration on Jacobi-scaled FP64 with FMA
     mixed_zero      FP32 sweeps in FP64 defect correction, zero guess
     mixed_previous  ... each step's first solve from the previous solution
-    mixed_learned   ... each step's first solve from the learned guess, with
-                    the first-sweep fallback to zero
+    mixed_learned   ... the run's first solve from the learned guess (with the
+                    first-sweep fallback to zero), later ones from the
+                    previous solution
 
 One JSON line per variant: mean and total device time per step (CUDA events
 inside the library), outer iterations, solves, sweeps and fallbacks per step,
@@ -57,8 +58,7 @@ def interior(a: np.ndarray) -> np.ndarray:
 def train_guess(sh, pairs: int, epochs: int, lr: float, dt_range, steps_per_case: int = 1,
                 seed: int = 10) -> tuple[bytes, dict]:
     """Train the learned guess on `pairs` first solves of steps: runs of
-    `steps_per_case` steps from seeded random irradiations and dt (so that
-    the pairs include later steps, with their previous solution); returns
+    `steps_per_case` steps from seeded random irradiations and dt; returns
     the weights blob and a summary."""
     f = start_run(sh)
     t0 = time.perf_counter()
@@ -131,8 +131,8 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--lr", type=float, default=5e-4)
     ap.add_argument("--dt-range", default="50,500")
-    ap.add_argument("--steps-per-case", type=int, default=4,
-                    help="consecutive steps per training case (pairs from later steps carry a previous solution)")
+    ap.add_argument("--steps-per-case", type=int, default=1,
+                    help="consecutive steps per training case (1: each pair is a run's first solve)")
     ap.add_argument("--delt", type=float, default=0.0, help="override the shell's dt")
     args = ap.parse_args(argv)
     sh = shell(args.config, seed=args.seed)
