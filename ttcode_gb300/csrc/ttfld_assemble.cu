@@ -62,12 +62,14 @@ static int qdens(ttfld_ctx* c) {
   return 0;
 }
 
-// FLIM pprphy.f:362-565 (IFLIMTYP 1 and 2, irad=3).
-static int flim(ttfld_ctx* c, int energy_iter) {
+// FLIM pprphy.f:362-565 (IFLIMTYP 1 and 2, irad=3).  skip_kappa /
+// skip_qdens: KAPPA / QDENS already ran on the same T and rho in this step,
+// so their outputs would be recomputed bit for bit (:396-402).
+static int flim(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
   if (energy_iter <= 1) {  // :396-402
-    int rc = kappa(c);
-    if (rc) return rc;
-    if ((rc = qdens(c))) return rc;
+    int rc;
+    if (!skip_kappa && (rc = kappa(c))) return rc;
+    if (!skip_qdens && (rc = qdens(c))) return rc;
   }
   Dev d = c->d;
   const double sg = d.sigval;
@@ -156,8 +158,8 @@ static int flim(ttfld_ctx* c, int energy_iter) {
 }
 
 // DIFF pprad.f:74-156
-static int diff(ttfld_ctx* c, int energy_iter) {
-  int rc = flim(c, energy_iter);
+static int diff(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
+  int rc = flim(c, energy_iter, skip_kappa, skip_qdens);
   if (rc) return rc;
   Dev d = c->d;
   const double sg = d.sigval;
@@ -204,8 +206,8 @@ static int diff(ttfld_ctx* c, int energy_iter) {
 }
 
 // CALCULATEFLUX ppenergy.f:880-920 followed by FLUX_BC ppenergy.f:922-982.
-static int calculateflux(ttfld_ctx* c, int energy_iter) {
-  int rc = diff(c, energy_iter);
+static int calculateflux(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
+  int rc = diff(c, energy_iter, skip_kappa, skip_qdens);
   if (rc) return rc;
   Dev d = c->d;
   launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
@@ -251,7 +253,7 @@ static int fill_evalues(ttfld_ctx* c, double theta) {
 }
 
 // CALCULATEDIVF_WITHF ppenergy.f:825-878, NCOSYS=2 (:853-867).
-static int divf_withf(ttfld_ctx* c, double* out, double theta) {
+static int divf_withf(ttfld_ctx* c, double* out, double theta, bool fill = true) {
   Dev d = c->d;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     double xb = G(xxb, i), szb = G(surzb, k);
@@ -264,7 +266,7 @@ static int divf_withf(ttfld_ctx* c, double* out, double theta) {
     out[cidx(d, i, j, k)] = v;
   });
   TT_CHECK_LAUNCH();
-  return fill_evalues(c, theta);
+  return fill ? fill_evalues(c, theta) : 0;
 }
 
 // CALCSTELLARTAU pprad.f:191-221, STELLAR_DTAU :223-242 and the grey
@@ -388,9 +390,11 @@ static int bounds(ttfld_ctx* c) {
 
 // ---- exported to the step driver ---------------------------------------
 int asm_kappa(ttfld_ctx* c) { return kappa(c); }
-int asm_calculateflux(ttfld_ctx* c, int energy_iter) { return calculateflux(c, energy_iter); }
+int asm_calculateflux(ttfld_ctx* c, int energy_iter, bool skip_kappa, bool skip_qdens) {
+  return calculateflux(c, energy_iter, skip_kappa, skip_qdens);
+}
 int asm_fill_evalues(ttfld_ctx* c, double theta) { return fill_evalues(c, theta); }
-int asm_divf(ttfld_ctx* c, double* out, double theta) { return divf_withf(c, out, theta); }
+int asm_divf(ttfld_ctx* c, double* out, double theta, bool fill) { return divf_withf(c, out, theta, fill); }
 int asm_stellar(ttfld_ctx* c) { return stellarinput_heating(c); }
 int asm_bounds(ttfld_ctx* c) { return bounds(c); }
 int asm_diff(ttfld_ctx* c, int energy_iter) { return diff(c, energy_iter); }

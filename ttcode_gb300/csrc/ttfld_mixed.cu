@@ -690,6 +690,20 @@ static int persistent_grid(K kernel, int threads, size_t smem, long long items) 
 
 enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2 };
 
+// Blocks of the two persistent kernels for nvec items (0: not available),
+// sized once per grid size.
+static void sweep_grids(long long nvec, int* pers, int* tma) {
+  static int tma_blocks = -1, pers_blocks = -1;
+  static long long sized_for = -1;
+  if (sized_for != nvec) {
+    tma_blocks = persistent_grid(sweeps32_tma, kTmaThreads, kTmaSmem, nvec);
+    pers_blocks = persistent_grid(sweeps32_persistent, kPersistThreads, 0, nvec);
+    sized_for = nvec;
+  }
+  if (pers) *pers = pers_blocks;
+  if (tma) *tma = tma_blocks;
+}
+
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
 // evaluates the in-sweep norm against stop_ratio (and, with stall_check,
 // stops at the FP32 rounding floor).  The product form is one persistent
@@ -708,13 +722,8 @@ int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_r
   double* partials = c->partials;
   int stall = stall_check ? 1 : 0;
   void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall};
-  static int tma_blocks = -1, pers_blocks = -1;
-  static long long sized_for = -1;
-  if (sized_for != nvec) {
-    tma_blocks = persistent_grid(sweeps32_tma, kTmaThreads, kTmaSmem, nvec);
-    pers_blocks = persistent_grid(sweeps32_persistent, kPersistThreads, 0, nvec);
-    sized_for = nvec;
-  }
+  int pers_blocks = 0, tma_blocks = 0;
+  sweep_grids(nvec, &pers_blocks, &tma_blocks);
   if (form == kFormTma && tma_blocks > 0) {
     TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma, dim3(tma_blocks), dim3(kTmaThreads), args,
                                          kTmaSmem, c->stream));
@@ -819,7 +828,17 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     int it_prev = it0;
     int chunk = 32;
     bool have_norm = false;  // r_prev is an in-sweep norm (the anchor is a true residual)
-    for (;;) {
+    int pers = 0;
+    sweep_grids(g.rows * (g.nxp >> 2), &pers, nullptr);
+    if (pers > 0) {
+      // the persistent kernel stops itself (target reached, FP32 floor, or
+      // the budget), so one launch per anchor and one poll suffice
+      const long long left = budget - c->host_sol->iter;
+      const int n = (int)(left < (1LL << 24) ? (left > 0 ? left : 1) : (1LL << 24));
+      if ((rc = launch_sweeps32(c, n, period, stop)) || (rc = poll(c))) return rc;
+      if (c->host_sol->nonfinite) status = TTFLD_E_NONFINITE;
+    }
+    for (; pers == 0;) {
       if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop))) return rc;
       if ((rc = poll(c))) return rc;
       const SolverDev* h = c->host_sol;

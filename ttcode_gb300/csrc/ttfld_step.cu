@@ -9,9 +9,9 @@
 
 namespace ttfld {
 int asm_kappa(ttfld_ctx* c);
-int asm_calculateflux(ttfld_ctx* c, int energy_iter);
+int asm_calculateflux(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false);
 int asm_fill_evalues(ttfld_ctx* c, double theta);
-int asm_divf(ttfld_ctx* c, double* out, double theta);
+int asm_divf(ttfld_ctx* c, double* out, double theta, bool fill = true);
 int asm_stellar(ttfld_ctx* c);
 int asm_bounds(ttfld_ctx* c);
 int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st);
@@ -195,16 +195,23 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
     d.Q[h] = d.RH[h] * d.CV[h] * d.T[h];                                 // :65
   });
   TT_CHECK_LAUNCH();
+  // Recomputations that reproduce their inputs bit for bit are left out:
+  // KAPPA and QDENS inside FLIM (energy_iter <= 1, pprphy.f:396-402) see the
+  // T and rho of the first call of this step, and the FILL_EVALUES that
+  // CALCULATEDIVF_WITHF ends with (ppenergy.f:876) is overwritten by the one
+  // at :348 before anything reads the EVAL arrays.
+  bool kappa_done = false;
   if (d.f_incident > 1) {                                               // :68-71
     if ((rc = asm_kappa(c)) || (rc = asm_stellar(c))) return rc;
+    kappa_done = true;
   }
-  if ((rc = asm_calculateflux(c, 0))) return rc;                        // :74-75
+  if ((rc = asm_calculateflux(c, 0, kappa_done, false))) return rc;     // :74-75
   if ((rc = upper_bc(c)) || (rc = left_bc(c)) || (rc = z_bc(c))) return rc;
   if ((rc = halo_shift(c, d.ER))) return rc;                            // :230-245
   TT_CHECK(cudaMemcpyAsync(d.Q_OLD, d.Q, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
   TT_CHECK(cudaMemcpyAsync(d.ER_OLD, d.ER, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
-  if ((rc = asm_calculateflux(c, 0))) return rc;                        // :253-255
-  if ((rc = asm_divf(c, d.DIVF_OLD, theta))) return rc;
+  if ((rc = asm_calculateflux(c, 0, true, true))) return rc;            // :253-255
+  if ((rc = asm_divf(c, d.DIVF_OLD, theta, false))) return rc;
   int energy_iter = 0;
   int status = TTFLD_OK;
   double solve_ms = 0.0;
@@ -216,7 +223,7 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
     // shift just done repeats the one of :230-245, and FLIM at energy_iter
     // 0 and 1 takes the same branch (:396-402) -- so they are not formed again.
     if (energy_iter > 1 && (rc = asm_calculateflux(c, energy_iter))) return rc;
-    if ((rc = asm_divf(c, d.DIVF, theta))) return rc;
+    if ((rc = asm_divf(c, d.DIVF, theta, false))) return rc;
     if ((rc = jacobian(c, theta))) return rc;                           // :287-345
     if ((rc = asm_fill_evalues(c, theta))) return rc;                   // :348
     if (c->params.adjust_sor && energy_iter == 1 && (c->params.iii % 10000 == 0 || c->params.iii == 1)) {
