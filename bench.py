@@ -37,7 +37,7 @@ SHELL = "shell256"
 WORKLOAD = ("shell256: 100x256x128 (r x phi x theta) synthetic spherical shell, 3276800 cells, "
             "dt=100 s, seed 1; the SOLVE_WITH_SOR system of its implicit step's first outer "
             "iteration, solved to ||b-Ax||_1/||b||_1 <= 1e-10")
-TRAIN_PAIRS, TRAIN_EPOCHS, TRAIN_LR = 16, 12, 5e-4
+TRAIN_PAIRS, TRAIN_EPOCHS, TRAIN_LR = 16, 20, 5e-4
 # Algorithmic bytes per cell update of one sweep (both colours):
 #   FP32 scaled sweep: 6 coefficients + rhat + e read + e write  = 9 x 4 B
 #   FP64 exact sweep : 7 coefficients + b + x read + x write      = 10 x 8 B
@@ -190,10 +190,33 @@ def run_profile_solve(args):
     torch.cuda.cudart().cudaProfilerStart()
     for solver, g in (("mixed", "learned"), ("sor64_exact", "zero")):
         f.set_solver(solver, guess=g, tol=1e-10, inner_min=16, inner_max=512)
+        f.begin_step(new_run=True)
         st = f.solve_system()
         print(json.dumps({"solver": solver, "guess": g, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStop()
+    f.close()
+
+
+def run_profile_step(args):
+    """For the step's launch list: the shell256 shell, two implicit steps
+    (mixed solver, previous-step guess), then a third inside
+    cudaProfilerStart/Stop."""
+    import torch
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import shell
+    torch.cuda.set_device(0)
+    sh = shell(SHELL, seed=1)
+    f = start_run(sh)
+    f.set_solver("mixed", guess="previous", tol=1e-10)
+    for _ in range(2):
+        f.coupled_energy_eqs(True)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    st = f.coupled_energy_eqs(True)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({"step_ms": st.step_ms, "solve_ms": st.solve_ms, "sweeps": st.sor_total}), flush=True)
     f.close()
 
 
@@ -463,12 +486,17 @@ def main():
                     help="only build the system and run one mixed and one exact FP64 solve")
     ap.add_argument("--profile-sweeps", action="store_true",
                     help="only build the system and run 8 + 16 FP32 sweeps")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="only run three implicit steps, the third inside cudaProfilerStart/Stop")
     args = ap.parse_args()
     if args.profile_solve:
         run_profile_solve(args)
         return
     if args.profile_sweeps:
         run_profile_sweeps(args)
+        return
+    if args.profile_step:
+        run_profile_step(args)
         return
     if args.warmup < 3:
         args.warmup = 3

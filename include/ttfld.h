@@ -309,6 +309,11 @@ int ttfld_guess_gradients(ttfld_ctx* ctx, const float* feat, const float* target
 /* Network output (normalised target units) for one input. */
 int ttfld_guess_predict(ttfld_ctx* ctx, const float* feat, float* pred);
 size_t ttfld_guess_num_params(void);
+/* Kernel form of the network's large-level convolutions, for the process:
+ * 0 (default) mma.sync on shared-memory tiles, 1 tcgen05 (5th-generation
+ * tensor cores, accumulators in tensor memory).  Same results up to FP32
+ * summation order. */
+int ttfld_guess_set_conv(int use_tcgen05);
 /* Weights blob: "TTFLDNN2", uint64 parameter count, FP32 parameters. */
 int ttfld_guess_load(ttfld_ctx* ctx, const void* blob, size_t bytes);
 int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);

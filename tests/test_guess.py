@@ -174,3 +174,28 @@ def test_trained_guess_saves_sweeps():
         assert l[2] == 0                      # the guess was kept
         assert l[0] < 0.9 * z[0], (l, z)      # at least 10% fewer sweeps
         assert np.linalg.norm(el - ez) <= 1e-9 * np.linalg.norm(ez)
+
+
+def test_tcgen05_and_mma_sync_convolutions_agree():
+    """The two kernel forms of the large-level convolutions (tcgen05 with
+    tensor-memory accumulators, and mma.sync on shared-memory tiles) give the
+    same prediction on a grid of several tiles in every direction."""
+    from ttcode_gb300 import guess
+    from ttcode_gb300.fld import FLD
+    from ttcode_gb300.grid import gitter
+    from ttcode_gb300.synthetic import default_params
+    X, Y, Z = 40, 64, 32
+    f = FLD(gitter(X, Y, Z, 7.0e9, 7.7e9), default_params())
+    guess.init(f, seed=5)
+    rng = np.random.default_rng(1)
+    feat = rng.uniform(-1, 1, (X * Y * Z, 5)).astype(np.float32)
+    preds = []
+    try:
+        for form in (1, 0):
+            assert f.L.ttfld_guess_set_conv(form) == 0
+            p = np.zeros(X * Y * Z, dtype=np.float32)
+            assert f.L.ttfld_guess_predict(f.h, feat.ctypes.data, p.ctypes.data) == 0
+            preds.append(p)
+    finally:
+        f.L.ttfld_guess_set_conv(0)
+    assert np.linalg.norm(preds[0] - preds[1]) <= 1e-3 * np.linalg.norm(preds[1])

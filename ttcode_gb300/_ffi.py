@@ -96,7 +96,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_kernel_launches", "ttfld_sor_solve_noalloc", "ttfld_guess_init",
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
-           "ttfld_guess_num_params", "ttfld_begin_step")
+           "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv")
 
 _lib = None
 
@@ -161,6 +161,7 @@ def lib():
     L.ttfld_guess_gradients.argtypes = [vp, vp, vp, vp, P_double, vp]
     L.ttfld_guess_predict.argtypes = [vp, vp, vp]
     L.ttfld_begin_step.argtypes = [vp, ctypes.c_int]
+    L.ttfld_guess_set_conv.argtypes = [ctypes.c_int]
     L.ttfld_guess_num_params.restype = ctypes.c_size_t
     L.ttfld_guess_num_params.argtypes = []
     L.ttfld_guess_load.argtypes = [vp, vp, ctypes.c_size_t]
