@@ -45,6 +45,16 @@ BYTES_FP32_SWEEP = 36
 BYTES_FP64_SWEEP = 80
 
 
+def max_over_ranks(value: float, device: str) -> float:
+    """The largest value over the ranks of the process group (the timed
+    region's length is the slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -292,9 +302,7 @@ def run_gpu(args):
     x_mixed = f.download("DELTA_ER")
     total_ms = float(sum(times))
     if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, "cuda")
     ms_per_solve = total_ms / args.steps / ws
     r_l1, b_l1 = f.true_residual()
     err = float(np.linalg.norm((x_mixed - x_ref).ravel()) / np.linalg.norm(x_ref.ravel()))

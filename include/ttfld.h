@@ -136,8 +136,9 @@ typedef struct {
   int32_t solver;      /* enum ttfld_solver                                */
   int32_t guess;       /* enum ttfld_guess                                 */
   double tol;          /* mixed solver: stop at ||b-Ax||_1/||b||_1 <= tol  */
-  int32_t inner_min;   /* mixed solver: FP32 sweeps per correction, bounds */
-  int32_t inner_max;
+  int32_t inner_min;   /* accepted and ignored: the mixed solver runs each  */
+  int32_t inner_max;   /* FP64 correction until its FP32 sweeps stop (target
+                          reached or rounding floor)                       */
   int32_t max_sweeps;  /* mixed solver sweep budget (0 = ITMAX)            */
   int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:
                             0 = the residual its first red-black sweep

@@ -226,3 +226,20 @@ def test_mixed_solver_multi_chunk_grid():
     # same iteration, a different stopping test (true FP64 residual at the
     # anchors against the in-sweep norm): about the same count
     assert abs(st.sor_iter - st64.sor_iter) <= max(16, st64.sor_iter // 20), (st.sor_iter, st64.sor_iter)
+
+
+def test_golden_fixture_on_the_gpu():
+    """The GPU step (exact FP64 solver) on the shell of the committed oracle
+    fixture (tests/golden/make_golden.py): the same sweep and outer-iteration
+    counts, E_R and T within the parity tolerance."""
+    import os
+    from ttcode_gb300.synthetic import make_shell
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shell_step.npz"))
+    sh = make_shell(int(z["nx"]), int(z["ny"]), int(z["nz"]), seed=int(z["seed"]), delt=float(z["delt"]))
+    f = fld_from_shell(sh, eps=float(z["eps"]))
+    f.set_solver("sor64_exact")
+    st = f.coupled_energy_eqs(True)
+    assert st.sor_total == int(z["sor_total"]) and st.energy_iter == int(z["energy_iter"])
+    nx, ny, nz = sh.dims
+    for n in ("ER", "T"):
+        assert rel_l2(f.download(n)[2:nx + 2, 2:ny + 2, 2:nz + 2], z[n]) <= TOL, n
