@@ -267,6 +267,25 @@ int ttfld_diffusion(ttfld_ctx* ctx, ttfld_solve_stats* stats);
  * from the learned guess or zero.  No reference counterpart. */
 int ttfld_begin_step(ttfld_ctx* ctx, int new_run);
 
+/* FP64 energy sums over the active cells (below UPPERBND, not an identity
+ * row of FILL_SOR_MATRIX: i < min(UPPERBND, NX), 1 < k < NZ), each cell
+ * weighted by V = surxb(i) dxa(i) dya(j) surzb(k) dza(k), the weight under
+ * which the discrete divergence of CALCULATEDIVF_WITHF telescopes (V is
+ * proportional to the cell volume).  Summed in a fixed order, so the
+ * results are reproducible.  No reference counterpart. */
+typedef struct {
+  double volume;       /* sum of V                                         */
+  double e_rad;        /* sum of V E_R                                     */
+  double e_gas;        /* sum of V Q                                       */
+  double heating;      /* sum of V STELLARINPUT (per unit time)            */
+  double flux_bottom;  /* FLUX_X through the faces i = 1, into the region  */
+  double flux_top;     /* FLUX_X through the upper faces of the last active
+                          cells, out of the region                        */
+  double flux_theta;   /* FLUX_Z through the faces k = 2 and k = NZ, out  */
+} ttfld_energy;
+/* The sums of the current state (E_R, Q, STELLARINPUT, FLUX_X/Z). */
+int ttfld_energy_sums(ttfld_ctx* ctx, ttfld_energy* out);
+
 /* ---- measurement (no reference counterpart) --------------------------- */
 /* Runs n back-to-back sweeps of a solver's sweep kernels on the current
  * system (TTFLD_SOLVER_SOR64_EXACT: DELTA_ER is iterated in place;

@@ -243,3 +243,44 @@ def test_golden_fixture_on_the_gpu():
     nx, ny, nz = sh.dims
     for n in ("ER", "T"):
         assert rel_l2(f.download(n)[2:nx + 2, 2:ny + 2, 2:nz + 2], z[n]) <= TOL, n
+
+
+def test_energy_sums_match_numpy(small):
+    """ttfld_energy_sums after one step against the same sums formed with
+    numpy from the downloaded fields (FP64, different summation order)."""
+    f = fld_from_shell(small)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)
+    got = f.energy_sums()
+    g = small.grid
+    nx, ny, nz = small.dims
+
+    def m(name, n):
+        return np.array([g.at(name, i) for i in range(-1, n + 3)])   # index i + 1
+
+    I, J, K = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), np.arange(1, nz + 1), indexing="ij")
+    ub = f.download("UPPERBND")[J + 1, K + 1]
+    itop = np.minimum(ub, nx) - 1
+    act = (I <= itop) & (K >= 2) & (K <= nz - 1)
+    surxb, dxa, surxa, xxb = m("surxb", nx), m("dxa", nx), m("surxa", nx), m("xxb", nx)
+    dya, surzb, dza, surza = m("dya", ny), m("surzb", nz), m("dza", nz), m("surza", nz)
+    vol = surxb[I + 1] * dxa[I + 1] * dya[J + 1] * surzb[K + 1] * dza[K + 1]
+    er, q = f.download("ER")[I + 1, J + 1, K + 1], f.download("Q")[I + 1, J + 1, K + 1]
+    si = f.download("STELLARINPUT")[I - 1, J + 1, K + 1]
+    fx, fz = f.download("FLUX_X"), f.download("FLUX_Z")
+    ax = dya[J + 1] * surzb[K + 1] * dza[K + 1]
+    az = surxb[I + 1] * dxa[I + 1] * dya[J + 1] / xxb[I + 1]
+    bottom = act & (I == 1)
+    top = act & (I == itop)
+    ref = {
+        "volume": vol[act].sum(), "e_rad": (vol * er)[act].sum(), "e_gas": (vol * q)[act].sum(),
+        "heating": (vol * si)[act].sum(),
+        "flux_bottom": (surxa[2] * ax * fx[0, J - 1, K - 1])[bottom].sum(),
+        "flux_top": (surxa[I + 2] * ax * fx[np.minimum(I, nx), J - 1, K - 1])[top].sum(),
+        "flux_theta": (surza[nz + 1] * az * fz[I - 1, J - 1, nz - 1])[act & (K == nz - 1)].sum()
+        - (surza[3] * az * fz[I - 1, J - 1, 1])[act & (K == 2)].sum(),
+    }
+    fscale = max(abs(ref["flux_bottom"]), abs(ref["flux_top"]), abs(ref["flux_theta"]))
+    for k, v in ref.items():
+        scale = fscale if k.startswith("flux") else abs(v)
+        assert abs(got[k] - v) <= 1e-11 * scale, (k, got[k], v)

@@ -56,6 +56,11 @@ class SolveStats(ctypes.Structure):
                 ("guess_ms", c_double)]
 
 
+class Energy(ctypes.Structure):
+    _fields_ = [(n, c_double) for n in ("volume", "e_rad", "e_gas", "heating", "flux_bottom", "flux_top",
+                                        "flux_theta")]
+
+
 class StepStats(ctypes.Structure):
     _fields_ = [("energy_iter", c_int32), ("sor_total", c_int32), ("solves", c_int32),
                 ("fallbacks", c_int32), ("status", c_int32), ("reserved", c_int32),
@@ -96,7 +101,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_kernel_launches", "ttfld_sor_solve_noalloc", "ttfld_guess_init",
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
-           "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv")
+           "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums")
 
 _lib = None
 
@@ -162,6 +167,7 @@ def lib():
     L.ttfld_guess_predict.argtypes = [vp, vp, vp]
     L.ttfld_begin_step.argtypes = [vp, ctypes.c_int]
     L.ttfld_guess_set_conv.argtypes = [ctypes.c_int]
+    L.ttfld_energy_sums.argtypes = [vp, ctypes.POINTER(Energy)]
     L.ttfld_guess_num_params.restype = ctypes.c_size_t
     L.ttfld_guess_num_params.argtypes = []
     L.ttfld_guess_load.argtypes = [vp, vp, ctypes.c_size_t]

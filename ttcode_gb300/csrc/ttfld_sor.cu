@@ -148,6 +148,53 @@ __global__ void __launch_bounds__(kThreads) resid_l1_kernel(Dev d, const double*
   }
 }
 
+// The seven sums of ttfld_energy_sums: per-block partials in a fixed order,
+// then the last block adds them (fixed order) into part[7 * nbmax + q].
+__global__ void __launch_bounds__(kThreads) energy_sums_kernel(Dev d, double* part, int nbmax) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long n = (long long)nx * ny * nz;
+  double s[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % nx) + 1;
+    const long long r = t / nx;
+    const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    const int ub = PA(UB, j, k);
+    const int itop = (ub < nx ? ub : nx) - 1;  // last active cell of the column
+    if (i > itop || k < 2 || k > nz - 1) continue;
+    const size_t h = hidx(d, i, j, k);
+    const double vol = G(surxb, i) * G(dxa, i) * G(dya, j) * G(surzb, k) * G(dza, k);
+    s[0] += vol;
+    s[1] += vol * d.ER[h];
+    s[2] += vol * d.Q[h];
+    s[3] += vol * d.SI[h];
+    const double ax = G(dya, j) * G(surzb, k) * G(dza, k);
+    if (i == 1) s[4] += G(surxa, 1) * ax * FA(FLUXX, 1, j, k);
+    if (i == itop) s[5] += G(surxa, i + 1) * ax * FA(FLUXX, i + 1, j, k);
+    const double az = G(surxb, i) * G(dxa, i) * G(dya, j) / G(xxb, i);
+    if (k == 2) s[6] -= G(surza, 2) * az * FA(FLUXZ, i, j, 2);
+    if (k == nz - 1) s[6] += G(surza, nz) * az * FA(FLUXZ, i, j, nz);
+  }
+  for (int q = 0; q < 7; ++q) {
+    const double b = block_sum(s[q], sh);
+    if (threadIdx.x == 0) part[q * nbmax + blockIdx.x] = b;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(&d.sol->ticket2, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int q = 0; q < 7; ++q) {
+      const double tot = block_sum_array(part + q * nbmax, gridDim.x, sh);
+      if (threadIdx.x == 0) part[7 * nbmax + q] = tot;
+    }
+    if (threadIdx.x == 0) d.sol->ticket2 = 0;
+  }
+}
+
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host) {
   int nb = grid_for((long long)ncell(c->d));
   if (nb > kMaxPartials) nb = kMaxPartials;
@@ -382,6 +429,22 @@ int ttfld_true_residual(ttfld_ctx* c, double* l1, double* rhs_l1) {
   double v = 0.0;
   if ((rc = true_residual(c, c->d.DELTA_ER, c->d.RHS, &v))) return rc;
   if (l1) *l1 = v;
+  return 0;
+}
+
+int ttfld_energy_sums(ttfld_ctx* c, ttfld_energy* out) {
+  if (!c || !out) return TTFLD_E_ARGS;
+  constexpr int kNb = 1024;  // blocks; partials [7][kNb] then 7 totals
+  int nb = grid_for((long long)ncell(c->d));
+  if (nb > kNb) nb = kNb;
+  energy_sums_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, c->partials, kNb);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  double t[7];
+  TT_CHECK(cudaMemcpyAsync(t, c->partials + 7 * kNb, sizeof(t), cudaMemcpyDeviceToHost, c->stream));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  out->volume = t[0]; out->e_rad = t[1]; out->e_gas = t[2]; out->heating = t[3];
+  out->flux_bottom = t[4]; out->flux_top = t[5]; out->flux_theta = t[6];
   return 0;
 }
 

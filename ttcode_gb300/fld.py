@@ -182,6 +182,12 @@ class FLD:
         check("DIFFUSION", self.L.ttfld_diffusion(self.h, ctypes.byref(st)), ok=(0, 1))
         return st
 
+    def energy_sums(self) -> dict:
+        """FP64 energy sums of the current state (ttfld_energy_sums)."""
+        e = _ffi.Energy()
+        check("energy_sums", self.L.ttfld_energy_sums(self.h, ctypes.byref(e)))
+        return {n: getattr(e, n) for n, _ in _ffi.Energy._fields_}
+
     def stream_ptr(self) -> int:
         """The cudaStream_t the library issues this context's work on."""
         return int(self.L.ttfld_stream(self.h))

@@ -89,6 +89,7 @@ def run_variant(sh, name: str, nsteps: int, snap_at: int, epsmat: float = 1e-10,
         G.load_weights(f, blob)
     f.set_solver(v["solver"], guess=v["guess"], tol=epsmat)
     steps, snap = [], None
+    e0 = f.energy_sums()
     for s in range(nsteps):
         st = _ffi.StepStats()
         rc = f.L.ttfld_coupled_energy_eqs(f.h, 1, ctypes.byref(st))
@@ -99,7 +100,9 @@ def run_variant(sh, name: str, nsteps: int, snap_at: int, epsmat: float = 1e-10,
             break
         if s + 1 == snap_at:
             snap = (interior(f.download("ER")), interior(f.download("T")))
+    e1 = f.energy_sums()
     f.close()
+    steps[-1]["energy"] = {"start": e0, "end": e1}
     return steps, snap
 
 
@@ -113,6 +116,11 @@ def summarize(name: str, steps, snap, ref_snap, snap_at: int) -> dict:
            "sweeps_per_step": tot("sweeps") / n, "sweeps_per_solve": tot("sweeps") / max(tot("solves"), 1),
            "fallbacks": int(tot("fallbacks")), "fallback_rate": tot("fallbacks") / max(tot("solves"), 1),
            "worst_status": min(s["status"] for s in steps)}
+    if "energy" in steps[-1]:
+        e0, e1 = steps[-1]["energy"]["start"], steps[-1]["energy"]["end"]
+        out["energy"] = {"e_rad_start": e0["e_rad"], "e_rad_end": e1["e_rad"], "e_gas_start": e0["e_gas"],
+                         "e_gas_end": e1["e_gas"], "heating_end": e1["heating"],
+                         "flux_bottom_end": e1["flux_bottom"], "flux_top_end": e1["flux_top"]}
     if snap is not None and ref_snap is not None:
         out["err_vs_fp64_1e-12"] = {"after_steps": snap_at, "ER": rel_l2(snap[0], ref_snap[0]),
                                      "T": rel_l2(snap[1], ref_snap[1])}
