@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) conv3_fwd_kernel(ConvArgs a) {
   }
 }
 
-// Shared-memory tiled form for the large levels (few channels, many
+// Shared-memory tiled form for the large levels (few output channels, many
 // voxels): a CTA computes 16 (x) x 8 (y) x 2 (z) output voxels and all
 // output channels.  The input tile with its one-voxel halo (18 x 10 x 4
 // voxels) and, when they fit, the weights are staged in shared memory with
@@ -307,10 +307,10 @@ static int launch_conv_smem(cudaStream_t s, const ConvArgs& a) {
   const size_t smem = conv_smem_bytes(a.cin, a.cout, with_w);
   static size_t opted = 0;
   if (smem > 48 * 1024 && smem > opted) {
-    if (cudaFuncSetAttribute(conv3_smem_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024) !=
+    if (cudaFuncSetAttribute(conv3_smem_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
         cudaSuccess)
       return TTFLD_E_CUDA;
-    opted = 128 * 1024;
+    opted = 200 * 1024;
   }
   const long long blocks = (long long)((a.X + kTX - 1) / kTX) * ((a.Y + kTY - 1) / kTY) * ((a.Z + kTZ - 1) / kTZ);
   conv3_smem_kernel<NB><<<(unsigned)blocks, 256, smem, s>>>(a, with_w ? 1 : 0);
@@ -524,6 +524,10 @@ static int conv_fwd(cudaStream_t s, const ConvArgs& a) {
   if (a.cin <= 48 && a.in_cs % 8 == 0 && a.in_co % 8 == 0 && a.out_cs % 2 == 0) {
     if (g_conv_tc && a.cout == 16) return launch_conv_tc<16>(s, a);
     if (g_conv_tc && a.cout == 32) return launch_conv_tc<32>(s, a);
+  }
+  // shared-memory tiles up to 96 input channels (a 150 KB input tile; the
+  // weights stay in global memory above 100 KB of tile + weights)
+  if (a.cin <= 96 && a.in_cs % 8 == 0 && a.in_co % 8 == 0) {
     if (a.cout == 16) return launch_conv_smem<2>(s, a);
     if (a.cout == 32) return launch_conv_smem<4>(s, a);
   }
