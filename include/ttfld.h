@@ -153,6 +153,12 @@ typedef struct {
                                 not yet removed.
                             The mixed solver runs tests 0 and 3 with its own
                             FP32 sweeps and keeps the winner's sweeps.   */
+  int32_t sweep_form;  /* mixed solver's FP32 sweep kernel: 0 = one
+                          persistent cooperative launch per FP64 anchor
+                          (default; two launches per sweep where
+                          cooperative launch is unavailable), 1 = the same
+                          with TMA-staged coefficients (slower here),
+                          2 = two launches per sweep                      */
 } ttfld_solve_opts;
 
 typedef struct {

@@ -200,10 +200,12 @@ def test_diffusion_parity(small):
     assert np.array_equal(f.download("SCALAR"), o.f("SCALAR"))
 
 
-def test_mixed_solver_multi_chunk_grid():
-    """The product FP32/FP64 solve on a 100x128x64 system (the TMA-staged sweep
-    kernel gives each block two chunks, the second partial) against the exact
-    FP64 SOR (the reference loop, bitwise) converged to 1e-12."""
+@pytest.mark.parametrize("form", ["persistent", "tma", "split"])
+def test_mixed_solver_multi_chunk_grid(form):
+    """The FP32/FP64 solve on a 100x128x64 system with each form of its sweep
+    kernel (persistent; TMA-staged, which gives each block two chunks, the
+    second partial; two launches per sweep) against the exact FP64 SOR (the
+    reference loop, bitwise) converged to 1e-12."""
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
     sh = make_shell(100, 128, 64, seed=5, delt=100.0)
@@ -215,7 +217,7 @@ def test_mixed_solver_multi_chunk_grid():
     st_ref = f.solve_system()
     ref = f.download("DELTA_ER")
     f.set_params(epsmat=1e-10)
-    f.set_solver("mixed", tol=1e-10)
+    f.set_solver("mixed", tol=1e-10, sweep_form=form)
     st = f.solve_system()
     x = f.download("DELTA_ER")
     r, b = f.true_residual()

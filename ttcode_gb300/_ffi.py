@@ -43,10 +43,11 @@ class Params(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("solver", c_int32), ("guess", c_int32), ("tol", c_double),
                 ("inner_min", c_int32), ("inner_max", c_int32), ("max_sweeps", c_int32),
-                ("fallback_rule", c_int32)]
+                ("fallback_rule", c_int32), ("sweep_form", c_int32)]
 
 
 FALLBACK = {"first_sweep": 0, "never": 1, "residual": 2, "four_sweeps": 3}
+SWEEP_FORM = {"persistent": 0, "tma": 1, "split": 2}
 
 
 class SolveStats(ctypes.Structure):

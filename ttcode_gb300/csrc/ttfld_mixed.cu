@@ -788,16 +788,22 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   bool hit_tol = false;
   bool resume = false;  // the first anchor and its first sweeps are done already
   if (fallback) *fallback = 0;
+  const SweepForm form =
+      c->opts.sweep_form == 1 ? kFormTma : (c->opts.sweep_form == 2 ? kFormSplit : kFormPersistent);
+  int pers_blocks = 0, tma_blocks = 0;
+  sweep_grids(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
+  // one launch per anchor needs a persistent kernel (it stops itself)
+  const bool one_launch = (form == kFormPersistent && pers_blocks > 0) || (form == kFormTma && tma_blocks > 0);
   if (guess_test) {
     if ((rc = rhat_of_b(c, b))) return rc;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
-    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0)) || (rc = poll(c))) return rc;
+    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0, form)) || (rc = poll(c))) return rc;
     const double r_zero = c->host_sol->rnorm;
     TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
     if ((rc = resid32(c, x, b, &l1))) return rc;
     if (st) st->guess_resid_l1 = l1;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
-    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0)) || (rc = poll(c))) return rc;
+    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0, form)) || (rc = poll(c))) return rc;
     const double r_guess = c->host_sol->rnorm;
     if (r_guess < r_zero) {
       resume = true;
@@ -828,18 +834,16 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     int it_prev = it0;
     int chunk = 32;
     bool have_norm = false;  // r_prev is an in-sweep norm (the anchor is a true residual)
-    int pers = 0;
-    sweep_grids(g.rows * (g.nxp >> 2), &pers, nullptr);
-    if (pers > 0) {
+    if (one_launch) {
       // the persistent kernel stops itself (target reached, FP32 floor, or
       // the budget), so one launch per anchor and one poll suffice
       const long long left = budget - c->host_sol->iter;
       const int n = (int)(left < (1LL << 24) ? (left > 0 ? left : 1) : (1LL << 24));
-      if ((rc = launch_sweeps32(c, n, period, stop)) || (rc = poll(c))) return rc;
+      if ((rc = launch_sweeps32(c, n, period, stop, form)) || (rc = poll(c))) return rc;
       if (c->host_sol->nonfinite) status = TTFLD_E_NONFINITE;
     }
-    for (; pers == 0;) {
-      if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop))) return rc;
+    for (; !one_launch;) {
+      if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop, kFormSplit))) return rc;
       if ((rc = poll(c))) return rc;
       const SolverDev* h = c->host_sol;
       if (h->nonfinite) { status = TTFLD_E_NONFINITE; break; }
