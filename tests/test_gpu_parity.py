@@ -286,3 +286,17 @@ def test_energy_sums_match_numpy(small):
     for k, v in ref.items():
         scale = fscale if k.startswith("flux") else abs(v)
         assert abs(got[k] - v) <= 1e-11 * scale, (k, got[k], v)
+
+
+def test_adjust_sor_param_same_omega(small):
+    """ADJUST_SOR_PARAM (ppsor.f:332-354, 50 solves over omega = 1.01 + 0.02 n)
+    on the oracle's post-step coefficients picks the same omega as the oracle
+    (ITMAX 200 bounds the slow end of the scan in both)."""
+    o = _system_after_one_step(small)
+    o.set("itmax", 200)
+    f = fld_from_shell(small, itmax=200)
+    for n in ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8", "EVAL_1_6", "RHS_ER"):
+        f.upload(n, o.f(n))
+    w_dev = f.adjust_sor_param()
+    assert o.call("adjust_sor_param") == 0
+    assert w_dev == o.get("sorparam")
