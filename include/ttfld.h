@@ -119,9 +119,15 @@ enum ttfld_solver {
   TTFLD_SOLVER_SOR64_FAST = 1,  /* red-black SOR in FP64 on Jacobi-scaled
                                    coefficients with FMA (same iteration,
                                    different rounding)                     */
-  TTFLD_SOLVER_MIXED = 2        /* FP32 red-black sweeps inside FP64 defect
+  TTFLD_SOLVER_MIXED = 2,       /* FP32 red-black sweeps inside FP64 defect
                                    correction, stopped on the true FP64
                                    residual ||b-Ax||_1/||b||_1            */
+  TTFLD_SOLVER_PCG = 3          /* FP32 conjugate gradients (radial line
+                                   preconditioner) on the symmetrised system
+                                   inside FP64 defect correction, same stop
+                                   rule as MIXED; a guess is kept if its
+                                   preconditioned residual r.z is below the
+                                   zero guess's (fallback rules 0 and 3)  */
 };
 
 enum ttfld_guess {
@@ -247,6 +253,17 @@ int ttfld_solve_with_sor(ttfld_ctx* ctx, int print_max_values,
                          ttfld_solve_stats* stats);
 /* As above on SOR_A..G / RHS_ER already on the device (no refill). */
 int ttfld_solve_system(ttfld_ctx* ctx, ttfld_solve_stats* stats);
+/* SOLVE_WITH_HYPRE, pphypre.f:1-111 (the IRAD=2 path): the system of
+ * FILLHYPREMATRIX / FILLHYPREVECTORS (pphypre.f:115-334; SOLVE_WITH_SOR's
+ * rows from the device EVAL arrays with the i=1 rows made identity rows and
+ * b zero on the boundary rows; RHS_ER itself is not changed, SOR_A..G are
+ * refilled) solved for DELTA_ER by PCG from x = 1 (pphypre.f:136) until
+ * ||Sigma W (b-Ax)||_2 / ||Sigma W b||_2 <= tol on the symmetrised system,
+ * or maxit iterations (then status 1).  tol <= 0 and maxit <= 0 select the
+ * reference's 1e-6 and 50 (pphypre.f:45-55).  hypre's SMG preconditioner is
+ * replaced by an exact radial line solve.  stats may be NULL. */
+int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
+                           ttfld_solve_stats* stats);
 /* Exactly n red-black sweeps on the current system from the current
  * DELTA_ER, FP64, reference rounding (for sweep-by-sweep parity tests). */
 int ttfld_sor_sweeps(ttfld_ctx* ctx, int n, double* rnorm, double* rhsnorm);

@@ -23,7 +23,8 @@ HALO = ("T", "RH", "CV", "ER", "ER_OLD", "Q", "Q_OLD", "DELTA_ER", "XKAPR", "XKA
 CELL = ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8",
         "EVAL_1_6", "JACOB_ETA", "FQ", "FR", "RHS_ER", "SOR_A", "SOR_B", "SOR_C",
         "SOR_D", "SOR_E", "SOR_F", "SOR_G", "DIVF", "DIVF_OLD", "DFQ_DQ", "DFR_DQ",
-        "DELTA_Q", "RHS_DIF")
+        "DELTA_Q", "RHS_DIF", "HYP_A", "HYP_B", "HYP_C", "HYP_D", "HYP_E", "HYP_F",
+        "HYP_G", "HYP_RHS")
 FACE = ("FLIMX", "FLIMY", "FLIMZ", "DIFRX", "DIFRY", "DIFRZ", "FLUX_X", "FLUX_Y", "FLUX_Z")
 PLANE = ("MU_STAR", "TINCIDENT")
 
@@ -53,7 +54,7 @@ def _load():
         lib.ttor_get.restype = ctypes.c_double
         lib.ttor_get.argtypes = [vp, ctypes.c_char_p]
         for name in ("gitter", "calcmustar", "bounds", "kappa", "qdens", "flim", "diff",
-                     "calculateflux", "flux_bc", "stellarinput_heating", "fill_sor_matrix",
+                     "calculateflux", "flux_bc", "stellarinput_heating", "fill_sor_matrix", "fill_hypre_system",
                      "b_vector_boundaries", "adjust_sor_param", "diffusion"):
             f = getattr(lib, "ttor_" + name)
             f.restype = ctypes.c_int

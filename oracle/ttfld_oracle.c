@@ -51,6 +51,8 @@ struct ttor_state {
       *EVAL_1_6, *JACOB_ETA, *FQ, *FR, *RHS_ER, *SOR_A, *SOR_B, *SOR_C,
       *SOR_D, *SOR_E, *SOR_F, *SOR_G, *DIVF, *DIVF_OLD, *DFQ_DQ, *DFR_DQ,
       *DELTA_Q, *RHS_DIF;
+  /* the IRAD=2 system of FILLHYPREMATRIX / FILLHYPREVECTORS */
+  double *HYP_A, *HYP_B, *HYP_C, *HYP_D, *HYP_E, *HYP_F, *HYP_G, *HYP_RHS;
   /* face fields */
   double *FLIMX, *FLIMY, *FLIMZ, *DIFRX, *DIFRY, *DIFRZ, *FLUX_X, *FLUX_Y,
       *FLUX_Z;
@@ -104,6 +106,9 @@ static const fdesc FIELDS[] = {
     FD_ENTRY(SOR_F, K_CELL), FD_ENTRY(SOR_G, K_CELL), FD_ENTRY(DIVF, K_CELL),
     FD_ENTRY(DIVF_OLD, K_CELL), FD_ENTRY(DFQ_DQ, K_CELL), FD_ENTRY(DFR_DQ, K_CELL),
     FD_ENTRY(DELTA_Q, K_CELL), FD_ENTRY(RHS_DIF, K_CELL),
+    FD_ENTRY(HYP_A, K_CELL), FD_ENTRY(HYP_B, K_CELL), FD_ENTRY(HYP_C, K_CELL),
+    FD_ENTRY(HYP_D, K_CELL), FD_ENTRY(HYP_E, K_CELL), FD_ENTRY(HYP_F, K_CELL),
+    FD_ENTRY(HYP_G, K_CELL), FD_ENTRY(HYP_RHS, K_CELL),
     FD_ENTRY(FLIMX, K_FACE), FD_ENTRY(FLIMY, K_FACE), FD_ENTRY(FLIMZ, K_FACE),
     FD_ENTRY(DIFRX, K_FACE), FD_ENTRY(DIFRY, K_FACE), FD_ENTRY(DIFRZ, K_FACE),
     FD_ENTRY(FLUX_X, K_FACE), FD_ENTRY(FLUX_Y, K_FACE), FD_ENTRY(FLUX_Z, K_FACE),
@@ -773,6 +778,51 @@ int ttor_fill_sor_matrix(ttor_state* s) {
         if (i == nx - 1) C(SOR_C, i, j, k) = 0.0;
         if (!s->poles && k == 2) C(SOR_F, i, j, k) = 0.0;
         if (!s->poles && k == nz - 1) C(SOR_G, i, j, k) = 0.0;
+      }
+  return 0;
+}
+
+/* FILLHYPREMATRIX pphypre.f:221-334 and the b of FILLHYPREVECTORS
+ * pphypre.f:115-219 (one rank: MPIleft, MPIright, MPIbelow and MPIabove
+ * are MPI_PROC_NULL; MPIlower/MPIupper are the rank itself, so no j row is
+ * a boundary row).  Stencil entries 1..7 are (i,j,k), i-1, i+1, j-1, j+1,
+ * k-1, k+1 (pphypre.f:553-581) -> HYP_A..HYP_G.  The grid is given only its
+ * extents (pphypre.f:404-413, no periodicity), so hypre drops the entries
+ * of rows j = 1 (j-1) and j = NY (j+1) that reach outside it; they are
+ * zeroed here.  The initial x of pphypre.f:136 is 1 everywhere. */
+int ttor_fill_hypre_system(ttor_state* s) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double h[7];
+        const double e8 = C(EVAL8, i, j, k);
+        h[0] = C(EVAL7, i, j, k) + e8 * C(EVAL_1_6, i, j, k);
+        h[1] = -e8 * C(EVAL2, i, j, k);
+        h[2] = -e8 * C(EVAL1, i, j, k);
+        h[3] = -e8 * C(EVAL4, i, j, k);
+        h[4] = -e8 * C(EVAL3, i, j, k);
+        h[5] = -e8 * C(EVAL6, i, j, k);
+        h[6] = -e8 * C(EVAL5, i, j, k);
+        const int ub = P(UPPERBND, j, k);
+        if (i >= ub) { h[0] = 1.0; for (int m = 1; m < 7; ++m) h[m] = 0.0; }
+        if (i == ub - 1) h[2] = 0.0;
+        if (i == 1 || i == nx || (!s->poles && (k == 1 || k == nz))) {
+          h[0] = 1.0;
+          for (int m = 1; m < 7; ++m) h[m] = 0.0;
+        }
+        if (i == 2) h[1] = 0.0;
+        if (i == nx - 1) h[2] = 0.0;
+        if (!s->poles && k == 2) h[5] = 0.0;
+        if (!s->poles && k == nz - 1) h[6] = 0.0;
+        if (j == 1) h[3] = 0.0;   /* outside the hypre grid */
+        if (j == ny) h[4] = 0.0;
+        C(HYP_A, i, j, k) = h[0]; C(HYP_B, i, j, k) = h[1]; C(HYP_C, i, j, k) = h[2];
+        C(HYP_D, i, j, k) = h[3]; C(HYP_E, i, j, k) = h[4]; C(HYP_F, i, j, k) = h[5];
+        C(HYP_G, i, j, k) = h[6];
+        double b = C(RHS_ER, i, j, k);
+        if (i >= ub || i == 1 || i == nx || (!s->poles && (k == 1 || k == nz))) b = 0.0;
+        C(HYP_RHS, i, j, k) = b;
       }
   return 0;
 }

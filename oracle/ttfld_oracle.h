@@ -65,6 +65,9 @@ int ttor_calculatedivf_withf(ttor_state* s, int which /*0 DIVF, 1 DIVF_OLD*/, do
 int ttor_stellarinput_heating(ttor_state* s);
 int ttor_fill_sor_matrix(ttor_state* s);
 int ttor_b_vector_boundaries(ttor_state* s);
+/* FILLHYPREMATRIX + FILLHYPREVECTORS (pphypre.f:115-334) into HYP_A..HYP_G,
+ * HYP_RHS from the EVAL arrays, RHS_ER and UPPERBND. */
+int ttor_fill_hypre_system(ttor_state* s);
 /* SOLVE_WITH_SOR.  use_guess=0 starts from zero (ppsor.f:29); use_guess=1
  * keeps the interior of DELTA_ER as the initial iterate (ghosts zeroed). */
 int ttor_solve_with_sor(ttor_state* s, int fill, int use_guess);

@@ -269,3 +269,75 @@ def test_golden_step_fixture():
     for n in ("ER", "T"):
         got = o.f(n)[2:nx + 2, 2:ny + 2, 2:nz + 2]
         assert rel_l2(got, z[n]) <= 1e-12, n
+
+
+def hypre_matrix(o):
+    """The oracle's FILLHYPREMATRIX system (HYP_A..HYP_G) as a scipy matrix;
+    no entry may reach outside the grid (hypre's grid has no periodicity)."""
+    nx, ny, nz = o.nx, o.ny, o.nz
+    n = nx * ny * nz
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    rows, cols, vals = [], [], []
+    for name, (di, dj, dk) in zip(("HYP_A", "HYP_B", "HYP_C", "HYP_D", "HYP_E", "HYP_F", "HYP_G"),
+                                  ((0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1))):
+        v = o.f(name)
+        ii, jj, kk = I + di, J + dj, K + dk
+        inside = (ii >= 0) & (ii < nx) & (jj >= 0) & (jj < ny) & (kk >= 0) & (kk < nz)
+        assert np.all(v[~inside] == 0.0), name
+        m = inside & (v != 0.0)
+        rows.append((I + nx * (J + ny * K))[m]); cols.append((ii + nx * (jj + ny * kk))[m]); vals.append(v[m])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+
+
+def test_hypre_system_is_sor_system_with_dirichlet_bottom(shell):
+    """FILLHYPREMATRIX / FILLHYPREVECTORS (pphypre.f:115-334) against
+    FILL_SOR_MATRIX / B_VECTOR_BOUNDARIES (ppsor.f:189-329) on the same EVAL
+    arrays: equal except the i = 1 rows (identity, b = 0), the i-1 coupling
+    of the i = 2 rows and the phi couplings that leave hypre's grid (j-1 of
+    j = 1, j+1 of j = NY); the system is non-singular."""
+    o = oracle_from_shell(shell)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    assert o.call("fill_sor_matrix") == 0 and o.call("b_vector_boundaries") == 0
+    assert o.call("fill_hypre_system") == 0
+    nx, ny, nz = o.nx, o.ny, o.nz
+    for s, h in zip("ABCDEFG", ("HYP_A", "HYP_B", "HYP_C", "HYP_D", "HYP_E", "HYP_F", "HYP_G")):
+        a, b = o.f("SOR_" + s).copy(), o.f(h)
+        a[0] = 1.0 if s == "A" else 0.0
+        if s == "B":
+            a[1] = 0.0
+        if s == "D":
+            a[:, 0] = 0.0
+        if s == "E":
+            a[:, ny - 1] = 0.0
+        assert np.array_equal(a, b), s
+    rhs = o.f("RHS_ER").copy()
+    rhs[0] = 0.0
+    assert np.array_equal(rhs, o.f("HYP_RHS"))
+    A = hypre_matrix(o)
+    x = spla.spsolve(A.tocsc(), o.f("HYP_RHS").ravel(order="F"))
+    assert np.all(np.isfinite(x)) and np.all(x.reshape((nx, ny, nz), order="F")[0] == 0.0)
+
+
+def test_weighted_rows_are_symmetric(shell):
+    """The symmetrising weight of the PCG solvers: W = V / |EVAL8| with
+    V = surxb dxa dya surzb dza makes W_n A_nm = W_m A_mn for every radial
+    and theta pair and every phi pair away from the periodic seam (whose two
+    face coefficients come from different halo cells)."""
+    o = oracle_from_shell(shell)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    o.call("fill_evalues", 1.0)
+    assert o.call("fill_sor_matrix") == 0
+    g = shell.grid
+    nx, ny, nz = shell.dims
+    I, J, K = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), np.arange(1, nz + 1), indexing="ij")
+    V = g.at("surxb", I) * g.at("dxa", I) * g.at("dya", J) * g.at("surzb", K) * g.at("dza", K)
+    W = V / np.abs(o.f("EVAL8"))
+    S = {c: o.f("SOR_" + c) for c in "ABCDEFG"}
+    for fwd, bwd, ax in (("C", "B", 0), ("E", "D", 1), ("G", "F", 2)):
+        lhs = (W * S[fwd])
+        rhs = np.roll(W * S[bwd], -1, axis=ax)
+        sl = [slice(None)] * 3
+        sl[ax] = slice(0, -1)           # the pair (n, n+1) inside the grid
+        l, r = lhs[tuple(sl)], rhs[tuple(sl)]
+        scale = np.max(np.abs(l))
+        assert np.max(np.abs(l - r)) <= 1e-12 * scale, fwd

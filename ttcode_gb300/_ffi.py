@@ -83,7 +83,7 @@ FIELDS = {
     "STELLARINPUT": 112, "STELLARTAU": 113, "DTAUS": 114,
 }
 
-SOLVER = {"sor64_exact": 0, "sor64_fast": 1, "mixed": 2}
+SOLVER = {"sor64_exact": 0, "sor64_fast": 1, "mixed": 2, "pcg": 3}
 TIMED_SWEEPS = dict(SOLVER, mixed_split=3, mixed_tma=4)   # ttfld_time_sweeps also times the per-colour launches
 GUESS = {"zero": 0, "previous": 1, "learned": 2}
 
@@ -102,7 +102,8 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_kernel_launches", "ttfld_sor_solve_noalloc", "ttfld_guess_init",
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
-           "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums")
+           "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums",
+           "ttfld_solve_with_hypre")
 
 _lib = None
 
@@ -149,6 +150,7 @@ def lib():
     L.ttfld_fill_evalues.argtypes = [vp, ctypes.c_double]
     L.ttfld_solve_with_sor.argtypes = [vp, ctypes.c_int, ctypes.POINTER(SolveStats)]
     L.ttfld_solve_system.argtypes = [vp, ctypes.POINTER(SolveStats)]
+    L.ttfld_solve_with_hypre.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolveStats)]
     L.ttfld_sor_sweeps.argtypes = [vp, ctypes.c_int, P_double, P_double]
     L.ttfld_true_residual.argtypes = [vp, P_double, P_double]
     L.ttfld_adjust_sor_param.argtypes = [vp, P_double]

@@ -278,6 +278,7 @@ int ttfld_destroy(ttfld_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   unet_free(c);
   mix_free(c);
+  krylov_free(c);
   if (c->prev_x) cudaFree(c->prev_x);
   if (c->guess_tmp) cudaFree(c->guess_tmp);
   if (c->slab) cudaFree(c->slab);
@@ -307,7 +308,7 @@ int ttfld_get_params(const ttfld_ctx* c, ttfld_params* p) {
 
 int ttfld_set_solver(ttfld_ctx* c, const ttfld_solve_opts* o) {
   if (!c || !o) return TTFLD_E_ARGS;
-  if (o->solver < 0 || o->solver > 2 || o->guess < 0 || o->guess > 2) return TTFLD_E_ARGS;
+  if (o->solver < 0 || o->solver > 3 || o->guess < 0 || o->guess > 2) return TTFLD_E_ARGS;
   if (o->solver == TTFLD_SOLVER_MIXED && !(o->tol > 0.0)) return TTFLD_E_ARGS;
   if (o->fallback_rule < 0 || o->fallback_rule > 3) return TTFLD_E_ARGS;
   if (o->sweep_form < 0 || o->sweep_form > 2) return TTFLD_E_ARGS;

@@ -37,6 +37,7 @@ struct SolverDev {
   unsigned int ticket2;
   int bar_timeout;     // 1 if a grid barrier wait ran out (the kernel gave up)
   int stalled;         // 1 if the FP32 inner loop stopped at its rounding floor
+  int bad_weights;     // PCG: a row without a valid symmetrising weight
 };
 
 // Reduction targets of the outer Newton loop.
@@ -167,6 +168,47 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* a, double 
   atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }
 
+// Grid-wide barrier of the persistent kernel (a cooperative launch, so all
+// blocks are resident).  Thread 0 of each block arrives on a counter; the
+// last arrival resets it and advances the generation the others wait on.
+// The wait is bounded: after kBarrierSpins polls (seconds of polling at an
+// L2 round trip each) or once another block has given up, the block records the
+// timeout and returns false, and the kernel returns without further work.
+constexpr long long kBarrierSpins = 1LL << 23;
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) {
+  __shared__ int ok_sh;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int g0 = ld_acquire(&sol->bar_gen);
+    __threadfence();
+    if (atomicAdd(&sol->bar_count, 1u) == nblocks - 1) {
+      atomicExch(&sol->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&sol->bar_gen, 1u);
+    } else {
+      long long polls = 0;
+      while (ld_acquire(&sol->bar_gen) == g0) {
+        if (++polls > kBarrierSpins || *(volatile int*)&sol->bar_timeout) {
+          atomicExch(&sol->bar_timeout, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok_sh = ok;
+  }
+  __syncthreads();
+  return ok_sh != 0;
+}
+
 __device__ __forceinline__ bool solver_done(const Dev& d) {
   return *(volatile int*)&d.sol->done != 0;
 }
@@ -221,6 +263,7 @@ struct ttfld_ctx {
   int solve_idx;            // solves so far in the current step
   double* prev_x;           // previous solution (halo)
   double* guess_tmp;        // scratch halo array of the first-sweep guess test
+  void* krylov;             // PCG workspace (allocated on first use)
   double last_solve_ms;
 };
 
@@ -238,7 +281,10 @@ int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax
 int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st);
 int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test = 0,
                 int* fallback = nullptr);
-int fill_sor_matrix(ttfld_ctx* c);
+int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test = 0,
+              int* fallback = nullptr);
+void krylov_free(ttfld_ctx* c);
+int fill_sor_matrix(ttfld_ctx* c, bool zero_rhs = true);
 int halo_shift(ttfld_ctx* c, double* a);
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);
 int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1);

@@ -1,0 +1,629 @@
+// ttfld_krylov.cu -- preconditioned conjugate gradients on the FLD system.
+//
+//  * ttfld_solve_with_hypre: the IRAD=2 path's SOLVE_WITH_HYPRE
+//    (pphypre.f:1-111).  Its system is FILLHYPREMATRIX / FILLHYPREVECTORS
+//    (pphypre.f:115-334): SOLVE_WITH_SOR's 7-point matrix (ppsor.f:202-272)
+//    with the i = 1 rows made identity rows (pphypre.f:281-294), the west
+//    coupling of the i = 2 rows removed (pphypre.f:298-300) and b zero on the
+//    same boundary rows (pphypre.f:137-205).  hypre solves it by PCG from
+//    x = 1 (pphypre.f:136) to a relative residual of 1e-6 in at most 50
+//    iterations (pphypre.f:45-55), preconditioned by one SMG cycle.  Here
+//    the same PCG runs on the device with a radial line preconditioner.
+//  * TTFLD_SOLVER_PCG: SOLVE_WITH_SOR's own system solved by the same PCG,
+//    stopped like the mixed solver on ||b - A x||_1 / ||b||_1 <= tol.
+//
+// Symmetric form.  Row n of the matrix is (EVAL7 + EVAL8 EVAL_1_6) x_n -
+// EVAL8 sum_m EVALm x_m, and each EVALm is a face coefficient shared by the
+// two cells of the face divided by the metric factor of cell n
+// (ppenergy.f:995-1013).  Multiplied by W_n = V_n / |EVAL8_n| with
+// V = surxb dxa dya surzb dza, the rows form a symmetric matrix (the
+// identity rows are decoupled and get W = V).  PCG runs on
+// S = Sigma sym(W A) Sigma, Sigma = diag(1 / sqrt(W_n A_nn)), which has a
+// unit diagonal; sym() is the symmetric part, which differs from W A only
+// where the two cells of a face were given different face coefficients (the
+// phi seam of the periodic halo).  An FP64 defect correction on the rows as
+// they are (r = b - A x, x += Sigma e) removes that difference and the FP32
+// rounding of the inner iteration:
+//
+//   loop: r = b - A x (FP64); stop test; solve S e = Sigma W r by FP32 PCG
+//         to a relative reduction of its preconditioned residual norm; x += Sigma e.
+//
+// Preconditioner.  The radial couplings dominate by two to three orders of
+// magnitude (the shell is thin in r), so the preconditioner is the exact
+// solve of the tridiagonal radial line of every (j,k) column, factored once
+// per solve (Thomas algorithm, FP64 pivots stored in FP32).
+//
+// Layout.  The FP32 inner arrays are line-major, q = (i-1)*NY*NZ +
+// (k-1)*NY + (j-1): in a line solve one thread walks one column and the
+// threads of a warp touch 32 consecutive columns of the same radius
+// (coalesced); in the operator pass the phi and theta neighbours are at q
+// +- 1 and q +- NY.  The inner iteration is one persistent cooperative
+// kernel with two grid barriers per iteration (after s = S p for alpha,
+// after the line solve for beta).
+#include <math.h>
+#include <stdlib.h>
+
+#include "ttfld_internal.cuh"
+
+namespace ttfld {
+namespace {
+
+constexpr int kPcgThreads = 768;   // one block per SM
+constexpr int kPcgStall = 25;      // iterations without a new minimum of r.z end an inner run
+constexpr double kInnerReduce = 1e-5;  // relative reduction of sqrt(r.z) asked of one inner run
+
+struct Kry {
+  int nx, ny, nz;
+  long long n, ncol;
+  // couplings of S to the +i, +j (periodic) and +k neighbour, and the
+  // reciprocal pivots of the radial line factorisation (line-major, FP32)
+  float *cr, *cp, *ct, *g;
+  float *e, *r, *z, *s, *p[2];
+  double *sig, *wgt;  // Sigma_n and W_n (cell order, FP64)
+};
+
+struct KryWork {
+  Kry k;
+  void* mem;
+};
+
+__host__ __device__ __forceinline__ size_t lq(const Kry& k, int i, int j, int kk) {
+  return (size_t)(i - 1) * k.ncol + (size_t)(kk - 1) * k.ny + (size_t)(j - 1);
+}
+
+// The rows of the system being solved: SOR_A..G, with the hypre changes.
+struct Row {
+  double a, b, c, d, e, f, g;
+};
+// hypre's grid has only its extents (pphypre.f:404-413, no periodicity), so
+// the j-1 entry of rows j = 1 and the j+1 entry of rows j = NY reach outside
+// it and are dropped.
+__device__ __forceinline__ Row row_of(const Dev& d, size_t t, int i, int j, bool hypre) {
+  Row r{d.SA[t], d.SB[t], d.SC[t], d.SD[t], d.SE[t], d.SF[t], d.SG[t]};
+  if (hypre) {
+    if (i == 1) r = Row{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // pphypre.f:281-294
+    else if (i == 2) r.b = 0.0;                               // pphypre.f:298-300
+    if (j == 1) r.d = 0.0;
+    if (j == d.ny) r.e = 0.0;
+  }
+  return r;
+}
+
+// b of the hypre system (pphypre.f:137-205): zero at i >= upperbnd, i = 1,
+// i = NX, k = 1 and k = NZ (poles are not implemented).
+__device__ __forceinline__ double b_of(const Dev& d, const double* b, size_t t, int i, int j, int k, bool hypre) {
+  if (hypre && (i >= PA(UB, j, k) || i == 1 || i == d.nx || k == 1 || k == d.nz)) return 0.0;
+  return b[t];
+}
+
+__device__ __forceinline__ void cell_of(const Dev& d, long long t, int& i, int& j, int& k) {
+  i = (int)(t % d.nx) + 1;
+  const long long r = t / d.nx;
+  j = (int)(r % d.ny) + 1;
+  k = (int)(r / d.ny) + 1;
+}
+
+// W_n and Sigma_n (cell order).  A coupled row needs EVAL8 < 0.
+__global__ void __launch_bounds__(kThreads) kry_weights_kernel(Dev d, Kry kr, int hypre) {
+  const long long n = (long long)ncell(d);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(d, t, i, j, k);
+    const Row r = row_of(d, t, i, j, hypre != 0);
+    const bool decoupled = r.b == 0.0 && r.c == 0.0 && r.d == 0.0 && r.e == 0.0 && r.f == 0.0 && r.g == 0.0;
+    const double v = G(surxb, i) * G(dxa, i) * G(dya, j) * G(surzb, k) * G(dza, k);
+    const double e8 = d.E8[t];
+    const double w = decoupled ? v : v / (-e8);
+    const double dd = w * r.a;
+    bool ok = (decoupled || e8 < 0.0) && dd > 0.0 && isfinite(dd);
+    kr.wgt[t] = ok ? w : 0.0;
+    kr.sig[t] = ok ? 1.0 / sqrt(dd) : 0.0;
+    if (!ok) atomicExch(&d.sol->bad_weights, 1);
+  }
+}
+
+// Couplings of S (the symmetric part of Sigma W A Sigma) to the +i, +j, +k
+// neighbours, written line-major.
+__global__ void __launch_bounds__(kThreads) kry_couplings_kernel(Dev d, Kry kr, int hypre) {
+  const long long n = (long long)ncell(d);
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(d, t, i, j, k);
+    const bool h = hypre != 0;
+    const Row r = row_of(d, t, i, j, h);
+    const double wn = kr.wgt[t], sn = kr.sig[t];
+    float cr = 0.f, cp = 0.f, ct = 0.f;
+    if (i < nx) {
+      const size_t m = t + 1;
+      const Row rm = row_of(d, m, i + 1, j, h);
+      cr = (float)(0.5 * (wn * r.c + kr.wgt[m] * rm.b) * sn * kr.sig[m]);
+    }
+    {
+      const int jp = j == ny ? 1 : j + 1;
+      const size_t m = cidx(d, i, jp, k);
+      const Row rm = row_of(d, m, i, jp, h);
+      cp = (float)(0.5 * (wn * r.e + kr.wgt[m] * rm.d) * sn * kr.sig[m]);
+    }
+    if (k < nz) {
+      const size_t m = cidx(d, i, j, k + 1);
+      const Row rm = row_of(d, m, i, j, h);
+      ct = (float)(0.5 * (wn * r.g + kr.wgt[m] * rm.f) * sn * kr.sig[m]);
+    }
+    const size_t q = lq(kr, i, j, k);
+    kr.cr[q] = cr;
+    kr.cp[q] = cp;
+    kr.ct[q] = ct;
+  }
+}
+
+// Reciprocal pivots of every radial line (diagonal 1, off-diagonal cr):
+// u_1 = 1, u_i = 1 - cr_{i-1}^2 / u_{i-1}; g = 1/u.  One thread per column.
+__global__ void __launch_bounds__(kThreads) kry_factor_kernel(Kry kr, SolverDev* sol) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < kr.ncol;
+       c += (long long)gridDim.x * blockDim.x) {
+    double g = 1.0, cprev = 0.0;
+    size_t q = (size_t)c;
+    for (int i = 0; i < kr.nx; ++i, q += kr.ncol) {
+      const double u = 1.0 - cprev * cprev * g;
+      if (!(u > 0.0)) atomicExch(&sol->bad_weights, 1);
+      g = 1.0 / u;
+      kr.g[q] = (float)g;
+      cprev = (double)kr.cr[q];
+    }
+  }
+}
+
+// FP64 anchor: r = b - A x, its L1 norm, the scaled right-hand side
+// Sigma W r of the inner system (FP32, line-major) and its squared 2-norm;
+// with it ||b||_1 and ||Sigma W b||_2^2.  The last block writes the four
+// totals to sol->true_l1, sol->scratch[0], sol->rhsnorm, sol->scratch[1].
+__global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, const double* __restrict__ x,
+                                                              const double* __restrict__ b, int hypre,
+                                                              double* partials, int nbmax) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int nx = d.nx, ny = d.ny;
+  const long long n = (long long)ncell(d);
+  const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(d, t, i, j, k);
+    const Row r = row_of(d, t, i, j, hypre != 0);
+    const size_t q = hidx(d, i, j, k);
+    const size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
+    const size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
+    const double bb = b_of(d, b, t, i, j, k, hypre != 0);
+    const double ax = r.a * x[q] + r.b * x[q - 1] + r.c * x[q + 1] + r.d * x[qjm] + r.e * x[qjp] + r.f * x[q - sk] +
+                      r.g * x[q + sk];
+    const double rr = bb - ax;
+    const double sw = kr.sig[t] * kr.wgt[t];
+    const double rs = sw * rr, bs = sw * bb;
+    s[0] += fabs(rr);
+    s[1] += rs * rs;
+    s[2] += fabs(bb);
+    s[3] += bs * bs;
+    const size_t l = lq(kr, i, j, k);
+    kr.r[l] = (float)rs;
+    kr.e[l] = 0.f;
+  }
+  for (int m = 0; m < 4; ++m) {
+    const double v = block_sum(s[m], sh);
+    if (threadIdx.x == 0) partials[m * nbmax + blockIdx.x] = v;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(&d.sol->ticket2, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double tot[4];
+    for (int m = 0; m < 4; ++m) tot[m] = block_sum_array(partials + m * nbmax, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      d.sol->true_l1 = tot[0];
+      d.sol->scratch[0] = tot[1];
+      d.sol->rhsnorm = tot[2];
+      d.sol->scratch[1] = tot[3];
+      d.sol->ticket2 = 0;
+    }
+  }
+}
+
+// x += Sigma e (x a halo array, e line-major).
+__global__ void __launch_bounds__(kThreads) kry_update_kernel(Dev d, Kry kr, double* x) {
+  const long long n = (long long)ncell(d);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_of(d, t, i, j, k);
+    x[hidx(d, i, j, k)] += kr.sig[t] * (double)kr.e[lq(kr, i, j, k)];
+  }
+}
+
+// One radial line of the inner iteration for column c.  With update, first
+// e += alpha p and r -= alpha s along the line.  Then z = T^-1 r by the
+// factored tridiagonal T (forward: y_i = r_i - cr_{i-1} g_{i-1} y_{i-1},
+// kept in z; backward: z_i = (y_i - cr_i z_{i+1}) g_i).  Returns this
+// line's share of r.z.
+__device__ __forceinline__ double line_pass(const Kry& k, long long c, bool update, float alpha, const float* pn) {
+  const size_t ncol = (size_t)k.ncol;
+  const int nx = k.nx;
+  float yprev = 0.f, lprev = 0.f;
+  size_t q = (size_t)c;
+  for (int i = 0; i < nx; ++i, q += ncol) {
+    float ri = k.r[q];
+    if (update) {
+      k.e[q] = fmaf(alpha, pn[q], k.e[q]);
+      ri = fmaf(-alpha, k.s[q], ri);
+      k.r[q] = ri;
+    }
+    const float y = fmaf(-lprev, yprev, ri);
+    k.z[q] = y;
+    lprev = k.cr[q] * k.g[q];
+    yprev = y;
+  }
+  double dot = 0.0;
+  float znext = 0.f;
+  q = (size_t)c + (size_t)(nx - 1) * ncol;
+  for (int i = nx - 1; i >= 0; --i, q -= ncol) {
+    const float zi = fmaf(-k.cr[q], znext, k.z[q]) * k.g[q];
+    k.z[q] = zi;
+    znext = zi;
+    dot += (double)k.r[q] * (double)zi;
+  }
+  return dot;
+}
+
+// The FP32 PCG iteration on S e = r from e = 0 (r, e set by the anchor).
+// Line phases: the warps of all blocks are dealt round-robin over groups of
+// 32 consecutive columns.  Operator phase: p_new = z + beta p (p read from
+// p[cur], written to p[1-cur], so that neighbours read the old values),
+// s = S p_new.  Every block forms alpha and beta from all block partials in
+// the same fixed order, so all blocks take the same decisions.  The run ends
+// when sqrt(r.z / r0.z0) <= stop_ratio, after kPcgStall iterations without
+// a new minimum of r.z (the FP32 floor), on a non-positive p.s, or after
+// maxit iterations; maxit = 0 only computes r0.z0 (sol->scratch[2]).
+__global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, SolverDev* sol, double* partials,
+                                                                   int maxit, double stop_ratio) {
+  __shared__ double sh[32];
+  __shared__ double bc[3];
+  const unsigned int nb = gridDim.x;
+  const long long n = k.n, ncol = k.ncol;
+  const int ny = k.ny;
+  const long long nzl = k.nz;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long col0 = ((long long)warp * nb + blockIdx.x) * 32 + lane;
+  const long long colstride = (long long)(blockDim.x >> 5) * nb * 32;
+  double* pa = partials;                 // operator-phase partials
+  double* pb = partials + kMaxPartials;  // line-phase partials
+
+  // z0 = T^-1 r0, gamma0 = r0.z0
+  double acc = 0.0;
+  for (long long c = col0; c < ncol; c += colstride) acc += line_pass(k, c, false, 0.f, nullptr);
+  {
+    const double v = block_sum(acc, sh);
+    if (threadIdx.x == 0) pb[blockIdx.x] = v;
+  }
+  if (!grid_sync(sol, nb)) return;
+  {
+    const double tot = block_sum_array(pb, nb, sh);
+    if (threadIdx.x == 0) bc[0] = tot;
+    __syncthreads();
+  }
+  double gamma = bc[0];
+  const double gamma0 = gamma;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sol->scratch[2] = gamma0;
+  if (maxit <= 0 || !(gamma0 > 0.0) || !isfinite(gamma0)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !isfinite(gamma0)) sol->nonfinite = 1;
+    return;
+  }
+  const double stop2 = stop_ratio * stop_ratio * gamma0;
+  double gmin = gamma0;
+  int since_min = 0;
+  float beta = 0.f;
+  int cur = 0;
+  for (int it = 1; it <= maxit; ++it) {
+    const float* po = cur ? k.p[1] : k.p[0];
+    float* pn = cur ? k.p[0] : k.p[1];
+    // operator phase: p_new = z + beta p_old, s = S p_new, p_new . s
+    acc = 0.0;
+    for (long long q = tid; q < n; q += nth) {
+      const long long il = q / ncol;
+      const long long cc = q - il * ncol;
+      const int j0 = (int)(cc % ny);
+      const long long k0 = cc / ny;
+      const float pc = fmaf(beta, po[q], k.z[q]);
+      float sv = pc;
+      if (il + 1 < k.nx) sv = fmaf(k.cr[q], fmaf(beta, po[q + ncol], k.z[q + ncol]), sv);
+      if (il > 0) sv = fmaf(k.cr[q - ncol], fmaf(beta, po[q - ncol], k.z[q - ncol]), sv);
+      const long long qjp = j0 == ny - 1 ? q - (ny - 1) : q + 1;
+      const long long qjm = j0 == 0 ? q + (ny - 1) : q - 1;
+      sv = fmaf(k.cp[q], fmaf(beta, po[qjp], k.z[qjp]), sv);
+      sv = fmaf(k.cp[qjm], fmaf(beta, po[qjm], k.z[qjm]), sv);
+      if (k0 + 1 < nzl) sv = fmaf(k.ct[q], fmaf(beta, po[q + ny], k.z[q + ny]), sv);
+      if (k0 > 0) sv = fmaf(k.ct[q - ny], fmaf(beta, po[q - ny], k.z[q - ny]), sv);
+      pn[q] = pc;
+      k.s[q] = sv;
+      acc += (double)pc * (double)sv;
+    }
+    {
+      const double v = block_sum(acc, sh);
+      if (threadIdx.x == 0) pa[blockIdx.x] = v;
+    }
+    if (!grid_sync(sol, nb)) return;
+    {
+      const double tot = block_sum_array(pa, nb, sh);
+      if (threadIdx.x == 0) bc[1] = tot;
+      __syncthreads();
+    }
+    const double ps = bc[1];
+    if (!(ps > 0.0) || !isfinite(ps)) {  // breakdown: S p_new not positive (rounding)
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sol->stalled = 1;
+        if (!isfinite(ps)) sol->nonfinite = 1;
+      }
+      return;
+    }
+    const float alpha = (float)(gamma / ps);
+    // line phase: e += alpha p_new, r -= alpha s, z = T^-1 r, r.z
+    acc = 0.0;
+    for (long long c = col0; c < ncol; c += colstride) acc += line_pass(k, c, true, alpha, pn);
+    {
+      const double v = block_sum(acc, sh);
+      if (threadIdx.x == 0) pb[blockIdx.x] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+    if (!grid_sync(sol, nb)) return;
+    {
+      const double tot = block_sum_array(pb, nb, sh);
+      if (threadIdx.x == 0) bc[2] = tot;
+      __syncthreads();
+    }
+    const double gnew = bc[2];
+    cur = 1 - cur;
+    if (!isfinite(gnew)) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) sol->nonfinite = 1;
+      return;
+    }
+    if (gnew < gmin) {
+      gmin = gnew;
+      since_min = 0;
+    } else if (++since_min >= kPcgStall) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) sol->stalled = 1;
+      return;
+    }
+    if (!(gnew > stop2)) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) sol->done = 1;
+      return;
+    }
+    beta = (float)(gnew / gamma);
+    gamma = gnew;
+  }
+}
+
+int grid_cells(long long n) {
+  int nb = grid_for(n);
+  return nb > 1024 ? 1024 : nb;
+}
+
+KryWork* kry_work(ttfld_ctx* c) {
+  if (c->krylov) return (KryWork*)c->krylov;
+  const Dev& d = c->d;
+  KryWork* w = (KryWork*)calloc(1, sizeof(KryWork));
+  if (!w) return nullptr;
+  Kry& k = w->k;
+  k.nx = d.nx; k.ny = d.ny; k.nz = d.nz;
+  k.n = (long long)ncell(d);
+  k.ncol = (long long)d.ny * d.nz;
+  const size_t n = (size_t)k.n;
+  const size_t bytes = n * (10 * sizeof(float) + 2 * sizeof(double));
+  if (cudaMalloc(&w->mem, bytes) != cudaSuccess) {
+    free(w);
+    return nullptr;
+  }
+  double* dp = (double*)w->mem;
+  k.sig = dp; dp += n;
+  k.wgt = dp; dp += n;
+  float* fp = (float*)dp;
+  float** arrs[] = {&k.cr, &k.cp, &k.ct, &k.g, &k.e, &k.r, &k.z, &k.s, &k.p[0], &k.p[1]};
+  for (float** a : arrs) { *a = fp; fp += n; }
+  c->krylov = w;
+  return w;
+}
+
+int poll_sol(ttfld_ctx* c) {
+  TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  if (c->host_sol->bar_timeout) {
+    fprintf(stderr, "ttfld: a grid barrier of the PCG kernel timed out\n");
+    return TTFLD_E_CUDA;
+  }
+  return 0;
+}
+
+int pcg_blocks(long long ncells) {
+  static int blocks = -1;
+  if (blocks < 0) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg32_persistent, kPcgThreads, 0);
+    long long b = coop ? (long long)sms * per_sm : 0;
+    blocks = (int)(b > kMaxPartials ? kMaxPartials : b);
+  }
+  const long long need = (ncells + kPcgThreads - 1) / kPcgThreads;
+  return (int)(need < blocks ? need : blocks);
+}
+
+// One inner run; returns its iterations in *its.
+int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int* its) {
+  const int nb = pcg_blocks(w->k.n);
+  if (nb <= 0) {
+    fprintf(stderr, "ttfld: the PCG solver needs cooperative launch\n");
+    return TTFLD_E_UNSUPPORTED;
+  }
+  TT_CHECK(cudaMemsetAsync(w->k.p[0], 0, (size_t)w->k.n * sizeof(float), c->stream));
+  TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
+  TT_CHECK(cudaMemsetAsync(&c->sol->done, 0, sizeof(int), c->stream));
+  TT_CHECK(cudaMemsetAsync(&c->sol->stalled, 0, sizeof(int), c->stream));
+  Kry k = w->k;
+  SolverDev* sol = c->sol;
+  double* partials = c->partials;
+  void* args[] = {&k, &sol, &partials, &maxit, &stop_ratio};
+  TT_CHECK(cudaLaunchCooperativeKernel((const void*)pcg32_persistent, dim3(nb), dim3(kPcgThreads), args, 0,
+                                       c->stream));
+  count_launches(1);
+  int rc = poll_sol(c);
+  if (rc) return rc;
+  if (c->host_sol->nonfinite) return TTFLD_E_NONFINITE;
+  *its = c->host_sol->iter;
+  return 0;
+}
+
+int anchor(ttfld_ctx* c, KryWork* w, const double* x, const double* b, bool hypre) {
+  const int nb = grid_cells(w->k.n);
+  kry_anchor_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, hypre ? 1 : 0, c->partials, 1024);
+  count_launches(1);
+  TT_CHECK_LAUNCH();
+  return poll_sol(c);
+}
+
+// Factor the system (weights, couplings, line pivots).
+int prepare(ttfld_ctx* c, KryWork* w, bool hypre) {
+  const int nb = grid_cells(w->k.n);
+  TT_CHECK(cudaMemsetAsync(&c->sol->bad_weights, 0, sizeof(int), c->stream));
+  kry_weights_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->k, hypre ? 1 : 0);
+  kry_couplings_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->k, hypre ? 1 : 0);
+  kry_factor_kernel<<<grid_cells(w->k.ncol), kThreads, 0, c->stream>>>(w->k, c->sol);
+  count_launches(3);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// PCG with FP64 defect correction on x (halo array, holding the initial
+// iterate).  l2 = false: stop on ||b - A x||_1 / ||b||_1 <= tol (the SOR
+// system's rule); l2 = true: on ||Sigma W (b - A x)||_2 / ||Sigma W b||_2 <=
+// tol (the hypre system's PCG rule on the symmetric form).  budget bounds
+// the PCG iterations.  With guess_test, the initial iterate is kept only if
+// its preconditioned residual norm r.z is below that of the zero iterate.
+int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, long long budget, bool l2,
+             int guess_test, int* fallback, ttfld_solve_stats* st) {
+  KryWork* w = kry_work(c);
+  if (!w) return TTFLD_E_CUDA;
+  TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
+  int rc = prepare(c, w, hypre);
+  if (rc) return rc;
+  if (fallback) *fallback = 0;
+  if ((rc = anchor(c, w, x, b, hypre))) return rc;
+  if (c->host_sol->bad_weights) {
+    fprintf(stderr, "ttfld: PCG needs EVAL8 < 0 on every coupled row (the symmetrising weight)\n");
+    return TTFLD_E_UNSUPPORTED;
+  }
+  if (guess_test) {
+    int its = 0;
+    if ((rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
+    const double g_guess = c->host_sol->scratch[2];
+    // the zero iterate: r = b
+    double* zero_x = c->guess_tmp;
+    if (!zero_x) {
+      TT_CHECK(cudaMalloc((void**)&c->guess_tmp, nhalo(c->d) * 8));
+      zero_x = c->guess_tmp;
+    }
+    TT_CHECK(cudaMemsetAsync(zero_x, 0, nhalo(c->d) * 8, c->stream));
+    if ((rc = anchor(c, w, zero_x, b, hypre)) || (rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
+    const double g_zero = c->host_sol->scratch[2];
+    if (!(g_guess < g_zero)) {
+      TT_CHECK(cudaMemsetAsync(x, 0, nhalo(c->d) * 8, c->stream));
+      if (fallback) *fallback = 1;
+      // the anchor of the zero iterate is current
+    } else if ((rc = anchor(c, w, x, b, hypre))) {
+      return rc;
+    }
+  }
+  long long total = 0;
+  int anchors = 0, status = TTFLD_OK, slow = 0;
+  double prev = INFINITY, ratio = INFINITY;
+  for (;;) {
+    const SolverDev& h = *c->host_sol;
+    ratio = l2 ? (h.scratch[1] > 0.0 ? sqrt(h.scratch[0] / h.scratch[1]) : 0.0)
+               : (h.rhsnorm > 0.0 ? h.true_l1 / h.rhsnorm : 0.0);
+    if (!isfinite(ratio)) return TTFLD_E_NONFINITE;
+    if (!(ratio > tol)) break;
+    if (total >= budget) { status = TTFLD_MAXITER; break; }
+    // an anchor that does not halve the residual twice in a row: the
+    // symmetric part is too far from the rows (or FP32 cannot resolve them)
+    if (ratio > 0.5 * prev && ++slow >= 2) { status = TTFLD_MAXITER; break; }
+    prev = ratio;
+    double target = 0.3 * tol / ratio;
+    if (target < kInnerReduce) target = kInnerReduce;
+    long long left = budget - total;
+    int its = 0;
+    if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, &its))) return rc;
+    total += its;
+    ++anchors;
+    kry_update_kernel<<<grid_cells(w->k.n), kThreads, 0, c->stream>>>(c->d, w->k, x);
+    count_launches(1);
+    TT_CHECK_LAUNCH();
+    if ((rc = anchor(c, w, x, b, hypre))) return rc;
+  }
+  if (st) {
+    st->sor_iter = (int)total;
+    st->corrections = anchors;
+    st->rhsnorm = c->host_sol->rhsnorm;
+    st->true_resid_l1 = c->host_sol->true_l1;
+    st->rnorm = l2 ? sqrt(c->host_sol->scratch[0]) : c->host_sol->true_l1;
+  }
+  return status;
+}
+
+}  // namespace
+
+int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
+  const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
+  return pcg_core(c, x, b, false, c->opts.tol, budget, false, guess_test, fallback, st);
+}
+
+void krylov_free(ttfld_ctx* c) {
+  KryWork* w = (KryWork*)c->krylov;
+  if (!w) return;
+  if (w->mem) cudaFree(w->mem);
+  free(w);
+  c->krylov = nullptr;
+}
+
+}  // namespace ttfld
+
+extern "C" {
+
+int ttfld_solve_with_hypre(ttfld_ctx* c, double tol, int maxit, ttfld_solve_stats* st) {
+  using namespace ttfld;
+  if (!c) return TTFLD_E_ARGS;
+  if (!(tol > 0.0)) tol = 1e-6;  // pphypre.f:45
+  if (maxit <= 0) maxit = 50;    // pphypre.f:54-55
+  TT_CHECK(cudaSetDevice(c->device));
+  ttfld_solve_stats local{};
+  if (!st) st = &local;
+  int rc = fill_sor_matrix(c, false);  // the 7-point rows; b is taken from RHS_ER as it is
+  if (rc) return rc;
+  Dev d = c->d;
+  // x = 1 in the interior (pphypre.f:136), ghosts 0
+  double* x = d.DELTA_ER;
+  TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) { x[hidx(d, i, j, k)] = 1.0; });
+  TT_CHECK_LAUNCH();
+  TT_CHECK(cudaEventRecord(c->ev0, c->stream));
+  rc = pcg_core(c, x, d.RHS, true, tol, maxit, true, 0, nullptr, st);
+  TT_CHECK(cudaEventRecord(c->ev1, c->stream));
+  TT_CHECK(cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  st->solve_ms = ms;
+  c->last_solve_ms = ms;
+  return rc;
+}
+
+}  // extern "C"

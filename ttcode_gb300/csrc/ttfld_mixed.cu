@@ -279,53 +279,12 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
   }
 }
 
-// Grid-wide barrier of the persistent kernel (a cooperative launch, so all
-// blocks are resident).  Thread 0 of each block arrives on a counter; the
-// last arrival resets it and advances the generation the others wait on.
-// The wait is bounded: after kBarrierSpins polls (well over a second with
-// the back-off) or once another block has given up, the block records the
-// timeout and returns false, and the kernel returns without further work.
-constexpr long long kBarrierSpins = 1LL << 23;
 // A norm sweep whose in-sweep ratio is not below kStallFactor times the
 // previous one (8 sweeps earlier) ends the inner loop: the FP32 iteration
 // has reached its rounding floor relative to the anchor (on stiff,
 // high-contrast systems after one or two decades), and re-anchoring in FP64
 // continues the same iteration.  A false alarm costs one FP64 residual.
 constexpr double kStallFactor = 0.999;
-
-__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
-  unsigned int v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) {
-  __shared__ int ok_sh;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned int g0 = ld_acquire(&sol->bar_gen);
-    __threadfence();
-    if (atomicAdd(&sol->bar_count, 1u) == nblocks - 1) {
-      atomicExch(&sol->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&sol->bar_gen, 1u);
-    } else {
-      long long polls = 0;
-      while (ld_acquire(&sol->bar_gen) == g0) {
-        if (++polls > kBarrierSpins || *(volatile int*)&sol->bar_timeout) {
-          atomicExch(&sol->bar_timeout, 1);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-    ok_sh = ok;
-  }
-  __syncthreads();
-  return ok_sh != 0;
-}
 
 constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
 

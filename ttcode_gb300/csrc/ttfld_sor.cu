@@ -17,7 +17,8 @@ namespace ttfld {
 
 // FILL_SOR_MATRIX ppsor.f:189-277 and B_VECTOR_BOUNDARIES ppsor.f:280-329,
 // one rank, poles=.false.
-int fill_sor_matrix(ttfld_ctx* c) {
+// zero_rhs = false leaves RHS_ER as it is (B_VECTOR_BOUNDARIES not applied).
+int fill_sor_matrix(ttfld_ctx* c, bool zero_rhs) {
   Dev d = c->d;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     size_t q = cidx(d, i, j, k);
@@ -33,7 +34,7 @@ int fill_sor_matrix(ttfld_ctx* c) {
     if (k == 2) f = 0.0;
     if (k == d.nz - 1) g = 0.0;
     d.SA[q] = a; d.SB[q] = b; d.SC[q] = cc; d.SD[q] = dd; d.SE[q] = e; d.SF[q] = f; d.SG[q] = g;
-    if (ident) d.RHS[q] = 0.0;
+    if (ident && zero_rhs) d.RHS[q] = 0.0;
   });
   TT_CHECK_LAUNCH();
   return 0;
@@ -285,6 +286,7 @@ int solve_current(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax
     case TTFLD_SOLVER_SOR64_EXACT: return solve_exact64(c, x, b, itmin, itmax, st);
     case TTFLD_SOLVER_SOR64_FAST: return solve_fast64(c, x, b, itmin, itmax, st);
     case TTFLD_SOLVER_MIXED: return solve_mixed(c, x, b, st);
+    case TTFLD_SOLVER_PCG: return solve_pcg(c, x, b, st);
   }
   return TTFLD_E_ARGS;
 }
@@ -336,8 +338,8 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
       if ((rc = rhs_norm(c, d.RHS, &bl1)) || (rc = true_residual(c, x, d.RHS, &gl1))) return rc;
       st->guess_resid_l1 = gl1;
       reject = !(gl1 < bl1);
-    } else if (race_sweeps > 0 && c->opts.solver == TTFLD_SOLVER_MIXED) {
-      race = true;  // the mixed solver races the guess against zero itself
+    } else if (race_sweeps > 0 && (c->opts.solver == TTFLD_SOLVER_MIXED || c->opts.solver == TTFLD_SOLVER_PCG)) {
+      race = true;  // the mixed solver races the guess against zero itself, PCG compares r.z
     } else if (race_sweeps > 0) {
       // race_sweeps FP64 red-black sweeps from the guess and as many from
       // zero, on a scratch copy: keep the guess if the in-sweep residual
@@ -367,7 +369,8 @@ int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st) {
   }
   TT_CHECK(cudaEventRecord(c->evg, c->stream));
   int rc;
-  if (race) rc = solve_mixed(c, d.DELTA_ER, d.RHS, st, c->opts.fallback_rule == 3 ? 5 : 2, &fallback);
+  if (race && c->opts.solver == TTFLD_SOLVER_PCG) rc = solve_pcg(c, d.DELTA_ER, d.RHS, st, 1, &fallback);
+  else if (race) rc = solve_mixed(c, d.DELTA_ER, d.RHS, st, c->opts.fallback_rule == 3 ? 5 : 2, &fallback);
   else rc = solve_current(c, d.DELTA_ER, d.RHS, 1, d.itmax, st);
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));

@@ -151,6 +151,13 @@ class FLD:
         check("solve_system", self.L.ttfld_solve_system(self.h, ctypes.byref(st)), ok=(0, 1, 2))
         return st
 
+    def solve_with_hypre(self, tol: float = 0.0, maxit: int = 0) -> _ffi.SolveStats:
+        """SOLVE_WITH_HYPRE (IRAD=2): PCG on the FILLHYPREMATRIX system; tol
+        and maxit 0 select the reference's 1e-6 and 50."""
+        st = _ffi.SolveStats()
+        check("SOLVE_WITH_HYPRE", self.L.ttfld_solve_with_hypre(self.h, tol, maxit, ctypes.byref(st)), ok=(0, 1))
+        return st
+
     def sor_sweeps(self, n: int):
         r, b = ctypes.c_double(), ctypes.c_double()
         check("sor_sweeps", self.L.ttfld_sor_sweeps(self.h, n, ctypes.byref(r), ctypes.byref(b)))
