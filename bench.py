@@ -208,6 +208,34 @@ def run_profile_solve(args):
     f.close()
 
 
+def run_profile_pcg(args):
+    """For the PCG summaries under profiles/: the shell256 system of one
+    implicit step, then inside cudaProfilerStart/Stop one PCG solve of
+    SOLVE_WITH_SOR's system (zero guess, 1e-10) and one SOLVE_WITH_HYPRE
+    with the reference's settings (1e-6, 50 iterations)."""
+    import torch
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import shell
+    torch.cuda.set_device(0)
+    sh = shell(SHELL, seed=1)
+    f = start_run(sh)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)
+    f.fill_sor_matrix()
+    f.set_solver("pcg", tol=1e-10)
+    f.solve_system()                       # warm: workspace allocated, kernels loaded
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    st = f.solve_system()
+    sh_st = f.solve_with_hypre()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({"pcg": {"ms": st.solve_ms, "iterations": st.sor_iter, "anchors": st.corrections},
+                      "hypre": {"ms": sh_st.solve_ms, "iterations": sh_st.sor_iter, "status": sh_st.status}}),
+          flush=True)
+    f.close()
+
+
 def run_profile_step(args):
     """For the step's launch list: the shell256 shell, two implicit steps
     (mixed solver, previous-step guess), then a third inside
@@ -496,6 +524,8 @@ def main():
                     help="only build the system and run 8 + 16 FP32 sweeps")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run three implicit steps, the third inside cudaProfilerStart/Stop")
+    ap.add_argument("--profile-pcg", action="store_true",
+                    help="only build the system and run one PCG and one SOLVE_WITH_HYPRE solve")
     args = ap.parse_args()
     if args.profile_solve:
         run_profile_solve(args)
@@ -505,6 +535,9 @@ def main():
         return
     if args.profile_step:
         run_profile_step(args)
+        return
+    if args.profile_pcg:
+        run_profile_pcg(args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -48,7 +48,7 @@
 namespace ttfld {
 namespace {
 
-constexpr int kPcgThreads = 768;   // one block per SM
+constexpr int kPcgThreads = 512;   // one block per SM (registers for the batched line pass)
 constexpr int kPcgStall = 25;      // iterations without a new minimum of r.z end an inner run
 constexpr double kInnerReduce = 1e-5;  // relative reduction of sqrt(r.z) asked of one inner run
 
@@ -195,8 +195,10 @@ __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, con
     const size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
     const size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
     const double bb = b_of(d, b, t, i, j, k, hypre != 0);
-    const double ax = r.a * x[q] + r.b * x[q - 1] + r.c * x[q + 1] + r.d * x[qjm] + r.e * x[qjp] + r.f * x[q - sk] +
-                      r.g * x[q + sk];
+    // a zero coupling contributes nothing, whatever the ghost it points at holds
+    const double ax = r.a * x[q] + (r.b != 0.0 ? r.b * x[q - 1] : 0.0) + (r.c != 0.0 ? r.c * x[q + 1] : 0.0) +
+                      (r.d != 0.0 ? r.d * x[qjm] : 0.0) + (r.e != 0.0 ? r.e * x[qjp] : 0.0) +
+                      (r.f != 0.0 ? r.f * x[q - sk] : 0.0) + (r.g != 0.0 ? r.g * x[q + sk] : 0.0);
     const double rr = bb - ax;
     const double sw = kr.sig[t] * kr.wgt[t];
     const double rs = sw * rr, bs = sw * bb;
@@ -241,38 +243,125 @@ __global__ void __launch_bounds__(kThreads) kry_update_kernel(Dev d, Kry kr, dou
   }
 }
 
-// One radial line of the inner iteration for column c.  With update, first
+// One radial line of the inner iteration for column c.  With UPDATE, first
 // e += alpha p and r -= alpha s along the line.  Then z = T^-1 r by the
 // factored tridiagonal T (forward: y_i = r_i - cr_{i-1} g_{i-1} y_{i-1},
 // kept in z; backward: z_i = (y_i - cr_i z_{i+1}) g_i).  Returns this
-// line's share of r.z.
-__device__ __forceinline__ double line_pass(const Kry& k, long long c, bool update, float alpha, const float* pn) {
-  const size_t ncol = (size_t)k.ncol;
+// line's share of r.z.  The loads of kLineBatch radii are issued before any
+// of their stores (the compiler may not move a load above a store it cannot
+// prove independent), so a pass waits one memory latency per batch, not per
+// radius.
+constexpr int kLineBatch = 8;
+template <bool UPDATE>
+__device__ __forceinline__ double line_pass(const Kry& k, long long c, float alpha, const float* pn) {
+  constexpr int U = kLineBatch;
+  // 32-bit offsets (a context holds fewer than 2^31 cells per array)
+  const unsigned int ncol = (unsigned int)k.ncol;
+  const unsigned int c0 = (unsigned int)c;
   const int nx = k.nx;
   float yprev = 0.f, lprev = 0.f;
-  size_t q = (size_t)c;
-  for (int i = 0; i < nx; ++i, q += ncol) {
-    float ri = k.r[q];
-    if (update) {
-      k.e[q] = fmaf(alpha, pn[q], k.e[q]);
-      ri = fmaf(-alpha, k.s[q], ri);
-      k.r[q] = ri;
+  for (int i0 = 0; i0 < nx; i0 += U) {
+    const unsigned int qb = c0 + (unsigned int)i0 * ncol;
+    float rr[U], cc[U], gg[U], pp[U], ss[U], ee[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u < nx) {
+        const unsigned int q = qb + (unsigned int)u * ncol;
+        rr[u] = k.r[q];
+        cc[u] = k.cr[q];
+        gg[u] = k.g[q];
+        if (UPDATE) {
+          pp[u] = pn[q];
+          ss[u] = k.s[q];
+          ee[u] = k.e[q];
+        }
+      }
     }
-    const float y = fmaf(-lprev, yprev, ri);
-    k.z[q] = y;
-    lprev = k.cr[q] * k.g[q];
-    yprev = y;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u < nx) {
+        const unsigned int q = qb + (unsigned int)u * ncol;
+        float ri = rr[u];
+        if (UPDATE) {
+          k.e[q] = fmaf(alpha, pp[u], ee[u]);
+          ri = fmaf(-alpha, ss[u], ri);
+          k.r[q] = ri;
+        }
+        const float y = fmaf(-lprev, yprev, ri);
+        k.z[q] = y;
+        lprev = cc[u] * gg[u];
+        yprev = y;
+      }
+    }
   }
   double dot = 0.0;
   float znext = 0.f;
-  q = (size_t)c + (size_t)(nx - 1) * ncol;
-  for (int i = nx - 1; i >= 0; --i, q -= ncol) {
-    const float zi = fmaf(-k.cr[q], znext, k.z[q]) * k.g[q];
-    k.z[q] = zi;
-    znext = zi;
-    dot += (double)k.r[q] * (double)zi;
+  for (int i1 = nx - 1; i1 >= 0; i1 -= U) {
+    const unsigned int qb = c0 + (unsigned int)i1 * ncol;
+    float yy[U], cc[U], gg[U], rr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i1 - u >= 0) {
+        const unsigned int q = qb - (unsigned int)u * ncol;
+        yy[u] = k.z[q];
+        cc[u] = k.cr[q];
+        gg[u] = k.g[q];
+        rr[u] = k.r[q];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i1 - u >= 0) {
+        const unsigned int q = qb - (unsigned int)u * ncol;
+        const float zi = fmaf(-cc[u], znext, yy[u]) * gg[u];
+        k.z[q] = zi;
+        znext = zi;
+        dot += (double)rr[u] * (double)zi;
+      }
+    }
   }
   return dot;
+}
+
+__device__ __forceinline__ float4 ldf4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void stf4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {
+  return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+__device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
+  return make_float4(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z), fmaf(a.w, b.w, c.w));
+}
+
+// The operator pass on four cells q..q+3 of one phi row (NY a multiple of
+// four, q a multiple of four): p_new = z + beta p_old, s = S p_new; returns
+// p_new . s of the four.
+__device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* pn, float beta, long long q) {
+  const long long ncol = k.ncol;
+  const int ny = k.ny;
+  const long long il = q / ncol;
+  const long long cc = q - il * ncol;
+  const int j0 = (int)(cc % ny);
+  const long long k0 = cc / ny;
+  const float4 pc = axpy4(beta, ldf4(po + q), ldf4(k.z + q));
+  float4 sv = pc;
+  if (il + 1 < k.nx) sv = fma4(ldf4(k.cr + q), axpy4(beta, ldf4(po + q + ncol), ldf4(k.z + q + ncol)), sv);
+  if (il > 0) sv = fma4(ldf4(k.cr + q - ncol), axpy4(beta, ldf4(po + q - ncol), ldf4(k.z + q - ncol)), sv);
+  if (k0 + 1 < k.nz) sv = fma4(ldf4(k.ct + q), axpy4(beta, ldf4(po + q + ny), ldf4(k.z + q + ny)), sv);
+  if (k0 > 0) sv = fma4(ldf4(k.ct + q - ny), axpy4(beta, ldf4(po + q - ny), ldf4(k.z + q - ny)), sv);
+  // phi: the cells j0-1 and j0+4 (periodic) and the coupling (j0-1, j0)
+  const long long qm = j0 == 0 ? q + ny - 1 : q - 1;
+  const long long qp = j0 + 4 == ny ? q + 4 - ny : q + 4;
+  const float pl = fmaf(beta, po[qm], k.z[qm]);
+  const float pr = fmaf(beta, po[qp], k.z[qp]);
+  const float cl = k.cp[qm];
+  const float4 cp = ldf4(k.cp + q);
+  sv.x = fmaf(cp.x, pc.y, fmaf(cl, pl, sv.x));
+  sv.y = fmaf(cp.y, pc.z, fmaf(cp.x, pc.x, sv.y));
+  sv.z = fmaf(cp.z, pc.w, fmaf(cp.y, pc.y, sv.z));
+  sv.w = fmaf(cp.w, pr, fmaf(cp.z, pc.z, sv.w));
+  stf4(pn + q, pc);
+  stf4(k.s + q, sv);
+  return (double)pc.x * sv.x + (double)pc.y * sv.y + (double)pc.z * sv.z + (double)pc.w * sv.w;
 }
 
 // The FP32 PCG iteration on S e = r from e = 0 (r, e set by the anchor).
@@ -302,7 +391,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
 
   // z0 = T^-1 r0, gamma0 = r0.z0
   double acc = 0.0;
-  for (long long c = col0; c < ncol; c += colstride) acc += line_pass(k, c, false, 0.f, nullptr);
+  for (long long c = col0; c < ncol; c += colstride) acc += line_pass<false>(k, c, 0.f, nullptr);
   {
     const double v = block_sum(acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -330,24 +419,28 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     float* pn = cur ? k.p[0] : k.p[1];
     // operator phase: p_new = z + beta p_old, s = S p_new, p_new . s
     acc = 0.0;
-    for (long long q = tid; q < n; q += nth) {
-      const long long il = q / ncol;
-      const long long cc = q - il * ncol;
-      const int j0 = (int)(cc % ny);
-      const long long k0 = cc / ny;
-      const float pc = fmaf(beta, po[q], k.z[q]);
-      float sv = pc;
-      if (il + 1 < k.nx) sv = fmaf(k.cr[q], fmaf(beta, po[q + ncol], k.z[q + ncol]), sv);
-      if (il > 0) sv = fmaf(k.cr[q - ncol], fmaf(beta, po[q - ncol], k.z[q - ncol]), sv);
-      const long long qjp = j0 == ny - 1 ? q - (ny - 1) : q + 1;
-      const long long qjm = j0 == 0 ? q + (ny - 1) : q - 1;
-      sv = fmaf(k.cp[q], fmaf(beta, po[qjp], k.z[qjp]), sv);
-      sv = fmaf(k.cp[qjm], fmaf(beta, po[qjm], k.z[qjm]), sv);
-      if (k0 + 1 < nzl) sv = fmaf(k.ct[q], fmaf(beta, po[q + ny], k.z[q + ny]), sv);
-      if (k0 > 0) sv = fmaf(k.ct[q - ny], fmaf(beta, po[q - ny], k.z[q - ny]), sv);
-      pn[q] = pc;
-      k.s[q] = sv;
-      acc += (double)pc * (double)sv;
+    if ((ny & 3) == 0) {
+      for (long long g = tid; g < (n >> 2); g += nth) acc += op_quad(k, po, pn, beta, g << 2);
+    } else {
+      for (long long q = tid; q < n; q += nth) {
+        const long long il = q / ncol;
+        const long long cc = q - il * ncol;
+        const int j0 = (int)(cc % ny);
+        const long long k0 = cc / ny;
+        const float pc = fmaf(beta, po[q], k.z[q]);
+        float sv = pc;
+        if (il + 1 < k.nx) sv = fmaf(k.cr[q], fmaf(beta, po[q + ncol], k.z[q + ncol]), sv);
+        if (il > 0) sv = fmaf(k.cr[q - ncol], fmaf(beta, po[q - ncol], k.z[q - ncol]), sv);
+        const long long qjp = j0 == ny - 1 ? q - (ny - 1) : q + 1;
+        const long long qjm = j0 == 0 ? q + (ny - 1) : q - 1;
+        sv = fmaf(k.cp[q], fmaf(beta, po[qjp], k.z[qjp]), sv);
+        sv = fmaf(k.cp[qjm], fmaf(beta, po[qjm], k.z[qjm]), sv);
+        if (k0 + 1 < nzl) sv = fmaf(k.ct[q], fmaf(beta, po[q + ny], k.z[q + ny]), sv);
+        if (k0 > 0) sv = fmaf(k.ct[q - ny], fmaf(beta, po[q - ny], k.z[q - ny]), sv);
+        pn[q] = pc;
+        k.s[q] = sv;
+        acc += (double)pc * (double)sv;
+      }
     }
     {
       const double v = block_sum(acc, sh);
@@ -370,7 +463,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     const float alpha = (float)(gamma / ps);
     // line phase: e += alpha p_new, r -= alpha s, z = T^-1 r, r.z
     acc = 0.0;
-    for (long long c = col0; c < ncol; c += colstride) acc += line_pass(k, c, true, alpha, pn);
+    for (long long c = col0; c < ncol; c += colstride) acc += line_pass<true>(k, c, alpha, pn);
     {
       const double v = block_sum(acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -570,12 +663,17 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     TT_CHECK_LAUNCH();
     if ((rc = anchor(c, w, x, b, hypre))) return rc;
   }
+  // SOLVE_WITH_SOR leaves the phi halo of DELTA_ER refreshed (PLANETSHIFT(8)
+  // after the last colour); SOLVE_WITH_HYPRE writes the interior only and its
+  // caller shifts (ppenergy.f:353-356)
+  if (!hypre && (rc = halo_shift(c, x))) return rc;
   if (st) {
     st->sor_iter = (int)total;
     st->corrections = anchors;
     st->rhsnorm = c->host_sol->rhsnorm;
     st->true_resid_l1 = c->host_sol->true_l1;
     st->rnorm = l2 ? sqrt(c->host_sol->scratch[0]) : c->host_sol->true_l1;
+    st->status = status;
   }
   return status;
 }
@@ -610,9 +708,9 @@ int ttfld_solve_with_hypre(ttfld_ctx* c, double tol, int maxit, ttfld_solve_stat
   int rc = fill_sor_matrix(c, false);  // the 7-point rows; b is taken from RHS_ER as it is
   if (rc) return rc;
   Dev d = c->d;
-  // x = 1 in the interior (pphypre.f:136), ghosts 0
+  // x = 1 in the interior (pphypre.f:136); the halo is left as it is, as
+  // SOLVE_WITH_HYPRE only writes delta_ER(1:NX,1:NY,1:NZ) (pphypre.f:84-92)
   double* x = d.DELTA_ER;
-  TT_CHECK(cudaMemsetAsync(x, 0, nhalo(d) * 8, c->stream));
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) { x[hidx(d, i, j, k)] = 1.0; });
   TT_CHECK_LAUNCH();
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
