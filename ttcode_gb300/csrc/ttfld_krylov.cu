@@ -48,7 +48,7 @@
 namespace ttfld {
 namespace {
 
-constexpr int kPcgThreads = 512;   // one block per SM (registers for the batched line pass)
+constexpr int kPcgThreads = 256;   // one block per SM; 248 registers for the batched passes
 constexpr int kPcgStall = 25;      // iterations without a new minimum of r.z end an inner run
 constexpr double kInnerReduce = 1e-5;  // relative reduction of sqrt(r.z) asked of one inner run
 
@@ -244,16 +244,16 @@ __global__ void __launch_bounds__(kThreads) kry_update_kernel(Dev d, Kry kr, dou
 }
 
 // One radial line of the inner iteration for column c.  With UPDATE, first
-// e += alpha p and r -= alpha s along the line.  Then z = T^-1 r by the
-// factored tridiagonal T (forward: y_i = r_i - cr_{i-1} g_{i-1} y_{i-1},
-// kept in z; backward: z_i = (y_i - cr_i z_{i+1}) g_i).  Returns this
-// line's share of r.z.  The loads of kLineBatch radii are issued before any
-// of their stores (the compiler may not move a load above a store it cannot
-// prove independent), so a pass waits one memory latency per batch, not per
-// radius.
-constexpr int kLineBatch = 8;
+// r -= alpha s along the line.  Then z = T^-1 r by the factored tridiagonal
+// T (forward: y_i = r_i - cr_{i-1} g_{i-1} y_{i-1}, kept in z; backward:
+// z_i = (y_i - cr_i z_{i+1}) g_i).  Returns this line's share of r.z.  The
+// loads of kLineBatch radii are issued before any of their stores (the
+// compiler may not move a load above a store it cannot prove independent,
+// and a warp stalls at the first use of a pending load), so a pass waits
+// one memory latency per batch, not per radius.
+constexpr int kLineBatch = 16;
 template <bool UPDATE>
-__device__ __forceinline__ double line_pass(const Kry& k, long long c, float alpha, const float* pn) {
+__device__ __forceinline__ double line_pass(const Kry& k, long long c, float alpha) {
   constexpr int U = kLineBatch;
   // 32-bit offsets (a context holds fewer than 2^31 cells per array)
   const unsigned int ncol = (unsigned int)k.ncol;
@@ -262,7 +262,7 @@ __device__ __forceinline__ double line_pass(const Kry& k, long long c, float alp
   float yprev = 0.f, lprev = 0.f;
   for (int i0 = 0; i0 < nx; i0 += U) {
     const unsigned int qb = c0 + (unsigned int)i0 * ncol;
-    float rr[U], cc[U], gg[U], pp[U], ss[U], ee[U];
+    float rr[U], cc[U], gg[U], ss[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       if (i0 + u < nx) {
@@ -270,11 +270,7 @@ __device__ __forceinline__ double line_pass(const Kry& k, long long c, float alp
         rr[u] = k.r[q];
         cc[u] = k.cr[q];
         gg[u] = k.g[q];
-        if (UPDATE) {
-          pp[u] = pn[q];
-          ss[u] = k.s[q];
-          ee[u] = k.e[q];
-        }
+        if (UPDATE) ss[u] = k.s[q];
       }
     }
 #pragma unroll
@@ -283,7 +279,6 @@ __device__ __forceinline__ double line_pass(const Kry& k, long long c, float alp
         const unsigned int q = qb + (unsigned int)u * ncol;
         float ri = rr[u];
         if (UPDATE) {
-          k.e[q] = fmaf(alpha, pp[u], ee[u]);
           ri = fmaf(-alpha, ss[u], ri);
           k.r[q] = ri;
         }
@@ -331,30 +326,42 @@ __device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {
 __device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
   return make_float4(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z), fmaf(a.w, b.w, c.w));
 }
+__device__ __forceinline__ float4 keep4(bool on, float4 v) { return on ? v : make_float4(0.f, 0.f, 0.f, 0.f); }
 
 // The operator pass on four cells q..q+3 of one phi row (NY a multiple of
-// four, q a multiple of four): p_new = z + beta p_old, s = S p_new; returns
-// p_new . s of the four.
-__device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* pn, float beta, long long q) {
+// four, q a multiple of four): e += alpha_prev p_old (the previous
+// iteration's update of e, deferred to here so that the line pass reads
+// fewer arrays), p_new = z + beta p_old, s = S p_new; returns p_new . s.
+// Every load is issued before the first arithmetic (neighbours that do not
+// exist are read at q and their couplings zeroed), so the quad waits one
+// memory latency.
+__device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
+                                          long long q) {
   const long long ncol = k.ncol;
   const int ny = k.ny;
   const long long il = q / ncol;
   const long long cc = q - il * ncol;
   const int j0 = (int)(cc % ny);
   const long long k0 = cc / ny;
-  const float4 pc = axpy4(beta, ldf4(po + q), ldf4(k.z + q));
-  float4 sv = pc;
-  if (il + 1 < k.nx) sv = fma4(ldf4(k.cr + q), axpy4(beta, ldf4(po + q + ncol), ldf4(k.z + q + ncol)), sv);
-  if (il > 0) sv = fma4(ldf4(k.cr + q - ncol), axpy4(beta, ldf4(po + q - ncol), ldf4(k.z + q - ncol)), sv);
-  if (k0 + 1 < k.nz) sv = fma4(ldf4(k.ct + q), axpy4(beta, ldf4(po + q + ny), ldf4(k.z + q + ny)), sv);
-  if (k0 > 0) sv = fma4(ldf4(k.ct + q - ny), axpy4(beta, ldf4(po + q - ny), ldf4(k.z + q - ny)), sv);
-  // phi: the cells j0-1 and j0+4 (periodic) and the coupling (j0-1, j0)
-  const long long qm = j0 == 0 ? q + ny - 1 : q - 1;
+  const bool hn = il + 1 < k.nx, hs = il > 0, ht = k0 + 1 < k.nz, hb = k0 > 0;
+  const long long qn = hn ? q + ncol : q, qs = hs ? q - ncol : q;
+  const long long qt = ht ? q + ny : q, qb = hb ? q - ny : q;
+  const long long qm = j0 == 0 ? q + ny - 1 : q - 1;   // phi neighbours (periodic)
   const long long qp = j0 + 4 == ny ? q + 4 - ny : q + 4;
-  const float pl = fmaf(beta, po[qm], k.z[qm]);
-  const float pr = fmaf(beta, po[qp], k.z[qp]);
-  const float cl = k.cp[qm];
+  const float4 zc = ldf4(k.z + q), oc = ldf4(po + q), ec = ldf4(k.e + q);
+  const float4 zn = ldf4(k.z + qn), on = ldf4(po + qn), zs = ldf4(k.z + qs), os = ldf4(po + qs);
+  const float4 zt = ldf4(k.z + qt), ot = ldf4(po + qt), zb = ldf4(k.z + qb), ob = ldf4(po + qb);
+  const float4 crn = ldf4(k.cr + q), crs = ldf4(k.cr + qs), ctt = ldf4(k.ct + q), ctb = ldf4(k.ct + qb);
   const float4 cp = ldf4(k.cp + q);
+  const float zm = k.z[qm], om = po[qm], zp = k.z[qp], op = po[qp], cl = k.cp[qm];
+  stf4(k.e + q, axpy4(alpha_prev, oc, ec));
+  const float4 pc = axpy4(beta, oc, zc);
+  float4 sv = pc;
+  sv = fma4(keep4(hn, crn), axpy4(beta, on, zn), sv);
+  sv = fma4(keep4(hs, crs), axpy4(beta, os, zs), sv);
+  sv = fma4(keep4(ht, ctt), axpy4(beta, ot, zt), sv);
+  sv = fma4(keep4(hb, ctb), axpy4(beta, ob, zb), sv);
+  const float pl = fmaf(beta, om, zm), pr = fmaf(beta, op, zp);
   sv.x = fmaf(cp.x, pc.y, fmaf(cl, pl, sv.x));
   sv.y = fmaf(cp.y, pc.z, fmaf(cp.x, pc.x, sv.y));
   sv.z = fmaf(cp.z, pc.w, fmaf(cp.y, pc.y, sv.z));
@@ -364,15 +371,49 @@ __device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* 
   return (double)pc.x * sv.x + (double)pc.y * sv.y + (double)pc.z * sv.z + (double)pc.w * sv.w;
 }
 
+// The same for one cell (NY not a multiple of four).
+__device__ __forceinline__ double op_one(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
+                                         long long q) {
+  const long long ncol = k.ncol;
+  const int ny = k.ny;
+  const long long il = q / ncol;
+  const long long cc = q - il * ncol;
+  const int j0 = (int)(cc % ny);
+  const long long k0 = cc / ny;
+  const bool hn = il + 1 < k.nx, hs = il > 0, ht = k0 + 1 < k.nz, hb = k0 > 0;
+  const long long qn = hn ? q + ncol : q, qs = hs ? q - ncol : q;
+  const long long qt = ht ? q + ny : q, qb = hb ? q - ny : q;
+  const long long qm = j0 == 0 ? q + ny - 1 : q - 1;
+  const long long qp = j0 == ny - 1 ? q - (ny - 1) : q + 1;
+  const float zc = k.z[q], oc = po[q], ec = k.e[q];
+  const float zn = k.z[qn], on = po[qn], zs = k.z[qs], os = po[qs], zt = k.z[qt], ot = po[qt];
+  const float zb = k.z[qb], ob = po[qb], zm = k.z[qm], om = po[qm], zp = k.z[qp], op = po[qp];
+  const float crn = k.cr[q], crs = k.cr[qs], ctt = k.ct[q], ctb = k.ct[qb], cpp = k.cp[q], cpm = k.cp[qm];
+  k.e[q] = fmaf(alpha_prev, oc, ec);
+  const float pc = fmaf(beta, oc, zc);
+  float sv = pc;
+  sv = fmaf(hn ? crn : 0.f, fmaf(beta, on, zn), sv);
+  sv = fmaf(hs ? crs : 0.f, fmaf(beta, os, zs), sv);
+  sv = fmaf(ht ? ctt : 0.f, fmaf(beta, ot, zt), sv);
+  sv = fmaf(hb ? ctb : 0.f, fmaf(beta, ob, zb), sv);
+  sv = fmaf(cpp, fmaf(beta, op, zp), sv);
+  sv = fmaf(cpm, fmaf(beta, om, zm), sv);
+  pn[q] = pc;
+  k.s[q] = sv;
+  return (double)pc * sv;
+}
+
 // The FP32 PCG iteration on S e = r from e = 0 (r, e set by the anchor).
 // Line phases: the warps of all blocks are dealt round-robin over groups of
 // 32 consecutive columns.  Operator phase: p_new = z + beta p (p read from
 // p[cur], written to p[1-cur], so that neighbours read the old values),
-// s = S p_new.  Every block forms alpha and beta from all block partials in
-// the same fixed order, so all blocks take the same decisions.  The run ends
-// when sqrt(r.z / r0.z0) <= stop_ratio, after kPcgStall iterations without
-// a new minimum of r.z (the FP32 floor), on a non-positive p.s, or after
-// maxit iterations; maxit = 0 only computes r0.z0 (sol->scratch[2]).
+// s = S p_new, and the previous iteration's e += alpha p.  Every block forms
+// alpha and beta from all block partials in the same fixed order, so all
+// blocks take the same decisions.  The run ends when sqrt(r.z / r0.z0) <=
+// stop_ratio, after kPcgStall iterations without a new minimum of r.z (the
+// FP32 floor), on a non-positive p.s, or after maxit iterations; the last
+// iteration's e update is then applied.  maxit = 0 only computes r0.z0
+// (sol->scratch[2]).
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, SolverDev* sol, double* partials,
                                                                    int maxit, double stop_ratio) {
   __shared__ double sh[32];
@@ -380,7 +421,6 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   const unsigned int nb = gridDim.x;
   const long long n = k.n, ncol = k.ncol;
   const int ny = k.ny;
-  const long long nzl = k.nz;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nth = (long long)gridDim.x * blockDim.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -391,7 +431,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
 
   // z0 = T^-1 r0, gamma0 = r0.z0
   double acc = 0.0;
-  for (long long c = col0; c < ncol; c += colstride) acc += line_pass<false>(k, c, 0.f, nullptr);
+  for (long long c = col0; c < ncol; c += colstride) acc += line_pass<false>(k, c, 0.f);
   {
     const double v = block_sum(acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -412,36 +452,21 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   const double stop2 = stop_ratio * stop_ratio * gamma0;
   double gmin = gamma0;
   int since_min = 0;
-  float beta = 0.f;
+  float beta = 0.f, alpha_prev = 0.f;
   int cur = 0;
+  bool pending = false;  // e += alpha_prev p[cur] still to be applied
   for (int it = 1; it <= maxit; ++it) {
     const float* po = cur ? k.p[1] : k.p[0];
     float* pn = cur ? k.p[0] : k.p[1];
-    // operator phase: p_new = z + beta p_old, s = S p_new, p_new . s
+    // operator phase
     acc = 0.0;
+    const float ap = pending ? alpha_prev : 0.f;
     if ((ny & 3) == 0) {
-      for (long long g = tid; g < (n >> 2); g += nth) acc += op_quad(k, po, pn, beta, g << 2);
+      for (long long g = tid; g < (n >> 2); g += nth) acc += op_quad(k, po, pn, beta, ap, g << 2);
     } else {
-      for (long long q = tid; q < n; q += nth) {
-        const long long il = q / ncol;
-        const long long cc = q - il * ncol;
-        const int j0 = (int)(cc % ny);
-        const long long k0 = cc / ny;
-        const float pc = fmaf(beta, po[q], k.z[q]);
-        float sv = pc;
-        if (il + 1 < k.nx) sv = fmaf(k.cr[q], fmaf(beta, po[q + ncol], k.z[q + ncol]), sv);
-        if (il > 0) sv = fmaf(k.cr[q - ncol], fmaf(beta, po[q - ncol], k.z[q - ncol]), sv);
-        const long long qjp = j0 == ny - 1 ? q - (ny - 1) : q + 1;
-        const long long qjm = j0 == 0 ? q + (ny - 1) : q - 1;
-        sv = fmaf(k.cp[q], fmaf(beta, po[qjp], k.z[qjp]), sv);
-        sv = fmaf(k.cp[qjm], fmaf(beta, po[qjm], k.z[qjm]), sv);
-        if (k0 + 1 < nzl) sv = fmaf(k.ct[q], fmaf(beta, po[q + ny], k.z[q + ny]), sv);
-        if (k0 > 0) sv = fmaf(k.ct[q - ny], fmaf(beta, po[q - ny], k.z[q - ny]), sv);
-        pn[q] = pc;
-        k.s[q] = sv;
-        acc += (double)pc * (double)sv;
-      }
+      for (long long q = tid; q < n; q += nth) acc += op_one(k, po, pn, beta, ap, q);
     }
+    pending = false;
     {
       const double v = block_sum(acc, sh);
       if (threadIdx.x == 0) pa[blockIdx.x] = v;
@@ -458,17 +483,20 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
         sol->stalled = 1;
         if (!isfinite(ps)) sol->nonfinite = 1;
       }
-      return;
+      break;
     }
     const float alpha = (float)(gamma / ps);
-    // line phase: e += alpha p_new, r -= alpha s, z = T^-1 r, r.z
+    // line phase: r -= alpha s, z = T^-1 r, r.z
     acc = 0.0;
-    for (long long c = col0; c < ncol; c += colstride) acc += line_pass<true>(k, c, alpha, pn);
+    for (long long c = col0; c < ncol; c += colstride) acc += line_pass<true>(k, c, alpha);
     {
       const double v = block_sum(acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+    alpha_prev = alpha;
+    pending = true;
+    cur = 1 - cur;  // p[cur] is now this iteration's p
     if (!grid_sync(sol, nb)) return;
     {
       const double tot = block_sum_array(pb, nb, sh);
@@ -476,24 +504,27 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
       __syncthreads();
     }
     const double gnew = bc[2];
-    cur = 1 - cur;
     if (!isfinite(gnew)) {
       if (blockIdx.x == 0 && threadIdx.x == 0) sol->nonfinite = 1;
-      return;
+      break;
     }
     if (gnew < gmin) {
       gmin = gnew;
       since_min = 0;
     } else if (++since_min >= kPcgStall) {
       if (blockIdx.x == 0 && threadIdx.x == 0) sol->stalled = 1;
-      return;
+      break;
     }
     if (!(gnew > stop2)) {
       if (blockIdx.x == 0 && threadIdx.x == 0) sol->done = 1;
-      return;
+      break;
     }
     beta = (float)(gnew / gamma);
     gamma = gnew;
+  }
+  if (pending) {
+    const float* pl = cur ? k.p[1] : k.p[0];
+    for (long long q = tid; q < n; q += nth) k.e[q] = fmaf(alpha_prev, pl[q], k.e[q]);
   }
 }
 
