@@ -338,6 +338,15 @@ def run_gpu(args):
     # the same mixed solver from the zero guess
     zl = [solve_timed("mixed", "zero") for _ in range(3)]
     zero_guess = {"ms": min(m for m, _ in zl), "sweeps": zl[-1][1].sor_iter}
+    # the same system by FP32 PCG (radial line preconditioner) in FP64 defect
+    # correction, same stopping rule, from zero and from the learned guess
+    pcg = {}
+    for g in ("zero", "learned"):
+        pl = [solve_timed("pcg", g) for _ in range(3)]
+        xs = f.download("DELTA_ER")
+        pcg[g] = {"ms": min(m for m, _ in pl), "iterations": pl[-1][1].sor_iter,
+                  "anchors": pl[-1][1].corrections, "fallback": pl[-1][1].fallback,
+                  "err_vs_fp64_1e-12": float(np.linalg.norm((xs - x_ref).ravel()) / np.linalg.norm(x_ref.ravel()))}
     # the plain FP64 red-black SOR on the same GPU (same stopping rule as the
     # reference, in-sweep L1 ratio <= 1e-10)
     plain = {}
@@ -401,7 +410,7 @@ def run_gpu(args):
                    "l2": "flushed between timed solves (256 MB write)", "parallelism": "replicas"},
         "sweeps_per_solve": stats[-1].sor_iter, "corrections_per_solve": stats[-1].corrections,
         "fallbacks": int(sum(s.fallback for s in stats)), "guess_ms": stats[-1].guess_ms,
-        "guess_training": train_info, "zero_guess_mixed": zero_guess,
+        "guess_training": train_info, "zero_guess_mixed": zero_guess, "pcg": pcg,
         "true_rel_residual": r_l1 / b_l1,
         "err_vs_fp64_1e-12": err, "fp64_1e-12_sweeps": st_ref.sor_iter,
         "plain_fp64": plain,

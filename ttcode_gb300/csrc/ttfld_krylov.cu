@@ -31,7 +31,7 @@
 // Preconditioner.  The radial couplings dominate by two to three orders of
 // magnitude (the shell is thin in r), so the preconditioner is the exact
 // solve of the tridiagonal radial line of every (j,k) column, factored once
-// per solve (Thomas algorithm, FP64 pivots stored in FP32).
+// per solve (Thomas algorithm, FP32 pivots).
 //
 // Layout.  The FP32 inner arrays are line-major, q = (i-1)*NY*NZ +
 // (k-1)*NY + (j-1): in a line solve one thread walks one column and the
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kThreads) kry_weights_kernel(Dev d, Kry kr, in
     const double dd = w * r.a;
     bool ok = (decoupled || e8 < 0.0) && dd > 0.0 && isfinite(dd);
     kr.wgt[t] = ok ? w : 0.0;
-    kr.sig[t] = ok ? 1.0 / sqrt(dd) : 0.0;
+    kr.sig[t] = ok ? rsqrt(dd) : 0.0;  // any positive scaling serves; it is used consistently
     if (!ok) atomicExch(&d.sol->bad_weights, 1);
   }
 }
@@ -158,18 +158,19 @@ __global__ void __launch_bounds__(kThreads) kry_couplings_kernel(Dev d, Kry kr, 
 }
 
 // Reciprocal pivots of every radial line (diagonal 1, off-diagonal cr):
-// u_1 = 1, u_i = 1 - cr_{i-1}^2 / u_{i-1}; g = 1/u.  One thread per column.
+// u_1 = 1, u_i = 1 - cr_{i-1}^2 / u_{i-1}; g = 1/u.  One thread per column;
+// FP32 (the factorisation only preconditions).
 __global__ void __launch_bounds__(kThreads) kry_factor_kernel(Kry kr, SolverDev* sol) {
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < kr.ncol;
        c += (long long)gridDim.x * blockDim.x) {
-    double g = 1.0, cprev = 0.0;
+    float g = 1.f, cprev = 0.f;
     size_t q = (size_t)c;
     for (int i = 0; i < kr.nx; ++i, q += kr.ncol) {
-      const double u = 1.0 - cprev * cprev * g;
-      if (!(u > 0.0)) atomicExch(&sol->bad_weights, 1);
-      g = 1.0 / u;
-      kr.g[q] = (float)g;
-      cprev = (double)kr.cr[q];
+      const float u = fmaf(-cprev * cprev, g, 1.f);
+      if (!(u > 0.f)) atomicExch(&sol->bad_weights, 1);
+      g = 1.f / u;
+      kr.g[q] = g;
+      cprev = kr.cr[q];
     }
   }
 }
@@ -701,9 +702,10 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
   if (st) {
     st->sor_iter = (int)total;
     st->corrections = anchors;
-    st->rhsnorm = c->host_sol->rhsnorm;
-    st->true_resid_l1 = c->host_sol->true_l1;
+    // rnorm / rhsnorm is the stopping measure (L1, or the scaled 2-norm)
+    st->rhsnorm = l2 ? sqrt(c->host_sol->scratch[1]) : c->host_sol->rhsnorm;
     st->rnorm = l2 ? sqrt(c->host_sol->scratch[0]) : c->host_sol->true_l1;
+    st->true_resid_l1 = c->host_sol->true_l1;
     st->status = status;
   }
   return status;
