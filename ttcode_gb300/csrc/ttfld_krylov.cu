@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) kry_update_kernel(Dev d, Kry kr, dou
 // one memory latency per batch, not per radius.
 constexpr int kLineBatch = 16;
 template <bool UPDATE>
-__device__ __forceinline__ double line_pass(const Kry& k, long long c, float alpha) {
+__device__ __forceinline__ float line_pass(const Kry& k, long long c, float alpha) {
   constexpr int U = kLineBatch;
   // 32-bit offsets (a context holds fewer than 2^31 cells per array)
   const unsigned int ncol = (unsigned int)k.ncol;
@@ -290,7 +290,7 @@ __device__ __forceinline__ double line_pass(const Kry& k, long long c, float alp
       }
     }
   }
-  double dot = 0.0;
+  float dot = 0.f;
   float znext = 0.f;
   for (int i1 = nx - 1; i1 >= 0; i1 -= U) {
     const unsigned int qb = c0 + (unsigned int)i1 * ncol;
@@ -312,7 +312,7 @@ __device__ __forceinline__ double line_pass(const Kry& k, long long c, float alp
         const float zi = fmaf(-cc[u], znext, yy[u]) * gg[u];
         k.z[q] = zi;
         znext = zi;
-        dot += (double)rr[u] * (double)zi;
+        dot = fmaf(rr[u], zi, dot);
       }
     }
   }
@@ -336,8 +336,8 @@ __device__ __forceinline__ float4 keep4(bool on, float4 v) { return on ? v : mak
 // Every load is issued before the first arithmetic (neighbours that do not
 // exist are read at q and their couplings zeroed), so the quad waits one
 // memory latency.
-__device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
-                                          long long q) {
+__device__ __forceinline__ float op_quad(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
+                                         long long q) {
   const long long ncol = k.ncol;
   const int ny = k.ny;
   const long long il = q / ncol;
@@ -369,12 +369,12 @@ __device__ __forceinline__ double op_quad(const Kry& k, const float* po, float* 
   sv.w = fmaf(cp.w, pr, fmaf(cp.z, pc.z, sv.w));
   stf4(pn + q, pc);
   stf4(k.s + q, sv);
-  return (double)pc.x * sv.x + (double)pc.y * sv.y + (double)pc.z * sv.z + (double)pc.w * sv.w;
+  return fmaf(pc.x, sv.x, fmaf(pc.y, sv.y, fmaf(pc.z, sv.z, pc.w * sv.w)));
 }
 
 // The same for one cell (NY not a multiple of four).
-__device__ __forceinline__ double op_one(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
-                                         long long q) {
+__device__ __forceinline__ float op_one(const Kry& k, const float* po, float* pn, float beta, float alpha_prev,
+                                        long long q) {
   const long long ncol = k.ncol;
   const int ny = k.ny;
   const long long il = q / ncol;
@@ -401,7 +401,7 @@ __device__ __forceinline__ double op_one(const Kry& k, const float* po, float* p
   sv = fmaf(cpm, fmaf(beta, om, zm), sv);
   pn[q] = pc;
   k.s[q] = sv;
-  return (double)pc * sv;
+  return pc * sv;
 }
 
 // The FP32 PCG iteration on S e = r from e = 0 (r, e set by the anchor).
@@ -430,11 +430,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   double* pa = partials;                 // operator-phase partials
   double* pb = partials + kMaxPartials;  // line-phase partials
 
-  // z0 = T^-1 r0, gamma0 = r0.z0
-  double acc = 0.0;
+  // z0 = T^-1 r0, gamma0 = r0.z0.  Per-thread partial sums (a few hundred
+  // terms) are FP32 -- GB300's FP64 pipe is narrow -- and widened to FP64
+  // for the block and grid sums.
+  float acc = 0.f;
   for (long long c = col0; c < ncol; c += colstride) acc += line_pass<false>(k, c, 0.f);
   {
-    const double v = block_sum(acc, sh);
+    const double v = block_sum((double)acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
   }
   if (!grid_sync(sol, nb)) return;
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     const float* po = cur ? k.p[1] : k.p[0];
     float* pn = cur ? k.p[0] : k.p[1];
     // operator phase
-    acc = 0.0;
+    acc = 0.f;
     const float ap = pending ? alpha_prev : 0.f;
     if ((ny & 3) == 0) {
       for (long long g = tid; g < (n >> 2); g += nth) acc += op_quad(k, po, pn, beta, ap, g << 2);
@@ -469,7 +471,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     }
     pending = false;
     {
-      const double v = block_sum(acc, sh);
+      const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pa[blockIdx.x] = v;
     }
     if (!grid_sync(sol, nb)) return;
@@ -488,10 +490,10 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     }
     const float alpha = (float)(gamma / ps);
     // line phase: r -= alpha s, z = T^-1 r, r.z
-    acc = 0.0;
+    acc = 0.f;
     for (long long c = col0; c < ncol; c += colstride) acc += line_pass<true>(k, c, alpha);
     {
-      const double v = block_sum(acc, sh);
+      const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
