@@ -176,9 +176,13 @@ __global__ void __launch_bounds__(kThreads) kry_factor_kernel(Kry kr, SolverDev*
 }
 
 // FP64 anchor: r = b - A x, its L1 norm, the scaled right-hand side
-// Sigma W r of the inner system (FP32, line-major) and its squared 2-norm;
-// with it ||b||_1 and ||Sigma W b||_2^2.  The last block writes the four
-// totals to sol->true_l1, sol->scratch[0], sol->rhsnorm, sol->scratch[1].
+// Sigma W r of the inner system (FP32, line-major) and, with L2, its
+// squared 2-norm; with WITH_B also ||b||_1 and ||Sigma W b||_2^2 (b does not
+// change during a solve).  The last block writes the totals to
+// sol->true_l1, sol->scratch[0], sol->rhsnorm, sol->scratch[1].  The
+// residual is a chain of FP64 fused multiply-adds: GB300's FP64 pipe, not
+// HBM, bounds this kernel.
+template <bool L2, bool WITH_B>
 __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, const double* __restrict__ x,
                                                               const double* __restrict__ b, int hypre,
                                                               double* partials, int nbmax) {
@@ -197,16 +201,23 @@ __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, con
     const size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
     const double bb = b_of(d, b, t, i, j, k, hypre != 0);
     // a zero coupling contributes nothing, whatever the ghost it points at holds
-    const double ax = r.a * x[q] + (r.b != 0.0 ? r.b * x[q - 1] : 0.0) + (r.c != 0.0 ? r.c * x[q + 1] : 0.0) +
-                      (r.d != 0.0 ? r.d * x[qjm] : 0.0) + (r.e != 0.0 ? r.e * x[qjp] : 0.0) +
-                      (r.f != 0.0 ? r.f * x[q - sk] : 0.0) + (r.g != 0.0 ? r.g * x[q + sk] : 0.0);
+    double ax = r.a * x[q];
+    ax = fma(r.b, r.b != 0.0 ? x[q - 1] : 0.0, ax);
+    ax = fma(r.c, r.c != 0.0 ? x[q + 1] : 0.0, ax);
+    ax = fma(r.d, r.d != 0.0 ? x[qjm] : 0.0, ax);
+    ax = fma(r.e, r.e != 0.0 ? x[qjp] : 0.0, ax);
+    ax = fma(r.f, r.f != 0.0 ? x[q - sk] : 0.0, ax);
+    ax = fma(r.g, r.g != 0.0 ? x[q + sk] : 0.0, ax);
     const double rr = bb - ax;
     const double sw = kr.sig[t] * kr.wgt[t];
-    const double rs = sw * rr, bs = sw * bb;
+    const double rs = sw * rr;
     s[0] += fabs(rr);
-    s[1] += rs * rs;
-    s[2] += fabs(bb);
-    s[3] += bs * bs;
+    if (L2) s[1] = fma(rs, rs, s[1]);
+    if (WITH_B) {
+      const double bs = sw * bb;
+      s[2] += fabs(bb);
+      s[3] = fma(bs, bs, s[3]);
+    }
     const size_t l = lq(kr, i, j, k);
     kr.r[l] = (float)rs;
     kr.e[l] = 0.f;
@@ -226,9 +237,11 @@ __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, con
     for (int m = 0; m < 4; ++m) tot[m] = block_sum_array(partials + m * nbmax, gridDim.x, sh);
     if (threadIdx.x == 0) {
       d.sol->true_l1 = tot[0];
-      d.sol->scratch[0] = tot[1];
-      d.sol->rhsnorm = tot[2];
-      d.sol->scratch[1] = tot[3];
+      if (L2) d.sol->scratch[0] = tot[1];
+      if (WITH_B) {
+        d.sol->rhsnorm = tot[2];
+        d.sol->scratch[1] = tot[3];
+      }
       d.sol->ticket2 = 0;
     }
   }
@@ -611,9 +624,13 @@ int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int* it
   return 0;
 }
 
-int anchor(ttfld_ctx* c, KryWork* w, const double* x, const double* b, bool hypre) {
+int anchor(ttfld_ctx* c, KryWork* w, const double* x, const double* b, bool hypre, bool l2, bool with_b) {
   const int nb = grid_cells(w->k.n);
-  kry_anchor_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, hypre ? 1 : 0, c->partials, 1024);
+  const int h = hypre ? 1 : 0;
+  if (l2 && with_b) kry_anchor_kernel<true, true><<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, h, c->partials, 1024);
+  else if (l2) kry_anchor_kernel<true, false><<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, h, c->partials, 1024);
+  else if (with_b) kry_anchor_kernel<false, true><<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, h, c->partials, 1024);
+  else kry_anchor_kernel<false, false><<<nb, kThreads, 0, c->stream>>>(c->d, w->k, x, b, h, c->partials, 1024);
   count_launches(1);
   TT_CHECK_LAUNCH();
   return poll_sol(c);
@@ -645,7 +662,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
   int rc = prepare(c, w, hypre);
   if (rc) return rc;
   if (fallback) *fallback = 0;
-  if ((rc = anchor(c, w, x, b, hypre))) return rc;
+  if ((rc = anchor(c, w, x, b, hypre, l2, true))) return rc;
   if (c->host_sol->bad_weights) {
     fprintf(stderr, "ttfld: PCG needs EVAL8 < 0 on every coupled row (the symmetrising weight)\n");
     return TTFLD_E_UNSUPPORTED;
@@ -661,13 +678,13 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
       zero_x = c->guess_tmp;
     }
     TT_CHECK(cudaMemsetAsync(zero_x, 0, nhalo(c->d) * 8, c->stream));
-    if ((rc = anchor(c, w, zero_x, b, hypre)) || (rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
+    if ((rc = anchor(c, w, zero_x, b, hypre, l2, false)) || (rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
     const double g_zero = c->host_sol->scratch[2];
     if (!(g_guess < g_zero)) {
       TT_CHECK(cudaMemsetAsync(x, 0, nhalo(c->d) * 8, c->stream));
       if (fallback) *fallback = 1;
       // the anchor of the zero iterate is current
-    } else if ((rc = anchor(c, w, x, b, hypre))) {
+    } else if ((rc = anchor(c, w, x, b, hypre, l2, false))) {
       return rc;
     }
   }
@@ -695,7 +712,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     kry_update_kernel<<<grid_cells(w->k.n), kThreads, 0, c->stream>>>(c->d, w->k, x);
     count_launches(1);
     TT_CHECK_LAUNCH();
-    if ((rc = anchor(c, w, x, b, hypre))) return rc;
+    if ((rc = anchor(c, w, x, b, hypre, l2, false))) return rc;
   }
   // SOLVE_WITH_SOR leaves the phi halo of DELTA_ER refreshed (PLANETSHIFT(8)
   // after the last colour); SOLVE_WITH_HYPRE writes the interior only and its
