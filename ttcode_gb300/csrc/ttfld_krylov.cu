@@ -50,7 +50,7 @@ namespace {
 
 constexpr int kPcgThreads = 256;   // one block per SM; 248 registers for the batched passes
 constexpr int kPcgStall = 25;      // iterations without a new minimum of r.z end an inner run
-constexpr double kInnerReduce = 1e-5;  // relative reduction of sqrt(r.z) asked of one inner run
+constexpr double kInnerReduce = 1e-4;  // relative reduction of sqrt(r.z) asked of one inner run
 
 struct Kry {
   int nx, ny, nz;
