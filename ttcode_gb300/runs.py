@@ -15,6 +15,9 @@ with its solver and initial guess:
     mixed_learned   ... the run's first solve from the learned guess (with the
                     first-sweep fallback to zero), later ones from the
                     previous solution
+    pcg_zero        FP32 conjugate gradients (radial line preconditioner) in
+                    FP64 defect correction, zero guess
+    pcg_previous    ... each step's first solve from the previous solution
 
 One JSON line per variant: mean and total device time per step (CUDA events
 inside the library), outer iterations, solves, sweeps and fallbacks per step,
@@ -44,6 +47,8 @@ VARIANTS = {
     "mixed_zero": dict(solver="mixed", guess="zero"),
     "mixed_previous": dict(solver="mixed", guess="previous"),
     "mixed_learned": dict(solver="mixed", guess="learned"),
+    "pcg_zero": dict(solver="pcg", guess="zero"),
+    "pcg_previous": dict(solver="pcg", guess="previous"),
 }
 
 
