@@ -409,6 +409,10 @@ def run_gpu(args):
                    "tol": 1e-10, "omega": sh.params["sorparam"],
                    "l2": "flushed between timed solves (256 MB write)", "parallelism": "replicas"},
         "sweeps_per_solve": stats[-1].sor_iter, "corrections_per_solve": stats[-1].corrections,
+        # cell updates per second of the product path (sweeps x cells / solve time) and of one
+        # FP32 sweep on its own
+        "cell_updates_per_s": float(np.mean([s.sor_iter for s in stats])) * ncells / (ms_per_solve * 1e-3),
+        "cell_updates_per_s_sweep": ncells / (ms_sweep32 * 1e-3),
         "fallbacks": int(sum(s.fallback for s in stats)), "guess_ms": stats[-1].guess_ms,
         "guess_training": train_info, "zero_guess_mixed": zero_guess, "pcg": pcg,
         "true_rel_residual": r_l1 / b_l1,
