@@ -1,0 +1,366 @@
+"""ttcode's restart records (AKTTD / SNAP.xxx) read into, and written from,
+the arrays this library works on.
+
+PRINTOUT(1) (ppprt.f:13-124) writes, on unit 12, one Fortran unformatted
+sequential file per rank; each WRITE is one record framed by its byte
+length (a 4-byte marker before and after; records longer than 2**31-1
+bytes are split into sub-records whose leading marker is negative, as
+gfortran writes them).  The records, in order:
+
+     1  global_NX, global_NY, global_NZ                      INTEGER
+     2  locNX, locNY, locNZ, numprocs                        INTEGER
+     3  myid, proc_coords(1:3)                               INTEGER
+     4  proc_dims(1:3)                                       INTEGER
+     5  ZEIT, DELT (DOUBLE PRECISION), NUM_ITER (INTEGER)
+  6-14  XXA(0:NX+2) XXB(-1:NX+2) DXA(1:NX+2), the same for Y and Z
+ 15-17  V(0:NX+2,-1:NY+2,-1:NZ+2), G(-1:NX+2,0:NY+2,-1:NZ+2),
+        H(-1:NX+2,-1:NY+2,0:NZ+2)
+ 18-21  RH, T, ER, PG on (-1:NX+2,-1:NY+2,-1:NZ+2)
+    22  CS(0:NX+1,0:NY+1,0:NZ+1)
+    23  UPPERBND(1:NY,1:NZ)                                  INTEGER
+    24  TinitBottom, Tinittop, rhinittop, rhinitbottom, hydrotime, Maccreated
+    25  NCOSYS                                               INTEGER
+ 26-34  on (1:NX,1:NY,1:NZ): xkapR, flimx(1:NX,...), conv_flux(1), conv_flux(2),
+        conv_flux(3), xkapA, STELLARINPUT, disfn, xkapP
+
+(records 25-34 are "not read back into a restart", ppprt.f:44).  Arrays are
+column-major, first index fastest.  `read` returns a `Snapshot`; `stitch`
+joins the files of a (phi, theta) decomposition by proc_coords; `grid_of`
+rebuilds GITTER's NCOSYS=2 metrics (ppinit.f:1028-1406) from the coordinate
+records; `shell_of` makes the state a `synthetic.Shell` that
+`fld.start_run` accepts, so that a ttcode state drives the solver.
+"""
+from __future__ import annotations
+
+import math
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .grid import BOUNDS, AXIS, Grid
+
+COORDS = ("xxa", "xxb", "dxa", "xya", "xyb", "dya", "xza", "xzb", "dza")
+COORD_LO = {"xxa": 0, "xxb": -1, "dxa": 1, "xya": 0, "xyb": -1, "dya": 1, "xza": 0, "xzb": -1, "dza": 1}
+FIELDS3 = ("V", "G", "H", "RH", "T", "ER", "PG", "CS")
+EXTRAS = ("xkapR", "flimx", "conv_flux1", "conv_flux2", "conv_flux3", "xkapA", "STELLARINPUT", "disfn",
+          "xkapP")
+SCALARS = ("TinitBottom", "Tinittop", "rhinittop", "rhinitbottom", "hydrotime", "Maccreated")
+
+
+def field_bounds(name: str, nx: int, ny: int, nz: int):
+    """((lo_i, hi_i), (lo_j, hi_j), (lo_k, hi_k)) of a 3-D record."""
+    h = lambda n: (-1, n + 2)
+    if name == "V":
+        return (0, nx + 2), h(ny), h(nz)
+    if name == "G":
+        return h(nx), (0, ny + 2), h(nz)
+    if name == "H":
+        return h(nx), h(ny), (0, nz + 2)
+    if name == "CS":
+        return (0, nx + 1), (0, ny + 1), (0, nz + 1)
+    if name in EXTRAS:
+        return (1, nx), (1, ny), (1, nz)
+    return h(nx), h(ny), h(nz)
+
+
+def _shape(b):
+    return tuple(hi - lo + 1 for lo, hi in b)
+
+
+@dataclass
+class Snapshot:
+    nx: int
+    ny: int
+    nz: int
+    global_dims: tuple
+    numprocs: int
+    myid: int
+    proc_coords: tuple
+    proc_dims: tuple
+    zeit: float
+    delt: float
+    num_iter: int
+    coords: dict = field(default_factory=dict)   # name -> 1-D array from its lower bound
+    arrays: dict = field(default_factory=dict)   # V G H RH T ER PG CS, extras; Fortran order
+    upperbnd: np.ndarray | None = None           # (1:NY, 1:NZ) int32
+    scalars: dict = field(default_factory=dict)
+    ncosys: int | None = None
+
+
+class _Records:
+    def __init__(self, data: bytes, endian: str):
+        self.b = data
+        self.p = 0
+        self.e = endian
+
+    def next(self) -> bytes:
+        out = bytearray()
+        while True:
+            if self.p + 4 > len(self.b):
+                raise EOFError("truncated record marker")
+            (n,) = struct.unpack_from(self.e + "i", self.b, self.p)
+            more = n < 0
+            n = abs(n)
+            start = self.p + 4
+            if start + n + 4 > len(self.b):
+                raise EOFError("truncated record")
+            out += self.b[start:start + n]
+            (m,) = struct.unpack_from(self.e + "i", self.b, start + n)
+            if abs(m) != n:
+                raise ValueError(f"record markers disagree at byte {self.p}: {n} vs {m}")
+            self.p = start + n + 4
+            if not more:
+                return bytes(out)
+
+    def done(self) -> bool:
+        return self.p >= len(self.b)
+
+
+def _ints(rec: bytes, n: int, e: str):
+    if len(rec) != 4 * n:
+        raise ValueError(f"expected {n} INTEGERs, record has {len(rec)} bytes")
+    return struct.unpack(e + f"{n}i", rec)
+
+
+def _doubles(rec: bytes, shape, e: str) -> np.ndarray:
+    n = int(np.prod(shape))
+    if len(rec) != 8 * n:
+        raise ValueError(f"expected {n} DOUBLE PRECISION values, record has {len(rec)} bytes")
+    return np.frombuffer(rec, dtype=np.dtype(e + "f8")).astype(np.float64).reshape(shape, order="F")
+
+
+def read(path: str, endian: str = "<") -> Snapshot:
+    """One rank's AKTTD / SNAP.xxx file."""
+    with open(path, "rb") as f:
+        r = _Records(f.read(), endian)
+    e = endian
+    gx, gy, gz = _ints(r.next(), 3, e)
+    nx, ny, nz, nprocs = _ints(r.next(), 4, e)
+    rec = _ints(r.next(), 4, e)
+    myid, pc = rec[0], tuple(rec[1:])
+    pd = tuple(_ints(r.next(), 3, e))
+    rec = r.next()
+    if len(rec) != 20:
+        raise ValueError("ZEIT, DELT, NUM_ITER record is not 8+8+4 bytes")
+    zeit, delt = struct.unpack_from(e + "2d", rec, 0)
+    (num_iter,) = struct.unpack_from(e + "i", rec, 16)
+    s = Snapshot(nx, ny, nz, (gx, gy, gz), nprocs, myid, pc, pd, zeit, delt, num_iter)
+    n_of = {"x": nx, "y": ny, "z": nz}
+    for name in COORDS:
+        n = n_of[name[1]]
+        s.coords[name] = _doubles(r.next(), (n + 2 - COORD_LO[name] + 1,), e)
+    for name in FIELDS3:
+        s.arrays[name] = _doubles(r.next(), _shape(field_bounds(name, nx, ny, nz)), e)
+    rec = r.next()
+    if len(rec) != 4 * ny * nz:
+        raise ValueError("UPPERBND record size")
+    s.upperbnd = np.frombuffer(rec, dtype=np.dtype(e + "i4")).astype(np.int32).reshape((ny, nz), order="F")
+    rec = r.next()
+    vals = struct.unpack(e + "6d", rec)
+    s.scalars = dict(zip(SCALARS, vals))
+    if r.done():
+        return s
+    (s.ncosys,) = _ints(r.next(), 1, e)
+    for name in EXTRAS:
+        if r.done():
+            break
+        s.arrays[name] = _doubles(r.next(), (nx, ny, nz), e)
+    return s
+
+
+def _record(payload: bytes, endian: str, max_sub: int = 2**31 - 1) -> bytes:
+    out = bytearray()
+    chunks = [payload[i:i + max_sub] for i in range(0, len(payload), max_sub)] or [b""]
+    for q, c in enumerate(chunks):
+        m = -len(c) if q + 1 < len(chunks) else len(c)   # negative: another sub-record follows
+        out += struct.pack(endian + "i", m) + c + struct.pack(endian + "i", m)
+    return bytes(out)
+
+
+def write(path: str, s: Snapshot, endian: str = "<", max_sub: int = 2**31 - 1):
+    """The same record sequence (restart files made from this library's
+    state, and the round-trip tests)."""
+    e = endian
+    F = lambda a: np.asarray(a, dtype=np.float64).astype(np.dtype(e + "f8")).tobytes(order="F")
+    recs = [struct.pack(e + "3i", *s.global_dims), struct.pack(e + "4i", s.nx, s.ny, s.nz, s.numprocs),
+            struct.pack(e + "4i", s.myid, *s.proc_coords), struct.pack(e + "3i", *s.proc_dims),
+            struct.pack(e + "2di", s.zeit, s.delt, s.num_iter)]
+    recs += [F(s.coords[n]) for n in COORDS]
+    recs += [F(s.arrays[n]) for n in FIELDS3]
+    recs.append(np.asarray(s.upperbnd, dtype=np.dtype(e + "i4")).tobytes(order="F"))
+    recs.append(struct.pack(e + "6d", *[s.scalars.get(n, 0.0) for n in SCALARS]))
+    if s.ncosys is not None:
+        recs.append(struct.pack(e + "i", s.ncosys))
+        # the records are positional: the ones before the last present are
+        # written as zeros when absent
+        last = max((q for q, n in enumerate(EXTRAS) if n in s.arrays), default=-1)
+        recs += [F(s.arrays[n]) if n in s.arrays else F(np.zeros((s.nx, s.ny, s.nz))) for n in EXTRAS[:last + 1]]
+    with open(path, "wb") as f:
+        for r in recs:
+            f.write(_record(r, e, max_sub))
+
+
+def stitch(parts: list[Snapshot]) -> Snapshot:
+    """One snapshot from the per-rank files of a decomposition in phi and
+    theta (proc_coords(2), proc_coords(3)); the radial direction must not be
+    split.  Ghost layers come from the rank that owns them."""
+    if not parts:
+        raise ValueError("no files")
+    p0 = parts[0]
+    if any(p.proc_dims[0] != 1 for p in parts):
+        raise ValueError("a radial decomposition cannot be stitched")
+    py, pz = p0.proc_dims[1], p0.proc_dims[2]
+    if len(parts) != py * pz:
+        raise ValueError(f"{len(parts)} files for a {py} x {pz} decomposition")
+    by = {(p.proc_coords[1], p.proc_coords[2]): p for p in parts}
+    nx, ny, nz = p0.nx, p0.ny * py, p0.nz * pz
+    out = Snapshot(nx, ny, nz, p0.global_dims, 1, 0, (0, 0, 0), (1, 1, 1), p0.zeit, p0.delt, p0.num_iter)
+    out.scalars = dict(p0.scalars)
+    out.ncosys = p0.ncosys
+    out.coords["xxa"], out.coords["xxb"], out.coords["dxa"] = (p0.coords[n] for n in ("xxa", "xxb", "dxa"))
+    for ax, (names, nloc, idx) in {"y": (("xya", "xyb", "dya"), p0.ny, 1), "z": (("xza", "xzb", "dza"), p0.nz, 2)}.items():
+        nb = py if ax == "y" else pz
+        for name in names:
+            lo = COORD_LO[name]
+            full = np.zeros((ny if ax == "y" else nz) + 2 - lo + 1)
+            for b in range(nb):
+                p = by[(b, 0)] if ax == "y" else by[(0, b)]
+                a = p.coords[name]
+                # local index l (lo..nloc+2) -> global b*nloc + l
+                for l in range(lo, nloc + 3):
+                    g = b * nloc + l
+                    if (l >= 1 and l <= nloc) or (b == 0 and l < 1) or (b == nb - 1 and l > nloc):
+                        full[g - lo] = a[l - lo]
+            out.coords[name] = full
+    for name in list(p0.arrays):
+        (li, hi), (lj, hj), (lk, hk) = field_bounds(name, p0.nx, p0.ny, p0.nz)
+        gb = field_bounds(name, nx, ny, nz)
+        full = np.zeros(_shape(gb), order="F")
+        for (cy, cz), p in by.items():
+            a = p.arrays[name]
+            for l in range(lj, hj + 1):
+                if not ((1 <= l <= p0.ny) or (cy == 0 and l < 1) or (cy == py - 1 and l > p0.ny)):
+                    continue
+                gj = cy * p0.ny + l
+                for m in range(lk, hk + 1):
+                    if not ((1 <= m <= p0.nz) or (cz == 0 and m < 1) or (cz == pz - 1 and m > p0.nz)):
+                        continue
+                    gk = cz * p0.nz + m
+                    full[:, gj - gb[1][0], gk - gb[2][0]] = a[:, l - lj, m - lk]
+        out.arrays[name] = full
+    ub = np.zeros((ny, nz), dtype=np.int32, order="F")
+    for (cy, cz), p in by.items():
+        ub[cy * p0.ny:(cy + 1) * p0.ny, cz * p0.nz:(cz + 1) * p0.nz] = p.upperbnd
+    out.upperbnd = ub
+    return out
+
+
+def grid_of(s: Snapshot, dxmin: float = 0.0, dymin: float = 0.0, dzmin: float = 0.0) -> Grid:
+    """GITTER's NCOSYS=2 metrics (ppinit.f:1180-1406) from the coordinate
+    records.  DXMIN = 0 (linear grids) sets DDX0 = DDX1 = 1/2
+    (ppinit.f:1198-1202); otherwise they are formed from XXA, XXB, DXB."""
+    if s.ncosys not in (None, 2):
+        raise ValueError(f"NCOSYS={s.ncosys}: only the spherical grid (2) is implemented")
+    nx, ny, nz = s.nx, s.ny, s.nz
+    c = s.coords
+    full = {}
+
+    def on_halo(name, n):   # -> array over -1..n+2 (index +1)
+        a = np.zeros(n + 4)
+        lo = COORD_LO[name]
+        a[lo + 1:lo + 1 + c[name].size] = c[name]
+        return a
+
+    n_of = {"x": nx, "y": ny, "z": nz}
+    for ax, (a_, b_, da_, db_) in {"x": ("xxa", "xxb", "dxa", "dxb"), "y": ("xya", "xyb", "dya", "dyb"),
+                                   "z": ("xza", "xzb", "dza", "dzb")}.items():
+        n = n_of[ax]
+        full[a_], full[b_], full[da_] = on_halo(a_, n), on_halo(b_, n), on_halo(da_, n)
+        db = np.zeros(n + 4)
+        for i in range(0, n + 3):
+            db[i + 1] = full[b_][i + 1] - full[b_][i]
+        full[db_] = db
+        dmin = {"x": dxmin, "y": dymin, "z": dzmin}[ax]
+        d0, d1 = np.zeros(n + 4), np.zeros(n + 4)
+        for i in range(0, n + 3):
+            if dmin == 0.0:
+                d0[i + 1] = d1[i + 1] = 0.5
+            else:
+                d0[i + 1] = (full[b_][i + 1] - full[a_][i + 1]) / db[i + 1]
+                d1[i + 1] = (full[a_][i + 1] - full[b_][i]) / db[i + 1]
+        full["dd" + ax + "0"], full["dd" + ax + "1"] = d0, d1
+    xa, xb, za, zb = full["xxa"], full["xxb"], full["xza"], full["xzb"]
+    xxa1 = xa[2] if xa[2] != 0.0 else float(np.float32(1.e-20))
+    full["surxa"] = xa * xa
+    full["surxb"] = xb * xb
+    full["geoxga"] = xa.copy()
+    full["geoxha"] = xa.copy()
+    full["geoxga"][2] = xxa1
+    full["geoxha"][2] = xxa1
+    full["geoxg"] = xb.copy()
+    full["geoxh"] = xb.copy()
+    full["surza"] = np.array([math.cos(v) for v in za])
+    full["surzb"] = np.array([math.cos(v) for v in zb])
+    full["geozga"] = np.array([math.cos(v) for v in za])
+    full["geozg"] = np.array([math.cos(v) for v in zb])
+    if full["geozga"][nz + 2] == 0.0:
+        full["geozga"][nz + 2] = float(np.float32(1.e-10))
+    if full["geozga"][2] == 0.0:
+        full["geozga"][2] = float(np.float32(1.e-10))
+    g = Grid(nx, ny, nz, float(xa[2]), float(xa[nx + 2]), float(c["xya"][1] / (2 * math.pi)),
+             float(c["xya"][ny + 1] / (2 * math.pi)), float(c["xza"][1] / (math.pi / 2)),
+             float(c["xza"][nz + 1] / (math.pi / 2)))
+    for name, (lo, hioff) in BOUNDS.items():
+        n = n_of[AXIS[name]]
+        g.m[name] = np.ascontiguousarray(full[name][lo + 1:n + hioff + 2])
+        g.lo[name] = lo
+    return g
+
+
+def shell_of(s: Snapshot, params: dict | None = None, dxmin: float = 0.0):
+    """The snapshot as a `synthetic.Shell`: grid from the coordinates, T, RH
+    and ER as written, c_v of GASINIT (ppinit.f:1408-1417) for the params'
+    gamma and mu, the stellar geometry of the grid.  With the snapshot's
+    xkapR/xkapA/xkapP records the opacities are prescribed there
+    (kappa_model 1 uploads them; they hold the interior only, so the halo
+    takes the nearest interior value); otherwise the analytic model runs."""
+    from . import synthetic as S
+    g = grid_of(s, dxmin)
+    p = dict(S.default_params(s.delt))
+    if params:
+        p.update(params)
+    shape = (s.nx + 4, s.ny + 4, s.nz + 4)
+    gamma, mu = p.pop("gamma", 1.4), p.pop("mu", 2.3)
+    fields = {"T": np.asfortranarray(s.arrays["T"]), "RH": np.asfortranarray(s.arrays["RH"]),
+              "ER": np.asfortranarray(s.arrays["ER"]),
+              "CV": np.full(shape, S.RGAS / (mu * (gamma - 1.0)), order="F"),
+              "KMUL": np.ones(shape, order="F")}
+    mu_s, tinc = S.mu_star_tincident(g, p["tirr"], p["f_incident"])
+    fields["MU_STAR"], fields["TINCIDENT"] = mu_s, tinc
+    if all(n in s.arrays for n in ("xkapR", "xkapA", "xkapP")) and p.get("kappa_model", 0) == 1:
+        for src, dst in (("xkapR", "XKAPR"), ("xkapA", "XKAPA"), ("xkapP", "XKAPP")):
+            fields[dst] = np.asfortranarray(np.pad(s.arrays[src], 2, mode="edge"))
+    return S.Shell(g, fields, p, seed=-1)
+
+
+def snapshot_of(sh, zeit: float = 0.0, num_iter: int = 0, upperbnd=None) -> Snapshot:
+    """A one-rank snapshot of a `synthetic.Shell` (or of any state with the
+    same fields): the arrays PRINTOUT writes that this library holds, zero
+    velocities, pressure and sound speed."""
+    g = sh.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    s = Snapshot(nx, ny, nz, (nx, ny, nz), 1, 0, (0, 0, 0), (1, 1, 1), zeit, sh.params["delt"], num_iter)
+    for name in COORDS:
+        lo = COORD_LO[name]
+        n = {"x": nx, "y": ny, "z": nz}[name[1]]
+        s.coords[name] = np.array([g.at(name, i) for i in range(lo, n + 3)])
+    for name in FIELDS3:
+        src = {"RH": "RH", "T": "T", "ER": "ER"}.get(name)
+        shp = _shape(field_bounds(name, nx, ny, nz))
+        s.arrays[name] = np.asfortranarray(sh.fields[src]) if src else np.zeros(shp, order="F")
+    s.upperbnd = (np.full((ny, nz), nx - 1, dtype=np.int32) if upperbnd is None
+                  else np.asarray(upperbnd, dtype=np.int32))
+    s.scalars = {n: 0.0 for n in SCALARS}
+    s.ncosys = 2
+    return s
