@@ -264,6 +264,27 @@ int ttfld_solve_system(ttfld_ctx* ctx, ttfld_solve_stats* stats);
  * replaced by an exact radial line solve.  stats may be NULL. */
 int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
                            ttfld_solve_stats* stats);
+/* The IRAD=1 radiation step, RADDIF (pprad.f:1-38): ER = arad T^4, DIFFEL
+ * (DIFF's face coefficients into AX..CZ, pprad.f:40-72), B and RHS
+ * (pprad.f:21-29), SOLVMAT (ppmat.f:1-186: red-black SOR on ER, stop at
+ * ||XS||_2/||RHS||_2 <= EPSMAT after at least 5 iterations, or ITMAX, then
+ * status 1) with RADIATIVEBOUND (ppbou.f:2049-2299) after each colour, and
+ * T = (ER/arad)^(1/4).  RADIATIVEBOUND is implemented for IBDRAD 3, 4, 7, 8,
+ * 9 with MODVER <= 5 (other values: status -3). */
+typedef struct {
+  double d_t;           /* D_T, the bottom temperature gradient of the model
+                           (ppinit.f:121-171)                               */
+  double tinit_bottom;  /* TinitBottom (the bottom T when BCXMIN = 6)      */
+  int32_t modver;       /* MODVER                                           */
+  int32_t energy_iter;  /* energy_iter as DIFF/FLIM read it (<= 1: KAPPA,
+                           SUBSIG and QDENS are evaluated first)            */
+  const double* volxb;  /* VOLXB(1:NX), VOLYB(1:NY), VOLZB(1:NZ) of GITTER
+                           (ppinit.f:1342-1376), host memory               */
+  const double* volyb;
+  const double* volzb;
+} ttfld_raddif_params;
+int ttfld_raddif(ttfld_ctx* ctx, const ttfld_raddif_params* params,
+                 ttfld_solve_stats* stats);
 /* Exactly n red-black sweeps on the current system from the current
  * DELTA_ER, FP64, reference rounding (for sweep-by-sweep parity tests). */
 int ttfld_sor_sweeps(ttfld_ctx* ctx, int n, double* rnorm, double* rhsnorm);

@@ -24,7 +24,8 @@ CELL = ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8",
         "EVAL_1_6", "JACOB_ETA", "FQ", "FR", "RHS_ER", "SOR_A", "SOR_B", "SOR_C",
         "SOR_D", "SOR_E", "SOR_F", "SOR_G", "DIVF", "DIVF_OLD", "DFQ_DQ", "DFR_DQ",
         "DELTA_Q", "RHS_DIF", "HYP_A", "HYP_B", "HYP_C", "HYP_D", "HYP_E", "HYP_F",
-        "HYP_G", "HYP_RHS")
+        "HYP_G", "HYP_RHS", "RAD_AX", "RAD_CX", "RAD_AY", "RAD_CY", "RAD_AZ", "RAD_CZ", "RAD_B",
+        "RAD_RHS")
 FACE = ("FLIMX", "FLIMY", "FLIMZ", "DIFRX", "DIFRY", "DIFRZ", "FLUX_X", "FLUX_Y", "FLUX_Z")
 PLANE = ("MU_STAR", "TINCIDENT")
 
@@ -65,6 +66,7 @@ def _load():
         lib.ttor_solve_with_sor.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         lib.ttor_sor_sweeps.argtypes = [vp, ctypes.c_int]
         lib.ttor_coupled_energy_eqs.argtypes = [vp, ctypes.c_int]
+        lib.ttor_raddif.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         lib.ttor_true_residual_l1.restype = ctypes.c_double
         lib.ttor_true_residual_l1.argtypes = [vp]
         _lib = lib

@@ -40,7 +40,7 @@ struct ttor_state {
   double *xxa, *xxb, *dxa, *dxb, *xya, *xyb, *dya, *dyb, *xza, *xzb, *dza, *dzb;
   double *ddx0, *ddx1, *ddy0, *ddy1, *ddz0, *ddz1;
   double *surxa, *surxb, *surza, *surzb, *geoxg, *geoxh, *geoxga, *geoxha,
-      *geozg, *geozga, *volxb, *volzb;
+      *geozg, *geozga, *volxb, *volyb, *volzb;
   double xmin, xmax, ymin, ymax, zmin, zmax;
   /* halo fields */
   double *T, *RH, *CV, *ER, *ER_OLD, *Q, *Q_OLD, *DELTA_ER, *XKAPR, *XKAPP,
@@ -53,6 +53,8 @@ struct ttor_state {
       *DELTA_Q, *RHS_DIF;
   /* the IRAD=2 system of FILLHYPREMATRIX / FILLHYPREVECTORS */
   double *HYP_A, *HYP_B, *HYP_C, *HYP_D, *HYP_E, *HYP_F, *HYP_G, *HYP_RHS;
+  /* the IRAD=1 system of RADDIF / DIFFEL (rad_var_init AX..CZ, B, RHS) */
+  double *RAD_AX, *RAD_CX, *RAD_AY, *RAD_CY, *RAD_AZ, *RAD_CZ, *RAD_B, *RAD_RHS;
   /* face fields */
   double *FLIMX, *FLIMY, *FLIMZ, *DIFRX, *DIFRY, *DIFRZ, *FLUX_X, *FLUX_Y,
       *FLUX_Z;
@@ -109,6 +111,9 @@ static const fdesc FIELDS[] = {
     FD_ENTRY(HYP_A, K_CELL), FD_ENTRY(HYP_B, K_CELL), FD_ENTRY(HYP_C, K_CELL),
     FD_ENTRY(HYP_D, K_CELL), FD_ENTRY(HYP_E, K_CELL), FD_ENTRY(HYP_F, K_CELL),
     FD_ENTRY(HYP_G, K_CELL), FD_ENTRY(HYP_RHS, K_CELL),
+    FD_ENTRY(RAD_AX, K_CELL), FD_ENTRY(RAD_CX, K_CELL), FD_ENTRY(RAD_AY, K_CELL),
+    FD_ENTRY(RAD_CY, K_CELL), FD_ENTRY(RAD_AZ, K_CELL), FD_ENTRY(RAD_CZ, K_CELL),
+    FD_ENTRY(RAD_B, K_CELL), FD_ENTRY(RAD_RHS, K_CELL),
     FD_ENTRY(FLIMX, K_FACE), FD_ENTRY(FLIMY, K_FACE), FD_ENTRY(FLIMZ, K_FACE),
     FD_ENTRY(DIFRX, K_FACE), FD_ENTRY(DIFRY, K_FACE), FD_ENTRY(DIFRZ, K_FACE),
     FD_ENTRY(FLUX_X, K_FACE), FD_ENTRY(FLUX_Y, K_FACE), FD_ENTRY(FLUX_Z, K_FACE),
@@ -120,7 +125,7 @@ static const fdesc FIELDS[] = {
     FD_ENTRY(ddz0, K_1D), FD_ENTRY(ddz1, K_1D), FD_ENTRY(surxa, K_1D), FD_ENTRY(surxb, K_1D),
     FD_ENTRY(surza, K_1D), FD_ENTRY(surzb, K_1D), FD_ENTRY(geoxg, K_1D), FD_ENTRY(geoxh, K_1D),
     FD_ENTRY(geoxga, K_1D), FD_ENTRY(geoxha, K_1D), FD_ENTRY(geozg, K_1D),
-    FD_ENTRY(geozga, K_1D), FD_ENTRY(volxb, K_1D), FD_ENTRY(volzb, K_1D),
+    FD_ENTRY(geozga, K_1D), FD_ENTRY(volxb, K_1D), FD_ENTRY(volyb, K_1D), FD_ENTRY(volzb, K_1D),
 };
 #define NFIELDS (sizeof(FIELDS) / sizeof(FIELDS[0]))
 
@@ -275,6 +280,7 @@ int ttor_gitter(ttor_state* s) {
   }
   G1(geoxga, 1) = xxa1; G1(geoxha, 1) = xxa1;
   for (int i = -1; i <= nx + 2; ++i) { G1(geoxg, i) = G1(xxb, i); G1(geoxh, i) = G1(xxb, i); }
+  for (int j = 0; j <= ny + 1; ++j) G1(volyb, j) = G1(xya, j + 1) - G1(xya, j);   /* :1364 */
   for (int k = 0; k <= nz + 1; ++k) G1(volzb, k) = sin(G1(xza, k + 1)) - sin(G1(xza, k));
   for (int k = 0; k <= nz + 2; ++k) {
     G1(surza, k) = cos(G1(xza, k));
@@ -1168,5 +1174,143 @@ int ttor_diffusion(ttor_state* s) {
         }
       }
   int rc = sor_loop(s, s->SCALAR, s->RHS_DIF, 5, 500);
+  return rc;
+}
+
+/* ---- IRAD=1: RADDIF pprad.f:1-38, DIFFEL :40-72, SOLVMAT ppmat.f:1-186,
+ * RADIATIVEBOUND ppbou.f:2049-2299 (RADBOUNDVER = IBDRAD in 3, 4, 7, 8, 9
+ * with MODVER <= 5; one rank, periodic phi, poles = .false.) ------------- */
+
+/* RADIATIVEBOUND: bottom T and ER (:2127-2139), top ER at i >= upperbnd
+ * (:2145-2236), theta ghost copies (:2256-2271), PLANETSHIFT(6) (:2280). */
+static int radiativebound(ttor_state* s, double d_t, double tinit_bottom, int modver) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  if (s->ibdrad < 3 || s->ibdrad > 9 || s->ibdrad == 5 || s->ibdrad == 6) return -3;
+  if (modver > 5) return -3;
+  for (int k = -1; k <= nz + 2; ++k)
+    for (int j = -1; j <= ny + 2; ++j) {
+      if (s->bcxmin == 6) H(T, 1, j, k) = tinit_bottom;
+      H(T, 0, j, k) = H(T, 1, j, k) - d_t * (G1(xxb, 1) - G1(xxb, 0));
+      H(T, -1, j, k) = H(T, 1, j, k) - d_t * (G1(xxb, 1) - G1(xxb, -1));
+      H(ER, 1, j, k) = ARAD_C * p4(H(T, 1, j, k));
+      H(ER, 0, j, k) = ARAD_C * p4(H(T, 0, j, k));
+      H(ER, -1, j, k) = ARAD_C * p4(H(T, -1, j, k));
+    }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j) {
+      const int ub = P(UPPERBND, j, k);
+      if (!(ub < nx + 1)) return -3;
+      double tj = 0.0;
+      switch (s->ibdrad) {
+        case 3:
+        case 8:
+          tj = s->tirr * pow(cos(G1(xyb, j)) * cos(G1(xzb, k)), 0.25);
+          tj = s->ibdrad == 3 ? (tj > 100.0 ? tj : 100.0) : (tj > 950.0 ? tj : 950.0);
+          break;
+        case 4: tj = s->tirr; break;
+        case 7: tj = H(T, ub - 1, j, k); break;
+        case 9:
+          if (s->iii <= 1) tj = H(T, ub - 1, j, k);
+          else
+            tj = pow(H(ER, ub, j, k) / ARAD_C +
+                         H(STELLARINPUT, ub - 1, j, k) /
+                             (4.0 * SBCONST_C * H(RH, ub - 1, j, k) * H(XKAPP, ub - 1, j, k)),
+                     0.25);
+          break;
+      }
+      for (int i = ub; i <= nx + 2; ++i) H(ER, i, j, k) = ARAD_C * p4(tj);
+    }
+  if (!s->poles) {
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) {
+        H(ER, i, j, -1) = H(ER, i, j, 1);
+        H(ER, i, j, 0) = H(ER, i, j, 1);
+      }
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) {
+        H(ER, i, j, nz + 1) = H(ER, i, j, nz);
+        H(ER, i, j, nz + 2) = H(ER, i, j, nz);
+      }
+  }
+  shift_halo(s, s->ER);
+  return 0;
+}
+
+/* One colour of SOLVMAT (ppmat.f:66-82 / 110-121); returns nothing, XS
+ * (the residual of each updated cell) goes to xs. */
+static void solvmat_colour(ttor_state* s, double* xs, int parity, double om) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j) {
+      const int imin = 2 - ((j + k + parity) % 2);
+      for (int i = imin; i <= nx; i += 2) {
+        const size_t c = (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+        const double x = s->RAD_B[c] * H(ER, i, j, k) - s->RAD_RHS[c] + s->RAD_AX[c] * H(ER, i - 1, j, k) +
+                         s->RAD_CX[c] * H(ER, i + 1, j, k) + s->RAD_AY[c] * H(ER, i, j - 1, k) +
+                         s->RAD_CY[c] * H(ER, i, j + 1, k) + s->RAD_AZ[c] * H(ER, i, j, k - 1) +
+                         s->RAD_CZ[c] * H(ER, i, j, k + 1);
+        xs[c] = x;
+        H(ER, i, j, k) = H(ER, i, j, k) - om * x / s->RAD_B[c];
+      }
+    }
+}
+
+int ttor_raddif(ttor_state* s, double d_t, double tinit_bottom, int modver, int energy_iter) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  if (s->poles || nz == 1) return -3;
+  /* ER = arad T^4 on the whole array (pprad.f:12) */
+  for (size_t q = 0; q < nhalo(s); ++q) s->ER[q] = ARAD_C * p4(s->T[q]);
+  /* DIFFEL (pprad.f:40-72): DIFF, then the couplings */
+  s->energy_iter = energy_iter;
+  int rc = ttor_diff(s);
+  if (rc) return rc;
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t c = (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+        s->RAD_AX[c] = -F(DIFRX, i, j, k) * G1(surxa, i) / G1(volxb, i);
+        s->RAD_CX[c] = -F(DIFRX, i + 1, j, k) * G1(surxa, i + 1) / G1(volxb, i);
+        s->RAD_AY[c] = -F(DIFRY, i, j, k) * 1.0 / G1(volyb, j) / G1(geoxg, i) / G1(geozg, k);
+        s->RAD_CY[c] = -F(DIFRY, i, j + 1, k) * 1.0 / G1(volyb, j) / G1(geoxg, i) / G1(geozg, k);
+        s->RAD_AZ[c] = -F(DIFRZ, i, j, k) * G1(surza, k) / G1(volzb, k) / G1(geoxh, i);
+        s->RAD_CZ[c] = -F(DIFRZ, i, j, k + 1) * G1(surza, k + 1) / G1(volzb, k) / G1(geoxh, i);
+        /* B and RHS, pprad.f:21-29 */
+        const double t = H(T, i, j, k);
+        const double w = 1.0 / s->delt * H(CV, i, j, k) * H(RH, i, j, k) / (4.0 * ARAD_C * t * t * t);
+        s->RAD_B[c] = w - s->RAD_AX[c] - s->RAD_CX[c] - s->RAD_AY[c] - s->RAD_CY[c] - s->RAD_AZ[c] -
+                      s->RAD_CZ[c];
+        s->RAD_RHS[c] = H(ER, i, j, k) / s->delt * H(CV, i, j, k) * H(RH, i, j, k) / (4.0 * ARAD_C * t * t * t);
+      }
+  /* SOLVMAT */
+  double rhsnorm = 0.0;
+  for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + s->RAD_RHS[c] * s->RAD_RHS[c];
+  rhsnorm = sqrt(rhsnorm);
+  s->global_rhsnorm = rhsnorm;
+  shift_halo(s, s->ER);
+  double* xs = (double*)calloc(ncell(s), sizeof(double));
+  if (!xs) return -2;
+  const double om = s->sorparam;
+  int it = 0;
+  for (;;) {
+    ++it;
+    solvmat_colour(s, xs, 0, om);
+    if ((rc = radiativebound(s, d_t, tinit_bottom, modver))) break;
+    shift_halo(s, s->ER);
+    solvmat_colour(s, xs, 1, om);
+    if ((rc = radiativebound(s, d_t, tinit_bottom, modver))) break;
+    shift_halo(s, s->ER);
+    double rnorm = 0.0;
+    for (size_t c = 0; c < ncell(s); ++c) rnorm = rnorm + xs[c] * xs[c];
+    rnorm = sqrt(rnorm);
+    s->global_rnorm = rnorm;
+    if (it == s->itmax) { rc = 1; break; }
+    if (rnorm / rhsnorm > s->epsmat || it < 5) continue;
+    break;
+  }
+  free(xs);
+  s->sor_iter = it;
+  if (rc < 0) return rc;
+  /* T = (ER/arad)**0.25 (pprad.f:35) */
+  for (size_t q = 0; q < nhalo(s); ++q) s->T[q] = pow(s->ER[q] / ARAD_C, 0.25);
   return rc;
 }

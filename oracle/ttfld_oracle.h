@@ -68,6 +68,13 @@ int ttor_b_vector_boundaries(ttor_state* s);
 /* FILLHYPREMATRIX + FILLHYPREVECTORS (pphypre.f:115-334) into HYP_A..HYP_G,
  * HYP_RHS from the EVAL arrays, RHS_ER and UPPERBND. */
 int ttor_fill_hypre_system(ttor_state* s);
+/* RADDIF (pprad.f:1-38, IRAD=1): ER = arad T^4, DIFFEL, SOLVMAT (ppmat.f,
+ * red-black SOR on ER with the L2 stop and ITMIN = 5) with RADIATIVEBOUND
+ * (ppbou.f:2049-2299; IBDRAD 3, 4, 7, 8, 9, MODVER <= 5) after each colour,
+ * T = (ER/arad)^(1/4).  d_t is the bottom temperature gradient D_T,
+ * tinit_bottom TinitBottom (read with BCXMIN = 6); returns 0, 1 at ITMAX,
+ * -3 for a configuration outside that set. */
+int ttor_raddif(ttor_state* s, double d_t, double tinit_bottom, int modver, int energy_iter);
 /* SOLVE_WITH_SOR.  use_guess=0 starts from zero (ppsor.f:29); use_guess=1
  * keeps the interior of DELTA_ER as the initial iterate (ghosts zeroed). */
 int ttor_solve_with_sor(ttor_state* s, int fill, int use_guess);

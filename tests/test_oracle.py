@@ -341,3 +341,67 @@ def test_weighted_rows_are_symmetric(shell):
         l, r = lhs[tuple(sl)], rhs[tuple(sl)]
         scale = np.max(np.abs(l))
         assert np.max(np.abs(l - r)) <= 1e-12 * scale, fwd
+
+
+def rad_oracle(sh, ibdrad, eps, itmax):
+    """An oracle state for RADDIF: the shell, GITTER's volumes, IBDRAD,
+    III = 2 and the stellar heating the IBDRAD = 9 top reads."""
+    from ttcode_gb300.grid import volumes
+    o = oracle_from_shell(sh, eps=eps, itmax=itmax)
+    nx, ny, nz = sh.dims
+    vx, vy, vz = volumes(sh.grid)
+    o.f("volxb")[2:nx + 2] = vx
+    o.f("volyb")[2:ny + 2] = vy
+    o.f("volzb")[2:nz + 2] = vz
+    o.set("ibdrad", ibdrad)
+    o.set("iii", 2)
+    assert o.call("stellarinput_heating") == 0
+    return o
+
+
+def test_volumes_match_oracle_gitter(shell):
+    """grid.volumes (the VOLXB/VOLYB/VOLZB the RADDIF caller passes) equal
+    the oracle's restatement of GITTER (ppinit.f:1346-1375)."""
+    from oracle import Oracle
+    from ttcode_gb300.grid import volumes
+    nx, ny, nz = shell.dims
+    o = Oracle(nx, ny, nz)
+    g = shell.grid
+    for k, v in (("xmin", g.xmin), ("xmax", g.xmax)):
+        o.set(k, v)
+    assert o.call("gitter") == 0
+    vx, vy, vz = volumes(g)
+    assert np.array_equal(o.f("volxb")[2:nx + 2], vx)
+    assert np.array_equal(o.f("volyb")[2:ny + 2], vy)
+    assert np.array_equal(o.f("volzb")[2:nz + 2], vz)
+
+
+def test_raddif_solves_its_system(shell):
+    """RADDIF with a fixed top (IBDRAD = 4) and ITMAX iterations: the
+    interior ER it leaves satisfies B ER + couplings = RHS up to the
+    residual norm SOLVMAT reports; DIFFEL's rows are diagonally dominant."""
+    o = rad_oracle(shell, 4, 1e-10, 400)
+    assert o.call("raddif", 0.0, 0.0, 1, 0) == 1          # ITMAX: the boundary rows keep a residual
+    assert int(o.get("sor_iter")) == 400
+    B = o.f("RAD_B")
+    off = sum(np.abs(o.f(n)) for n in ("RAD_AX", "RAD_CX", "RAD_AY", "RAD_CY", "RAD_AZ", "RAD_CZ"))
+    assert np.all(B > off)
+    T = o.f("T")
+    assert np.all(np.isfinite(T)) and np.all(T[2:-2, 2:-2, 2:-2] > 0)
+
+
+def test_raddif_converges_with_gradient_top(shell):
+    """IBDRAD = 7 (zero gradient at the top): SOLVMAT reaches EPSMAT = 1e-6
+    (the L2 rule, ppmat.f:152-178) and stops; ITMIN = 5 holds."""
+    o = rad_oracle(shell, 7, 1e-6, 3000)
+    assert o.call("raddif", 0.0, 0.0, 1, 0) == 0
+    assert 5 <= int(o.get("sor_iter")) < 3000
+    assert o.get("global_rnorm") / o.get("global_rhsnorm") <= 1e-6
+
+
+def test_raddif_rejects_unimplemented_boundaries(shell):
+    for ib in (1, 5, 6):
+        o = rad_oracle(shell, ib, 1e-6, 10)
+        assert o.call("raddif", 0.0, 0.0, 1, 0) == -3
+    o = rad_oracle(shell, 9, 1e-6, 10)
+    assert o.call("raddif", 0.0, 0.0, 6, 0) == -3       # MODVER > 5

@@ -57,6 +57,12 @@ class SolveStats(ctypes.Structure):
                 ("guess_ms", c_double)]
 
 
+class RaddifParams(ctypes.Structure):
+    _fields_ = [("d_t", ctypes.c_double), ("tinit_bottom", ctypes.c_double), ("modver", ctypes.c_int32),
+                ("energy_iter", ctypes.c_int32), ("volxb", ctypes.c_void_p), ("volyb", ctypes.c_void_p),
+                ("volzb", ctypes.c_void_p)]
+
+
 class Energy(ctypes.Structure):
     _fields_ = [(n, c_double) for n in ("volume", "e_rad", "e_gas", "heating", "flux_bottom", "flux_top",
                                         "flux_theta")]
@@ -103,7 +109,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
            "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums",
-           "ttfld_solve_with_hypre")
+           "ttfld_solve_with_hypre", "ttfld_raddif")
 
 _lib = None
 
@@ -151,6 +157,7 @@ def lib():
     L.ttfld_solve_with_sor.argtypes = [vp, ctypes.c_int, ctypes.POINTER(SolveStats)]
     L.ttfld_solve_system.argtypes = [vp, ctypes.POINTER(SolveStats)]
     L.ttfld_solve_with_hypre.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolveStats)]
+    L.ttfld_raddif.argtypes = [vp, ctypes.POINTER(RaddifParams), ctypes.POINTER(SolveStats)]
     L.ttfld_sor_sweeps.argtypes = [vp, ctypes.c_int, P_double, P_double]
     L.ttfld_true_residual.argtypes = [vp, P_double, P_double]
     L.ttfld_adjust_sor_param.argtypes = [vp, P_double]

@@ -158,6 +158,18 @@ class FLD:
         check("SOLVE_WITH_HYPRE", self.L.ttfld_solve_with_hypre(self.h, tol, maxit, ctypes.byref(st)), ok=(0, 1))
         return st
 
+    def raddif(self, d_t: float = 0.0, tinit_bottom: float = 0.0, modver: int = 1,
+               energy_iter: int = 0) -> _ffi.SolveStats:
+        """RADDIF (IRAD=1): ER from T, DIFFEL, SOLVMAT with RADIATIVEBOUND,
+        T from ER (ttfld_raddif)."""
+        from .grid import volumes
+        vx, vy, vz = (np.ascontiguousarray(v, dtype=np.float64) for v in volumes(self.grid))
+        p = _ffi.RaddifParams(d_t, tinit_bottom, modver, energy_iter, vx.ctypes.data, vy.ctypes.data,
+                              vz.ctypes.data)
+        st = _ffi.SolveStats()
+        check("RADDIF", self.L.ttfld_raddif(self.h, ctypes.byref(p), ctypes.byref(st)), ok=(0, 1))
+        return st
+
     def sor_sweeps(self, n: int):
         r, b = ctypes.c_double(), ctypes.c_double()
         check("sor_sweeps", self.L.ttfld_sor_sweeps(self.h, n, ctypes.byref(r), ctypes.byref(b)))

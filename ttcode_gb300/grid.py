@@ -123,6 +123,17 @@ def gitter(nx: int, ny: int, nz: int, xmin: float, xmax: float, ymin: float = 0.
     return g
 
 
+def volumes(g: Grid):
+    """VOLXB(1:NX), VOLYB(1:NY), VOLZB(1:NZ) of GITTER for NCOSYS=2
+    (ppinit.f:1346, 1364, 1375): (r_a(i+1)^3 - r_a(i)^3)/3, the phi width,
+    sin(theta_a(k+1)) - sin(theta_a(k))."""
+    xa = lambda i: float(g.at("xxa", i))
+    vx = np.array([(xa(i + 1) * xa(i + 1) * xa(i + 1) - xa(i) * xa(i) * xa(i)) / 3.0 for i in range(1, g.nx + 1)])
+    vy = np.array([float(g.at("xya", j + 1)) - float(g.at("xya", j)) for j in range(1, g.ny + 1)])
+    vz = np.array([math.sin(float(g.at("xza", k + 1))) - math.sin(float(g.at("xza", k))) for k in range(1, g.nz + 1)])
+    return vx, vy, vz
+
+
 def full_1d(g: Grid, name: str) -> np.ndarray:
     """The metric on (-1:N+2) with zeros outside its reference bounds (the
     storage the oracle uses)."""
