@@ -269,8 +269,8 @@ int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
  * (pprad.f:21-29), SOLVMAT (ppmat.f:1-186: red-black SOR on ER, stop at
  * ||XS||_2/||RHS||_2 <= EPSMAT after at least 5 iterations, or ITMAX, then
  * status 1) with RADIATIVEBOUND (ppbou.f:2049-2299) after each colour, and
- * T = (ER/arad)^(1/4).  RADIATIVEBOUND is implemented for IBDRAD 3, 4, 7, 8,
- * 9 with MODVER <= 5 (other values: status -3). */
+ * T = (ER/arad)^(1/4).  RADIATIVEBOUND is implemented for the IBDRAD values
+ * the context accepts (4, 7, 9) with MODVER <= 5 (MODVER > 5: status -3). */
 typedef struct {
   double d_t;           /* D_T, the bottom temperature gradient of the model
                            (ppinit.f:121-171)                               */

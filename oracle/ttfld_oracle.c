@@ -1178,14 +1178,15 @@ int ttor_diffusion(ttor_state* s) {
 }
 
 /* ---- IRAD=1: RADDIF pprad.f:1-38, DIFFEL :40-72, SOLVMAT ppmat.f:1-186,
- * RADIATIVEBOUND ppbou.f:2049-2299 (RADBOUNDVER = IBDRAD in 3, 4, 7, 8, 9
- * with MODVER <= 5; one rank, periodic phi, poles = .false.) ------------- */
+ * RADIATIVEBOUND ppbou.f:2049-2299 (RADBOUNDVER = IBDRAD 4, 7 or 9, the
+ * top boundaries the rest of this library implements, with MODVER <= 5; one
+ * rank, periodic phi, poles = .false.) ----------------------------------- */
 
 /* RADIATIVEBOUND: bottom T and ER (:2127-2139), top ER at i >= upperbnd
  * (:2145-2236), theta ghost copies (:2256-2271), PLANETSHIFT(6) (:2280). */
 static int radiativebound(ttor_state* s, double d_t, double tinit_bottom, int modver) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
-  if (s->ibdrad < 3 || s->ibdrad > 9 || s->ibdrad == 5 || s->ibdrad == 6) return -3;
+  if (s->ibdrad != 4 && s->ibdrad != 7 && s->ibdrad != 9) return -3;
   if (modver > 5) return -3;
   for (int k = -1; k <= nz + 2; ++k)
     for (int j = -1; j <= ny + 2; ++j) {
@@ -1202,11 +1203,6 @@ static int radiativebound(ttor_state* s, double d_t, double tinit_bottom, int mo
       if (!(ub < nx + 1)) return -3;
       double tj = 0.0;
       switch (s->ibdrad) {
-        case 3:
-        case 8:
-          tj = s->tirr * pow(cos(G1(xyb, j)) * cos(G1(xzb, k)), 0.25);
-          tj = s->ibdrad == 3 ? (tj > 100.0 ? tj : 100.0) : (tj > 950.0 ? tj : 950.0);
-          break;
         case 4: tj = s->tirr; break;
         case 7: tj = H(T, ub - 1, j, k); break;
         case 9:

@@ -70,7 +70,7 @@ int ttor_b_vector_boundaries(ttor_state* s);
 int ttor_fill_hypre_system(ttor_state* s);
 /* RADDIF (pprad.f:1-38, IRAD=1): ER = arad T^4, DIFFEL, SOLVMAT (ppmat.f,
  * red-black SOR on ER with the L2 stop and ITMIN = 5) with RADIATIVEBOUND
- * (ppbou.f:2049-2299; IBDRAD 3, 4, 7, 8, 9, MODVER <= 5) after each colour,
+ * (ppbou.f:2049-2299; IBDRAD 4, 7, 9, MODVER <= 5) after each colour,
  * T = (ER/arad)^(1/4).  d_t is the bottom temperature gradient D_T,
  * tinit_bottom TinitBottom (read with BCXMIN = 6); returns 0, 1 at ITMAX,
  * -3 for a configuration outside that set. */

@@ -41,10 +41,12 @@ def test_raddif_matches_oracle(sh, ibdrad, eps, itmax):
         o.get("global_rnorm") / o.get("global_rhsnorm"))
 
 
-def test_raddif_rejects_unimplemented_boundary(sh):
+def test_raddif_rejects_unimplemented_bottom(sh):
+    """RADIATIVEBOUND's bottom for MODVER > 5 is not implemented: status -3,
+    as the oracle returns."""
     f = fld_from_shell(sh, eps=1e-6, itmax=10)
-    f.set_params(ibdrad=5, iii=2)
+    f.set_params(ibdrad=9, iii=2)
     from ttcode_gb300._ffi import TTFLDError
     with pytest.raises(TTFLDError) as e:
-        f.raddif(0.0, 0.0, 1, 0)
+        f.raddif(0.0, 0.0, 6, 0)
     assert e.value.status == -3

@@ -400,7 +400,7 @@ def test_raddif_converges_with_gradient_top(shell):
 
 
 def test_raddif_rejects_unimplemented_boundaries(shell):
-    for ib in (1, 5, 6):
+    for ib in (1, 3, 5, 6, 8):
         o = rad_oracle(shell, ib, 1e-6, 10)
         assert o.call("raddif", 0.0, 0.0, 1, 0) == -3
     o = rad_oracle(shell, 9, 1e-6, 10)

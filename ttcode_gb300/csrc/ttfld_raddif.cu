@@ -12,7 +12,7 @@
 // and the top (ER at i >= upperbnd), copies the theta ghosts and shifts the
 // phi halo.  Every kernel keeps the reference's operation order (the library
 // is built with --fmad=false), so the iterates equal the reference loop's
-// except where pow() enters (the IBDRAD = 3, 8, 9 tops and the final T).
+// except where pow() enters (the IBDRAD = 9 top and the final T).
 #include <math.h>
 
 #include "ttfld_internal.cuh"
@@ -112,11 +112,6 @@ __global__ void __launch_bounds__(kThreads) radbound_xkernel(Dev d, double d_t, 
     }
     double tj = 0.0;
     switch (d.ibdrad) {
-      case 3:
-      case 8:
-        tj = d.tirr * pow(cos(G(xyb, j)) * cos(G(xzb, k)), 0.25);
-        tj = d.ibdrad == 3 ? (tj > 100.0 ? tj : 100.0) : (tj > 950.0 ? tj : 950.0);
-        break;
       case 4: tj = d.tirr; break;
       case 7: tj = HA(T, ub - 1, j, k); break;
       default:  // 9
@@ -207,7 +202,7 @@ extern "C" int ttfld_raddif(ttfld_ctx* c, const ttfld_raddif_params* p, ttfld_so
   if (!c || !p || !p->volxb || !p->volyb || !p->volzb) return TTFLD_E_ARGS;
   const Dev& d = c->d;
   if (d.nz == 1 || c->dims.poles) return TTFLD_E_UNSUPPORTED;
-  if (!(d.ibdrad == 3 || d.ibdrad == 4 || d.ibdrad == 7 || d.ibdrad == 8 || d.ibdrad == 9) || p->modver > 5)
+  if (!(d.ibdrad == 4 || d.ibdrad == 7 || d.ibdrad == 9) || p->modver > 5)
     return TTFLD_E_UNSUPPORTED;
   TT_CHECK(cudaSetDevice(c->device));
   ttfld_solve_stats local{};
