@@ -27,8 +27,6 @@ struct SolverDev {
   double ratio;        // rnorm / rhsnorm
   double true_l1;      // ||b - A x||_1 of the last residual pass
   double scratch[3];
-  unsigned int bar_count;  // grid barrier of the persistent sweep kernel:
-  unsigned int bar_gen;    // arrivals and generation
   int iter;            // SOR_ITER
   int done;            // 1 once the stopping rule fired
   int maxit;           // 1 if ITMAX ended the loop
@@ -38,6 +36,11 @@ struct SolverDev {
   int bar_timeout;     // 1 if a grid barrier wait ran out (the kernel gave up)
   int stalled;         // 1 if the FP32 inner loop stopped at its rounding floor
   int bad_weights;     // PCG: a row without a valid symmetrising weight
+  // grid barrier of the persistent kernels: arrivals and generation, each on
+  // a cache line of its own so that the waiters' polls of the generation do
+  // not contend with the arrivals' atomics
+  alignas(128) unsigned int bar_count;
+  alignas(128) unsigned int bar_gen;
 };
 
 // Reduction targets of the outer Newton loop.
@@ -195,6 +198,7 @@ __device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) 
     } else {
       long long polls = 0;
       while (ld_acquire(&sol->bar_gen) == g0) {
+        __nanosleep(32);
         if (++polls > kBarrierSpins || *(volatile int*)&sol->bar_timeout) {
           atomicExch(&sol->bar_timeout, 1);
           ok = 0;
