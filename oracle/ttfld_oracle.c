@@ -12,8 +12,10 @@
  * each site) the restatement uses a clamped, defined value instead; the
  * cells affected are ghost cells that the step never reads back.
  */
+#define _POSIX_C_SOURCE 200809L  /* pthread barriers under -std=c11 */
 #include "ttfld_oracle.h"
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -846,11 +848,11 @@ int ttor_b_vector_boundaries(ttor_state* s) {
 }
 
 /* One colour pass of the red-black loop, ppsor.f:59-88 / 107-136. */
-static double sor_colour(ttor_state* s, double* x, const double* b, int colour, int zmax) {
+static double sor_colour_k(ttor_state* s, double* x, const double* b, int colour, int k0, int k1) {
   const int nx = s->nx, ny = s->ny;
   double rnorm = 0.0;
 #define X(i, j, k) x[(size_t)((i) + 1) + (size_t)NXH * ((size_t)((j) + 1) + (size_t)NYH * (size_t)((k) + 1))]
-  for (int k = 1; k <= zmax; ++k)
+  for (int k = k0; k <= k1; ++k)
     for (int j = 1; j <= ny; ++j) {
       int imin = 2 - ((j + k + colour) % 2);
       for (int i = imin; i <= nx; i += 2) {
@@ -865,6 +867,10 @@ static double sor_colour(ttor_state* s, double* x, const double* b, int colour, 
     }
 #undef X
   return rnorm;
+}
+
+static double sor_colour(ttor_state* s, double* x, const double* b, int colour, int zmax) {
+  return sor_colour_k(s, x, b, colour, 1, zmax);
 }
 
 /* The red-black iteration with the ppsor.f:161-177 stopping rule. */
@@ -907,6 +913,82 @@ int ttor_solve_with_sor(ttor_state* s, int fill, int use_guess) {
   s->sor_total += s->sor_iter;
   s->solves += 1;
   return rc;
+}
+
+/* The phi halo copies of shift_halo for the theta rows k0..k1. */
+static void shift_halo_k(ttor_state* s, double* a, int k0, int k1) {
+  const int nx = s->nx, ny = s->ny;
+#define A(i, j, k) a[(size_t)((i) + 1) + (size_t)NXH * ((size_t)((j) + 1) + (size_t)NYH * (size_t)((k) + 1))]
+  for (int k = k0; k <= k1; ++k)
+    for (int i = -1; i <= nx + 2; ++i) {
+      A(i, 0, k) = A(i, ny, k);
+      A(i, -1, k) = A(i, ny - 1, k);
+      A(i, ny + 1, k) = A(i, 1, k);
+      A(i, ny + 2, k) = A(i, 2, k);
+    }
+#undef A
+}
+
+/* The reference decomposes the grid over MPI ranks, one serial rank per
+ * core; its CPU baseline is the same red-black sweeps on theta slabs, one
+ * thread per slab, a barrier after each colour (where the ranks exchange
+ * halos), the slab norms added in slab order. */
+typedef struct {
+  ttor_state* s;
+  int k0, k1, nsweeps;
+  pthread_barrier_t* bar;
+  double* part;  /* per slab */
+} mt_arg;
+
+static void* mt_worker(void* p) {
+  mt_arg* a = (mt_arg*)p;
+  ttor_state* s = a->s;
+  for (int it = 0; it < a->nsweeps; ++it) {
+    double r = sor_colour_k(s, s->DELTA_ER, s->RHS_ER, 0, a->k0, a->k1);
+    shift_halo_k(s, s->DELTA_ER, a->k0, a->k1);
+    pthread_barrier_wait(a->bar);
+    r = r + sor_colour_k(s, s->DELTA_ER, s->RHS_ER, 1, a->k0, a->k1);
+    shift_halo_k(s, s->DELTA_ER, a->k0, a->k1);
+    *a->part = r;
+    pthread_barrier_wait(a->bar);
+  }
+  return NULL;
+}
+
+int ttor_sor_sweeps_mt(ttor_state* s, int nsweeps, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > s->nz) nthreads = s->nz;
+  if (nthreads > 256) nthreads = 256;
+  double rhsnorm = 0.0;
+  for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(s->RHS_ER[c]);
+  s->global_rhsnorm = rhsnorm;
+  pthread_barrier_t bar;
+  if (pthread_barrier_init(&bar, NULL, (unsigned)nthreads)) return -2;
+  pthread_t th[256];
+  mt_arg args[256];
+  double part[256];
+  int rc = 0, started = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    args[t].s = s;
+    args[t].k0 = 1 + (int)((long long)s->nz * t / nthreads);
+    args[t].k1 = (int)((long long)s->nz * (t + 1) / nthreads);
+    args[t].nsweeps = nsweeps;
+    args[t].bar = &bar;
+    args[t].part = &part[t];
+  }
+  for (int t = 1; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, mt_worker, &args[t])) { rc = -2; break; }
+    ++started;
+  }
+  if (rc == 0) mt_worker(&args[0]);
+  for (int t = 1; t <= started; ++t) pthread_join(th[t], NULL);
+  pthread_barrier_destroy(&bar);
+  if (rc) return rc;
+  double r = 0.0;
+  for (int t = 0; t < nthreads; ++t) r = r + part[t];
+  s->global_rnorm = r;
+  s->sor_iter = nsweeps;
+  return 0;
 }
 
 int ttor_sor_sweeps(ttor_state* s, int nsweeps) {

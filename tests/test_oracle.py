@@ -405,3 +405,17 @@ def test_raddif_rejects_unimplemented_boundaries(shell):
         assert o.call("raddif", 0.0, 0.0, 1, 0) == -3
     o = rad_oracle(shell, 9, 1e-6, 10)
     assert o.call("raddif", 0.0, 0.0, 6, 0) == -3       # MODVER > 5
+
+
+def test_slab_threads_give_the_serial_sweeps(shell):
+    """The CPU baseline's slab-parallel sweeps (one thread per theta slab, a
+    barrier per colour) leave the serial loop's iterate bit for bit."""
+    o = oracle_from_shell(shell)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("sor_sweeps", 7) == 0
+    x1, r1 = o.f("DELTA_ER").copy(), o.get("global_rnorm")
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("sor_sweeps_mt", 7, 5) == 0
+    assert np.array_equal(o.f("DELTA_ER"), x1)
+    assert abs(o.get("global_rnorm") - r1) <= 1e-12 * r1
