@@ -261,7 +261,8 @@ int ttfld_solve_system(ttfld_ctx* ctx, ttfld_solve_stats* stats);
  * ||Sigma W (b-Ax)||_2 / ||Sigma W b||_2 <= tol on the symmetrised system,
  * or maxit iterations (then status 1).  tol <= 0 and maxit <= 0 select the
  * reference's 1e-6 and 50 (pphypre.f:45-55).  hypre's SMG preconditioner is
- * replaced by an exact radial line solve.  stats may be NULL. */
+ * replaced by one symmetric red-black Gauss-Seidel sweep over the radial
+ * lines (each line solved exactly).  stats may be NULL. */
 int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
                            ttfld_solve_stats* stats);
 /* The IRAD=1 radiation step, RADDIF (pprad.f:1-38): ER = arad T^4, DIFFEL

@@ -29,9 +29,12 @@
 //         to a relative reduction of its preconditioned residual norm; x += Sigma e.
 //
 // Preconditioner.  The radial couplings dominate by two to three orders of
-// magnitude (the shell is thin in r), so the preconditioner is the exact
-// solve of the tridiagonal radial line of every (j,k) column, factored once
-// per solve (Thomas algorithm, FP32 pivots).
+// magnitude (the shell is thin in r), so the preconditioner is built on the
+// exact solve of the tridiagonal radial line of a (j,k) column, factored
+// once per solve (Thomas algorithm, FP32 pivots): TTFLD_SOLVER_PCG applies
+// it to every column (block Jacobi); SOLVE_WITH_HYPRE, whose caller bounds
+// the iterations at hypre's 50, applies one symmetric red-black line
+// Gauss-Seidel sweep (half the iterations, three times the cost of one).
 //
 // Layout.  The FP32 inner arrays are line-major, q = (i-1)*NY*NZ +
 // (k-1)*NY + (j-1): in a line solve one thread walks one column and the
@@ -332,6 +335,93 @@ __device__ __forceinline__ float line_pass(const Kry& k, long long c, float alph
   return dot;
 }
 
+// One radial line of the red-black line Gauss-Seidel preconditioner for
+// column c (j0, k0): with UPDATE first r -= alpha s; then
+// z = T^-1 (r - the couplings to the four phi/theta neighbour columns, which
+// all have the other colour, times their z).  Returns r.z of the line.
+constexpr int kGsBatch = 4;
+template <bool UPDATE>
+__device__ __forceinline__ float line_gs(const Kry& k, long long c, float alpha) {
+  constexpr int U = kGsBatch;
+  const unsigned int ncol = (unsigned int)k.ncol;
+  const int nx = k.nx, ny = k.ny;
+  const int j0 = (int)(c % ny), k0 = (int)(c / ny);
+  const unsigned int c0 = (unsigned int)c;
+  // neighbour columns (theta neighbours outside the grid read column c with a zero coupling)
+  const unsigned int cjp = j0 == ny - 1 ? c0 - (ny - 1) : c0 + 1;
+  const unsigned int cjm = j0 == 0 ? c0 + (ny - 1) : c0 - 1;
+  const bool hkp = k0 + 1 < k.nz, hkm = k0 > 0;
+  const unsigned int ckp = hkp ? c0 + ny : c0, ckm = hkm ? c0 - ny : c0;
+  float yprev = 0.f, lprev = 0.f;
+  for (int i0 = 0; i0 < nx; i0 += U) {
+    const unsigned int qb = (unsigned int)i0 * ncol;
+    float rr[U], ss[U], cc[U], gg[U], nb[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u < nx) {
+        const unsigned int o = qb + (unsigned int)u * ncol;
+        rr[u] = k.r[o + c0];
+        if (UPDATE) ss[u] = k.s[o + c0];
+        cc[u] = k.cr[o + c0];
+        gg[u] = k.g[o + c0];
+        const float ctm = hkm ? k.ct[o + ckm] : 0.f;
+        nb[u] = fmaf(k.cp[o + c0], k.z[o + cjp],
+                fmaf(k.cp[o + cjm], k.z[o + cjm], fmaf(k.ct[o + c0], k.z[o + ckp], ctm * k.z[o + ckm])));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u < nx) {
+        const unsigned int q = qb + (unsigned int)u * ncol + c0;
+        float ri = rr[u];
+        if (UPDATE) {
+          ri = fmaf(-alpha, ss[u], ri);
+          k.r[q] = ri;
+        }
+        const float y = fmaf(-lprev, yprev, ri - nb[u]);
+        k.z[q] = y;
+        lprev = cc[u] * gg[u];
+        yprev = y;
+      }
+    }
+  }
+  float dot = 0.f, znext = 0.f;
+  for (int i1 = nx - 1; i1 >= 0; i1 -= U) {
+    const unsigned int qb = c0 + (unsigned int)i1 * ncol;
+    float yy[U], cc[U], gg[U], rr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i1 - u >= 0) {
+        const unsigned int q = qb - (unsigned int)u * ncol;
+        yy[u] = k.z[q];
+        cc[u] = k.cr[q];
+        gg[u] = k.g[q];
+        rr[u] = k.r[q];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i1 - u >= 0) {
+        const unsigned int q = qb - (unsigned int)u * ncol;
+        const float zi = fmaf(-cc[u], znext, yy[u]) * gg[u];
+        k.z[q] = zi;
+        znext = zi;
+        dot = fmaf(rr[u], zi, dot);
+      }
+    }
+  }
+  return dot;
+}
+
+// Column m of colour C (0: (j+k) even, 1: odd) in the red-black order of
+// the columns; NY is even, so each theta row holds NY/2 of each colour.
+__device__ __forceinline__ long long col_of(long long m, int C, int ny) {
+  const long long half = ny >> 1;
+  const long long k0 = m / half;
+  const long long jj = m - k0 * half;
+  return k0 * ny + 2 * jj + ((k0 + C) & 1);
+}
+
 __device__ __forceinline__ float4 ldf4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void stf4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {
@@ -417,6 +507,28 @@ __device__ __forceinline__ float op_one(const Kry& k, const float* po, float* pn
   return pc * sv;
 }
 
+// z = M^-1 r for the preconditioner M, with UPDATE first r -= alpha s.
+// SGS: one symmetric red-black line Gauss-Seidel sweep (red lines, black
+// lines against the new red z, red lines against the black z; two more grid
+// barriers); otherwise the radial line solve of every column (block
+// Jacobi).  acc gains this thread's share of r.z.  False if a barrier gave
+// up.
+template <bool UPDATE, bool SGS>
+__device__ __forceinline__ bool precondition(const Kry& k, SolverDev* sol, unsigned int nb, long long col0,
+                                             long long colstride, float alpha, float& acc) {
+  if (!SGS) {
+    for (long long c = col0; c < k.ncol; c += colstride) acc += line_pass<UPDATE>(k, c, alpha);
+    return true;
+  }
+  const long long half = k.ncol >> 1;
+  for (long long m = col0; m < half; m += colstride) (void)line_pass<UPDATE>(k, col_of(m, 0, k.ny), alpha);
+  if (!grid_sync(sol, nb)) return false;
+  for (long long m = col0; m < half; m += colstride) acc += line_gs<UPDATE>(k, col_of(m, 1, k.ny), alpha);
+  if (!grid_sync(sol, nb)) return false;
+  for (long long m = col0; m < half; m += colstride) acc += line_gs<false>(k, col_of(m, 0, k.ny), 0.f);
+  return true;
+}
+
 // The FP32 PCG iteration on S e = r from e = 0 (r, e set by the anchor).
 // Line phases: the warps of all blocks are dealt round-robin over groups of
 // 32 consecutive columns.  Operator phase: p_new = z + beta p (p read from
@@ -428,12 +540,13 @@ __device__ __forceinline__ float op_one(const Kry& k, const float* po, float* pn
 // FP32 floor), on a non-positive p.s, or after maxit iterations; the last
 // iteration's e update is then applied.  maxit = 0 only computes r0.z0
 // (sol->scratch[2]).
+template <bool SGS>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, SolverDev* sol, double* partials,
                                                                    int maxit, double stop_ratio) {
   __shared__ double sh[32];
   __shared__ double bc[3];
   const unsigned int nb = gridDim.x;
-  const long long n = k.n, ncol = k.ncol;
+  const long long n = k.n;
   const int ny = k.ny;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nth = (long long)gridDim.x * blockDim.x;
@@ -447,7 +560,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   // terms) are FP32 -- GB300's FP64 pipe is narrow -- and widened to FP64
   // for the block and grid sums.
   float acc = 0.f;
-  for (long long c = col0; c < ncol; c += colstride) acc += line_pass<false>(k, c, 0.f);
+  if (!precondition<false, SGS>(k, sol, nb, col0, colstride, 0.f, acc)) return;
   {
     const double v = block_sum((double)acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -502,9 +615,9 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
       break;
     }
     const float alpha = (float)(gamma / ps);
-    // line phase: r -= alpha s, z = T^-1 r, r.z
+    // line phase: r -= alpha s, z = M^-1 r, r.z
     acc = 0.f;
-    for (long long c = col0; c < ncol; c += colstride) acc += line_pass<true>(k, c, alpha);
+    if (!precondition<true, SGS>(k, sol, nb, col0, colstride, alpha, acc)) return;
     {
       const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -591,7 +704,10 @@ int pcg_blocks(long long ncells) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg32_persistent, kPcgThreads, 0);
+    int per_sm_gs = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg32_persistent<false>, kPcgThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_gs, pcg32_persistent<true>, kPcgThreads, 0);
+    if (per_sm_gs < per_sm) per_sm = per_sm_gs;
     long long b = coop ? (long long)sms * per_sm : 0;
     blocks = (int)(b > kMaxPartials ? kMaxPartials : b);
   }
@@ -600,7 +716,7 @@ int pcg_blocks(long long ncells) {
 }
 
 // One inner run; returns its iterations in *its.
-int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int* its) {
+int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, bool sgs, int* its) {
   const int nb = pcg_blocks(w->k.n);
   if (nb <= 0) {
     fprintf(stderr, "ttfld: the PCG solver needs cooperative launch\n");
@@ -614,8 +730,8 @@ int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int* it
   SolverDev* sol = c->sol;
   double* partials = c->partials;
   void* args[] = {&k, &sol, &partials, &maxit, &stop_ratio};
-  TT_CHECK(cudaLaunchCooperativeKernel((const void*)pcg32_persistent, dim3(nb), dim3(kPcgThreads), args, 0,
-                                       c->stream));
+  const void* kern = sgs ? (const void*)pcg32_persistent<true> : (const void*)pcg32_persistent<false>;
+  TT_CHECK(cudaLaunchCooperativeKernel(kern, dim3(nb), dim3(kPcgThreads), args, 0, c->stream));
   count_launches(1);
   int rc = poll_sol(c);
   if (rc) return rc;
@@ -654,7 +770,7 @@ int prepare(ttfld_ctx* c, KryWork* w, bool hypre) {
 // tol (the hypre system's PCG rule on the symmetric form).  budget bounds
 // the PCG iterations.  With guess_test, the initial iterate is kept only if
 // its preconditioned residual norm r.z is below that of the zero iterate.
-int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, long long budget, bool l2,
+int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, long long budget, bool l2, bool sgs,
              int guess_test, int* fallback, ttfld_solve_stats* st) {
   KryWork* w = kry_work(c);
   if (!w) return TTFLD_E_CUDA;
@@ -669,7 +785,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
   }
   if (guess_test) {
     int its = 0;
-    if ((rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
+    if ((rc = launch_inner(c, w, 0, 0.0, sgs, &its))) return rc;
     const double g_guess = c->host_sol->scratch[2];
     // the zero iterate: r = b
     double* zero_x = c->guess_tmp;
@@ -678,7 +794,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
       zero_x = c->guess_tmp;
     }
     TT_CHECK(cudaMemsetAsync(zero_x, 0, nhalo(c->d) * 8, c->stream));
-    if ((rc = anchor(c, w, zero_x, b, hypre, l2, false)) || (rc = launch_inner(c, w, 0, 0.0, &its))) return rc;
+    if ((rc = anchor(c, w, zero_x, b, hypre, l2, false)) || (rc = launch_inner(c, w, 0, 0.0, sgs, &its))) return rc;
     const double g_zero = c->host_sol->scratch[2];
     if (!(g_guess < g_zero)) {
       TT_CHECK(cudaMemsetAsync(x, 0, nhalo(c->d) * 8, c->stream));
@@ -706,7 +822,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     if (target < kInnerReduce) target = kInnerReduce;
     long long left = budget - total;
     int its = 0;
-    if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, &its))) return rc;
+    if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, sgs, &its))) return rc;
     total += its;
     ++anchors;
     kry_update_kernel<<<grid_cells(w->k.n), kThreads, 0, c->stream>>>(c->d, w->k, x);
@@ -734,7 +850,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
 
 int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
-  return pcg_core(c, x, b, false, c->opts.tol, budget, false, guess_test, fallback, st);
+  return pcg_core(c, x, b, false, c->opts.tol, budget, false, false, guess_test, fallback, st);
 }
 
 void krylov_free(ttfld_ctx* c) {
@@ -766,7 +882,7 @@ int ttfld_solve_with_hypre(ttfld_ctx* c, double tol, int maxit, ttfld_solve_stat
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) { x[hidx(d, i, j, k)] = 1.0; });
   TT_CHECK_LAUNCH();
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
-  rc = pcg_core(c, x, d.RHS, true, tol, maxit, true, 0, nullptr, st);
+  rc = pcg_core(c, x, d.RHS, true, tol, maxit, true, true, 0, nullptr, st);
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));
   float ms = 0.f;
