@@ -44,7 +44,10 @@ enum ttfld_status {
   TTFLD_E_UNSUPPORTED = -3, /* configuration outside the implemented set  */
   TTFLD_E_NONPOSITIVE_Q = -7, /* Q+conv*dQ <= 0, ppenergy.f:411-521       */
   TTFLD_E_NONFINITE = -8,   /* NaN/Inf found in a solver norm             */
-  TTFLD_E_NOMODEL = -9      /* learned guess requested without a model    */
+  TTFLD_E_NOMODEL = -9,     /* learned guess requested without a model    */
+  TTFLD_E_OPACITY = -10     /* KAPPA from a table: T <= 0, (T, rho) outside
+                               the table, or a non-positive interpolated
+                               opacity, where the reference stops          */
 };
 
 /* Fields addressable through ttfld_upload / ttfld_download. */
@@ -110,6 +113,8 @@ typedef struct {
   int32_t adjust_sor; /* call ADJUST_SOR_PARAM where the reference would  */
   int32_t kappa_model; /* 0 = synthetic analytic (stand-in for the tables) */
                        /* 1 = prescribed: XKAP* are uploaded, KAPPA no-op  */
+                       /* 2 = a (T, rho) table, BurrowsOPC's interpolation
+                              (ttfld_set_opacity_table)                    */
 } ttfld_params;
 
 /* How SOLVE_WITH_SOR's linear system is solved on the device. */
@@ -330,6 +335,23 @@ typedef struct {
 } ttfld_energy;
 /* The sums of the current state (E_R, Q, STELLARINPUT, FLUX_X/Z). */
 int ttfld_energy_sums(ttfld_ctx* ctx, ttfld_energy* out);
+
+/* The opacity table of kappa_model 2 (BurrowsOPC, pprphy.f:1005-1229, as
+ * KAPPA's IKAPTYP 20:25 branch calls it, pprphy.f:321-351): log10 T and
+ * log10 rho nodes (increasing) and log10 of the Rosseland, Planck and
+ * absorption means on them, T index fastest (the layout of
+ * BurrowsXKAP_ross(IT,IW)).  The reference reads them from files
+ * (READBURROWSOPCTABLE, pprphy.f:1231-1541) that are not in its tree; the
+ * caller passes the arrays.  Host memory, copied. */
+typedef struct {
+  int32_t nt, nrh;
+  const double* log_t;     /* (nt)  */
+  const double* log_rho;   /* (nrh) */
+  const double* log_ross;  /* (nt, nrh) */
+  const double* log_plnk;
+  const double* log_abs;
+} ttfld_opacity_table;
+int ttfld_set_opacity_table(ttfld_ctx* ctx, const ttfld_opacity_table* table);
 
 /* ---- measurement (no reference counterpart) --------------------------- */
 /* Runs n back-to-back sweeps of a solver's sweep kernels on the current

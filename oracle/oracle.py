@@ -68,6 +68,7 @@ def _load():
         lib.ttor_sor_sweeps_mt.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         lib.ttor_coupled_energy_eqs.argtypes = [vp, ctypes.c_int]
         lib.ttor_raddif.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        lib.ttor_set_opacity_table.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [vp] * 5
         lib.ttor_true_residual_l1.restype = ctypes.c_double
         lib.ttor_true_residual_l1.argtypes = [vp]
         _lib = lib

@@ -35,6 +35,9 @@ struct ttor_state {
   double kap0, theta_last;
   int itmax, bcxmin, ibdrad, iflimtyp, f_incident, ieta, isigtyp, iii;
   int adjust_sor, poles, ikaptyp;
+  /* opacity table (BurrowsOPC's arrays), used by KAPPA when opac_nt > 0 */
+  int opac_nt, opac_nrh;
+  double *opac_lt, *opac_lrh, *opac_ross, *opac_plnk, *opac_abs;
   /* results */
   int sor_iter, energy_iter, status, sor_total, solves;
   double global_rnorm, global_rhsnorm, global_deltaq, global_deltaer;
@@ -169,6 +172,7 @@ void ttor_destroy(ttor_state* s) {
   if (!s) return;
   for (size_t f = 0; f < NFIELDS; ++f) free(*(double**)((char*)s + FIELDS[f].off));
   free(s->UPPERBND);
+  free(s->opac_lt); free(s->opac_lrh); free(s->opac_ross); free(s->opac_plnk); free(s->opac_abs);
   free(s);
 }
 
@@ -382,8 +386,99 @@ static double kap_formula(const ttor_state* s, double t, double rh, double kmul)
   return ((s->kap0 * sqrt(rh)) * (th * sqrt(th))) * kmul;
 }
 
+/* BurrowsOPC pprphy.f:1005-1229 (Rosseland, Planck, absorption means and
+ * the T-derivative stand-ins of :1180-1185).  Returns 0, or 1 T <= 0, 2
+ * above the table, 3 below it, 4 a non-positive opacity. */
+static int burrows_opc(const ttor_state* s, double t, double rh, double* kp, double* kr, double* ka, double* dkp,
+                       double* dka) {
+  if (!(t > 0.0)) return 1;
+  double rh1 = log10(rh), tm1 = log10(t);
+  if (tm1 < (double)1.69896f) tm1 = (double)1.69897f;
+  if (tm1 > (double)3.69889f) tm1 = (double)3.69888f;
+  if (rh1 < (double)-11.9996f) rh1 = (double)-11.9995f;
+  if (rh1 > (double)-1.99993f) rh1 = (double)-1.99994f;
+  const int nt = s->opac_nt, nr = s->opac_nrh;
+  int K;
+  for (K = 1; K <= nt; ++K)
+    if (s->opac_lt[K - 1] > tm1) break;
+  if (K == nt + 1) return 2;
+  const int it = K, it1 = K - 1;
+  if (it1 == 0) return 3;
+  double ws1 = s->opac_lt[it1 - 1] - tm1;
+  double ws = s->opac_lt[it1 - 1] - s->opac_lt[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  for (K = 1; K <= nr; ++K)
+    if (s->opac_lrh[K - 1] > rh1) break;
+  if (K == nr + 1) return 2;
+  const int iw = K, iw1 = K - 1;
+  if (iw1 == 0) return 3;
+  double ws2 = rh1 - s->opac_lrh[iw1 - 1];
+  double ws3 = s->opac_lrh[iw - 1] - s->opac_lrh[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+#define TB(a, p, q) a[(size_t)((p) - 1) + (size_t)nt * (size_t)((q) - 1)]
+  const double* tabs[3] = {s->opac_ross, s->opac_plnk, s->opac_abs};
+  double out[3];
+  for (int m = 0; m < 3; ++m) {
+    const double* a = tabs[m];
+    const double w4 = ws2 * (ws1 * TB(a, it, iw) + ws * TB(a, it1, iw));
+    const double w5 = ws3 * (ws1 * TB(a, it, iw1) + ws * TB(a, it1, iw1));
+    out[m] = pow(10.0, w4 + w5);
+  }
+  *kr = out[0]; *kp = out[1]; *ka = out[2];
+  const double dt = pow(10.0, s->opac_lt[it - 1]) - pow(10.0, s->opac_lt[it1 - 1]);
+  *dkp = (pow(10.0, TB(s->opac_plnk, it, iw)) - pow(10.0, TB(s->opac_plnk, it1, iw))) / dt;
+  *dka = (pow(10.0, TB(s->opac_abs, it, iw)) - pow(10.0, TB(s->opac_abs, it1, iw))) / dt;
+#undef TB
+  if (*kr <= 0.0 || *kp <= 0.0 || *ka <= 0.0) return 4;
+  return 0;
+}
+
+int ttor_set_opacity_table(ttor_state* s, int nt, int nrh, const double* lt, const double* lrh,
+                           const double* ross, const double* plnk, const double* absk) {
+  if (nt < 2 || nrh < 2) return -1;
+  free(s->opac_lt); free(s->opac_lrh); free(s->opac_ross); free(s->opac_plnk); free(s->opac_abs);
+  const size_t nn = (size_t)nt * nrh;
+  s->opac_lt = (double*)malloc(nt * sizeof(double));
+  s->opac_lrh = (double*)malloc(nrh * sizeof(double));
+  s->opac_ross = (double*)malloc(nn * sizeof(double));
+  s->opac_plnk = (double*)malloc(nn * sizeof(double));
+  s->opac_abs = (double*)malloc(nn * sizeof(double));
+  if (!s->opac_lt || !s->opac_lrh || !s->opac_ross || !s->opac_plnk || !s->opac_abs) return -2;
+  memcpy(s->opac_lt, lt, nt * sizeof(double));
+  memcpy(s->opac_lrh, lrh, nrh * sizeof(double));
+  memcpy(s->opac_ross, ross, nn * sizeof(double));
+  memcpy(s->opac_plnk, plnk, nn * sizeof(double));
+  memcpy(s->opac_abs, absk, nn * sizeof(double));
+  s->opac_nt = nt;
+  s->opac_nrh = nrh;
+  return 0;
+}
+
 int ttor_kappa(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
+  if (s->opac_nt > 0) {   /* the IKAPTYP 20:25 branch with BurrowsOPC, pprphy.f:321-351 */
+    for (int k = -1; k <= nz + 2; ++k)
+      for (int j = -1; j <= ny + 2; ++j) {
+        int ub = P(UPPERBND, j, k);
+        if (ub < 1 || ub > nx + 1) return -2;
+        for (int i = -1; i <= ub; ++i) {
+          double kp, kr, ka, dkp, dka;
+          if (burrows_opc(s, H(T, i, j, k), H(RH, i, j, k), &kp, &kr, &ka, &dkp, &dka)) return -10;
+          H(XKAPP, i, j, k) = kp; H(XKAPR, i, j, k) = kr; H(XKAPA, i, j, k) = ka;
+          H(DXKAPP_DT, i, j, k) = dkp; H(DXKAPA_DT, i, j, k) = dka;
+        }
+        for (int i = ub; i <= nx + 2; ++i) {
+          H(XKAPR, i, j, k) = H(XKAPR, ub - 1, j, k);
+          H(XKAPP, i, j, k) = H(XKAPP, ub - 1, j, k);
+          H(XKAPA, i, j, k) = H(XKAPA, ub - 1, j, k);
+          H(DXKAPP_DT, i, j, k) = H(DXKAPP_DT, ub - 1, j, k);
+          H(DXKAPA_DT, i, j, k) = H(DXKAPA_DT, ub - 1, j, k);
+        }
+      }
+    return 0;
+  }
   for (int k = -1; k <= nz + 2; ++k)
     for (int j = -1; j <= ny + 2; ++j) {
       int ub = P(UPPERBND, j, k);
@@ -692,6 +787,10 @@ int ttor_bounds(ttor_state* s) {
   /* BOUNDXMIN(9) */
   double kapT111 = 0.0;
   if (s->iii <= 0) kapT111 = kap_formula(s, H(T, 1, 1, 1), H(RH, 1, 1, 1), H(KMUL, 1, 1, 1));
+  if (s->iii <= 0 && s->opac_nt > 0) {   /* ppbou.f:1040-1044 */
+    double kp, ka, dkp, dka;
+    if (burrows_opc(s, H(T, 1, 1, 1), H(RH, 1, 1, 1), &kp, &kapT111, &ka, &dkp, &dka)) return -10;
+  }
   for (int k = -1; k <= nz + 2; ++k)
     for (int j = -1; j <= ny + 2; ++j) {
       double dtdr;

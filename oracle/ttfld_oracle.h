@@ -68,6 +68,11 @@ int ttor_b_vector_boundaries(ttor_state* s);
 /* FILLHYPREMATRIX + FILLHYPREVECTORS (pphypre.f:115-334) into HYP_A..HYP_G,
  * HYP_RHS from the EVAL arrays, RHS_ER and UPPERBND. */
 int ttor_fill_hypre_system(ttor_state* s);
+/* The opacity table KAPPA interpolates (BurrowsOPC) once set: log10 T (nt),
+ * log10 rho (nrh), log10 Rosseland / Planck / absorption means (nt x nrh, T
+ * index fastest).  KAPPA then returns -10 where the reference stops. */
+int ttor_set_opacity_table(ttor_state* s, int nt, int nrh, const double* lt, const double* lrh,
+                           const double* ross, const double* plnk, const double* absk);
 /* RADDIF (pprad.f:1-38, IRAD=1): ER = arad T^4, DIFFEL, SOLVMAT (ppmat.f,
  * red-black SOR on ER with the L2 stop and ITMIN = 5) with RADIATIVEBOUND
  * (ppbou.f:2049-2299; IBDRAD 4, 7, 9, MODVER <= 5) after each colour,

@@ -300,3 +300,35 @@ def test_adjust_sor_param_same_omega(small):
     w_dev = f.adjust_sor_param()
     assert o.call("adjust_sor_param") == 0
     assert w_dev == o.get("sorparam")
+
+
+def test_opacity_table_step_matches_oracle(small):
+    """kappa_model 2: KAPPA interpolates a (T, rho) table as BurrowsOPC does
+    (pprphy.f:1005-1229); opacities, their T-derivative stand-ins and a full
+    implicit step against the oracle's."""
+    from ttcode_gb300.fld import FLD
+    from ttcode_gb300.synthetic import analytic_opacity_table
+    import oracle as orc
+    tab = analytic_opacity_table(1e-2)
+    o = oracle_from_shell(small, eps=1e-12, start=False)
+    keep = [np.ascontiguousarray(a) for a in tab[:2]] + [np.asfortranarray(a) for a in tab[2:]]
+    assert orc._load().ttor_set_opacity_table(o.h, tab[0].size, tab[1].size, *[a.ctypes.data for a in keep]) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    o.set("iii", small.params.get("iii", 1))
+    p = dict(small.params, kappa_model=2, epsmat=1e-10, itmax=200000)
+    f = FLD(small.grid, p)
+    f.set_opacity_table(*tab)
+    f.load_shell(small)
+    f.set_params(iii=0)
+    f.bounds()
+    f.kappa()
+    f.set_params(iii=small.params.get("iii", 1))
+    for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= 1e-13, n
+    f.set_solver("mixed", tol=1e-10)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    st = f.coupled_energy_eqs(True)
+    assert st.energy_iter == int(o.get("energy_iter"))
+    for n in ("ER", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= TOL, n

@@ -419,3 +419,32 @@ def test_slab_threads_give_the_serial_sweeps(shell):
     assert o.call("sor_sweeps_mt", 7, 5) == 0
     assert np.array_equal(o.f("DELTA_ER"), x1)
     assert abs(o.get("global_rnorm") - r1) <= 1e-12 * r1
+
+
+def test_opacity_table_interpolation(shell):
+    """BurrowsOPC's interpolation (ttor_set_opacity_table + KAPPA) on a table
+    of the analytic model reproduces the model (log kappa is linear in log T
+    and log rho), with the T-derivative stand-ins of pprphy.f:1180-1185."""
+    from ttcode_gb300.synthetic import analytic_opacity_table
+    o = oracle_from_shell(shell, start=False)
+    o.f("KMUL")[...] = 1.0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    ref = {n: o.f(n).copy() for n in ("XKAPR", "XKAPP", "XKAPA")}
+    lt, lr, kr, kp, ka = analytic_opacity_table(1e-2)
+    keep = [np.ascontiguousarray(a) for a in (lt, lr)] + [np.asfortranarray(a) for a in (kr, kp, ka)]
+    lib = __import__("oracle")._load()
+    assert lib.ttor_set_opacity_table(o.h, lt.size, lr.size, *[a.ctypes.data for a in keep]) == 0
+    assert o.call("kappa") == 0
+    # inside the table's range (the ghosts below the shell, rho > 1e-2, are
+    # clamped to its edge as the reference clamps them)
+    rho = o.f("RH")
+    inside = (np.log10(rho) < -1.99994) & (np.log10(rho) > -11.9995)
+    for n, a in ref.items():
+        assert rel_l2(o.f(n)[inside], a[inside]) <= 1e-12, n
+    assert not np.all(inside)
+    # dkappa_P/dT: the table's finite difference at the bracketing T nodes
+    assert np.all(o.f("DXKAPP_DT")[2:-2, 2:-2, 2:-2] > 0)
+    # T <= 0 stops (pprphy.f:1037-1043)
+    o.f("T")[5, 5, 5] = -1.0
+    assert o.call("kappa") == -10

@@ -63,6 +63,12 @@ class RaddifParams(ctypes.Structure):
                 ("volzb", ctypes.c_void_p)]
 
 
+class OpacityTable(ctypes.Structure):
+    _fields_ = [("nt", ctypes.c_int32), ("nrh", ctypes.c_int32), ("log_t", ctypes.c_void_p),
+                ("log_rho", ctypes.c_void_p), ("log_ross", ctypes.c_void_p), ("log_plnk", ctypes.c_void_p),
+                ("log_abs", ctypes.c_void_p)]
+
+
 class Energy(ctypes.Structure):
     _fields_ = [(n, c_double) for n in ("volume", "e_rad", "e_gas", "heating", "flux_bottom", "flux_top",
                                         "flux_theta")]
@@ -95,7 +101,8 @@ GUESS = {"zero": 0, "previous": 1, "learned": 2}
 
 STATUS = {0: "ok", 1: "iteration limit reached", 2: "learned guess rejected",
           -1: "bad argument", -2: "CUDA error", -3: "configuration not implemented",
-          -7: "non-positive Q (CLEAN_STOP)", -8: "non-finite norm", -9: "no learned-guess model"}
+          -7: "non-positive Q (CLEAN_STOP)", -8: "non-finite norm", -9: "no learned-guess model",
+          -10: "opacity table: T <= 0 or outside the table"}
 
 EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_destroy",
            "ttfld_set_params", "ttfld_get_params", "ttfld_set_solver", "ttfld_upload",
@@ -109,7 +116,7 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
            "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums",
-           "ttfld_solve_with_hypre", "ttfld_raddif")
+           "ttfld_solve_with_hypre", "ttfld_raddif", "ttfld_set_opacity_table")
 
 _lib = None
 
@@ -158,6 +165,7 @@ def lib():
     L.ttfld_solve_system.argtypes = [vp, ctypes.POINTER(SolveStats)]
     L.ttfld_solve_with_hypre.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolveStats)]
     L.ttfld_raddif.argtypes = [vp, ctypes.POINTER(RaddifParams), ctypes.POINTER(SolveStats)]
+    L.ttfld_set_opacity_table.argtypes = [vp, ctypes.POINTER(OpacityTable)]
     L.ttfld_sor_sweeps.argtypes = [vp, ctypes.c_int, P_double, P_double]
     L.ttfld_true_residual.argtypes = [vp, P_double, P_double]
     L.ttfld_adjust_sor_param.argtypes = [vp, P_double]

@@ -31,9 +31,112 @@ __device__ __forceinline__ double kap_formula(const Dev& d, double t, double rh,
   return ((d.kap0 * sqrt(rh)) * (th * sqrt(th))) * kmul;
 }
 
+// The opacity table of kappa_model 2 in device memory: an error word, then
+// log10 T (nt), log10 rho (nrh) and the three log10 means (nt x nrh, T
+// index fastest).
+struct OpacTab {
+  int nt, nrh;
+  int* err;
+  const double *lt, *lrh, *ross, *plnk, *absk;
+};
+
+static OpacTab opac_tab(const ttfld_ctx* c) {
+  OpacTab t;
+  t.nt = c->opac_nt;
+  t.nrh = c->opac_nrh;
+  t.err = (int*)c->opac;
+  const double* p = (const double*)c->opac + 1;
+  t.lt = p; p += t.nt;
+  t.lrh = p; p += t.nrh;
+  t.ross = p; p += (size_t)t.nt * t.nrh;
+  t.plnk = p; p += (size_t)t.nt * t.nrh;
+  t.absk = p;
+  return t;
+}
+
+// BurrowsOPC (pprphy.f:1005-1229) for the Rosseland, Planck and absorption
+// means: log10 T and log10 rho clamped to the table's interior (REAL*4
+// literals, :1045-1049), the first node above each (:1050, :1087), weights
+// WS1/WS along T and WS2/WS3 along rho (:1081-1084, :1106-1109), 10^ of the
+// bilinear form (:1112-1135), the T-derivative stand-ins of :1180-1185.
+// Returns 0, or the reason the reference stops (1: T <= 0, 2: above the
+// table, 3: below it, 4: a non-positive opacity).
+__device__ __forceinline__ int burrows_opc(const OpacTab& tb, double t, double rh, double& kp, double& kr,
+                                           double& ka, double& dkp, double& dka) {
+  if (!(t > 0.0)) return 1;
+  double rh1 = log10(rh), tm1 = log10(t);
+  if (tm1 < (double)1.69896f) tm1 = (double)1.69897f;
+  if (tm1 > (double)3.69889f) tm1 = (double)3.69888f;
+  if (rh1 < (double)-11.9996f) rh1 = (double)-11.9995f;
+  if (rh1 > (double)-1.99993f) rh1 = (double)-1.99994f;
+  int it = 1;
+  while (it <= tb.nt && !(tb.lt[it - 1] > tm1)) ++it;
+  if (it == tb.nt + 1) return 2;
+  if (it == 1) return 3;
+  const int it1 = it - 1;
+  double ws1 = tb.lt[it1 - 1] - tm1;
+  double ws = tb.lt[it1 - 1] - tb.lt[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  int iw = 1;
+  while (iw <= tb.nrh && !(tb.lrh[iw - 1] > rh1)) ++iw;
+  if (iw == tb.nrh + 1) return 2;
+  if (iw == 1) return 3;
+  const int iw1 = iw - 1;
+  double ws2 = rh1 - tb.lrh[iw1 - 1];
+  double ws3 = tb.lrh[iw - 1] - tb.lrh[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+  const size_t n00 = (size_t)(it - 1) + (size_t)tb.nt * (iw - 1), n10 = (size_t)(it - 1) + (size_t)tb.nt * (iw1 - 1);
+  const size_t n11 = (size_t)(it1 - 1) + (size_t)tb.nt * (iw1 - 1), n01 = (size_t)(it1 - 1) + (size_t)tb.nt * (iw - 1);
+  auto interp = [&](const double* a) {
+    const double w4 = ws2 * (ws1 * a[n00] + ws * a[n01]);
+    const double w5 = ws3 * (ws1 * a[n10] + ws * a[n11]);
+    return pow(10.0, w4 + w5);
+  };
+  kr = interp(tb.ross);
+  kp = interp(tb.plnk);
+  ka = interp(tb.absk);
+  const double dt = pow(10.0, tb.lt[it - 1]) - pow(10.0, tb.lt[it1 - 1]);
+  dkp = (pow(10.0, tb.plnk[n00]) - pow(10.0, tb.plnk[n01])) / dt;
+  dka = (pow(10.0, tb.absk[n00]) - pow(10.0, tb.absk[n01])) / dt;
+  if (kr <= 0.0 || kp <= 0.0 || ka <= 0.0) return 4;
+  return 0;
+}
+
 static int kappa(ttfld_ctx* c) {
   Dev d = c->d;
   if (d.kappa_model == 1) return 0;  // prescribed opacities: KAPPA is the caller's
+  if (d.kappa_model == 2) {
+    if (!c->opac) {
+      fprintf(stderr, "ttfld: kappa_model 2 without an opacity table (ttfld_set_opacity_table)\n");
+      return TTFLD_E_OPACITY;
+    }
+    const OpacTab tb = opac_tab(c);
+    TT_CHECK(cudaMemsetAsync(tb.err, 0, sizeof(int), c->stream));
+    // cells from UPPERBND up take the values of UPPERBND-1 (pprphy.f:336-348)
+    launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+      int ub = PA(UB, j, k);
+      if (ub < 1 || ub > d.nx + 1) return;
+      size_t s = hidx(d, i < ub ? i : ub - 1, j, k);
+      size_t q = hidx(d, i, j, k);
+      double kp, kr, ka, dkp, dka;
+      const int e = burrows_opc(tb, d.T[s], d.RH[s], kp, kr, ka, dkp, dka);
+      if (e) atomicExch(tb.err, e);
+      d.XKAPR[q] = kr; d.XKAPP[q] = kp; d.XKAPA[q] = ka;
+      d.DXKAPP[q] = dkp; d.DXKAPA[q] = dka;
+    });
+    TT_CHECK_LAUNCH();
+    int err = 0;
+    TT_CHECK(cudaMemcpyAsync(&err, tb.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    if (err) {
+      fprintf(stderr, "ttfld: KAPPA from the opacity table stopped (reason %d: 1 T<=0, 2 above, 3 below the "
+                      "table, 4 non-positive opacity)\n", err);
+      return TTFLD_E_OPACITY;
+    }
+    return 0;
+  }
   // One thread per cell: the cells from UPPERBND up end with the value of
   // UPPERBND-1, which each of them evaluates itself (same inputs, same bits).
   launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
@@ -333,7 +436,11 @@ static int bounds(ttfld_ctx* c) {
     PA(UB, j, nz + 1) = PA(UB, j, nz); PA(UB, j, nz + 2) = PA(UB, j, nz);
   });
   TT_CHECK_LAUNCH();
-  // BOUNDXMIN(9)
+  // BOUNDXMIN(9); at III = 0 the opacity of cell (1,1,1) comes from the
+  // opacity table (ppbou.f:1040-1044) where kappa_model 2 has one, else from
+  // the analytic model
+  const bool tab = d.kappa_model == 2 && c->opac;
+  const OpacTab tb = tab ? opac_tab(c) : OpacTab{};
   launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
     double dtdr;
     if (d.ieta == 5) {
@@ -343,6 +450,10 @@ static int bounds(ttfld_ctx* c) {
                (4.0 * TT_ARAD * TT_FD * p3(HA(T, 1, j, k))));
     } else {
       double k111 = kap_formula(d, HA(T, 1, 1, 1), HA(RH, 1, 1, 1), HA(KMUL, 1, 1, 1));
+      if (tab) {
+        double kp, ka, dkp, dka;
+        if (burrows_opc(tb, HA(T, 1, 1, 1), HA(RH, 1, 1, 1), kp, k111, ka, dkp, dka)) atomicExch(tb.err, 5);
+      }
       dtdr = -(3.0 * d.fbottom * k111 * HA(RH, 1, 1, 1) / (4.0 * TT_ARAD * TT_FD * p3(HA(T, 1, 1, 1))));
     }
     HA(T, 0, j, k) = HA(T, 1, j, k) - dtdr * (G(xxb, 1) - G(xxb, 0));
@@ -427,6 +538,34 @@ int ttfld_stellarinput_heating(ttfld_ctx* c) {
   if (rc) return rc;
   TT_CHECK(cudaStreamSynchronize(c->stream));
   return 0;
+}
+
+int ttfld_set_opacity_table(ttfld_ctx* c, const ttfld_opacity_table* t) {
+  if (!c || !t || t->nt < 2 || t->nrh < 2 || !t->log_t || !t->log_rho || !t->log_ross || !t->log_plnk ||
+      !t->log_abs)
+    return TTFLD_E_ARGS;
+  const size_t nn = (size_t)t->nt * t->nrh;
+  const size_t bytes = (1 + (size_t)t->nt + t->nrh + 3 * nn) * sizeof(double);
+  TT_CHECK(cudaSetDevice(c->device));
+  if (c->opac) {
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->opac);
+    c->opac = nullptr;
+  }
+  TT_CHECK(cudaMalloc(&c->opac, bytes));
+  c->opac_nt = t->nt;
+  c->opac_nrh = t->nrh;
+  double* p = (double*)c->opac + 1;
+  TT_CHECK(cudaMemcpy(p, t->log_t, t->nt * sizeof(double), cudaMemcpyHostToDevice));
+  p += t->nt;
+  TT_CHECK(cudaMemcpy(p, t->log_rho, t->nrh * sizeof(double), cudaMemcpyHostToDevice));
+  p += t->nrh;
+  TT_CHECK(cudaMemcpy(p, t->log_ross, nn * sizeof(double), cudaMemcpyHostToDevice));
+  p += nn;
+  TT_CHECK(cudaMemcpy(p, t->log_plnk, nn * sizeof(double), cudaMemcpyHostToDevice));
+  p += nn;
+  TT_CHECK(cudaMemcpy(p, t->log_abs, nn * sizeof(double), cudaMemcpyHostToDevice));
+  return TTFLD_OK;
 }
 
 int ttfld_diff(ttfld_ctx* c, int energy_iter) {

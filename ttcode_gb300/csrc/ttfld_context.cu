@@ -139,7 +139,7 @@ int validate_params(const ttfld_params* p) {
   if (p->f_incident < 0 || p->f_incident > 5) return TTFLD_E_UNSUPPORTED;
   if (p->isigtyp != 0 && p->isigtyp != 1) return TTFLD_E_UNSUPPORTED;
   if (p->ibdrad != 4 && p->ibdrad != 7 && p->ibdrad != 9) return TTFLD_E_UNSUPPORTED;
-  if (p->kappa_model != 0 && p->kappa_model != 1) return TTFLD_E_UNSUPPORTED;
+  if (p->kappa_model < 0 || p->kappa_model > 2) return TTFLD_E_UNSUPPORTED;
   return 0;
 }
 
@@ -162,6 +162,7 @@ const char* ttfld_status_string(int s) {
     case TTFLD_E_NONPOSITIVE_Q: return "non-positive Q after the update (CLEAN_STOP)";
     case TTFLD_E_NONFINITE: return "non-finite norm";
     case TTFLD_E_NOMODEL: return "no learned-guess model loaded";
+    case TTFLD_E_OPACITY: return "opacity table: T <= 0, (T, rho) outside the table or a non-positive opacity";
   }
   return "unknown status";
 }
@@ -279,6 +280,7 @@ int ttfld_destroy(ttfld_ctx* c) {
   unet_free(c);
   mix_free(c);
   krylov_free(c);
+  if (c->opac) cudaFree(c->opac);
   if (c->prev_x) cudaFree(c->prev_x);
   if (c->guess_tmp) cudaFree(c->guess_tmp);
   if (c->slab) cudaFree(c->slab);

@@ -268,6 +268,8 @@ struct ttfld_ctx {
   double* prev_x;           // previous solution (halo)
   double* guess_tmp;        // scratch halo array of the first-sweep guess test
   void* krylov;             // PCG workspace (allocated on first use)
+  void* opac;               // opacity table of kappa_model 2 (device), with its sizes
+  int opac_nt, opac_nrh;
   double last_solve_ms;
 };
 

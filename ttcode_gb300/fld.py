@@ -170,6 +170,17 @@ class FLD:
         check("RADDIF", self.L.ttfld_raddif(self.h, ctypes.byref(p), ctypes.byref(st)), ok=(0, 1))
         return st
 
+    def set_opacity_table(self, log_t, log_rho, log_ross, log_plnk, log_abs):
+        """The (T, rho) opacity table kappa_model 2 interpolates (BurrowsOPC):
+        log10 nodes and log10 means, shape (len(log_t), len(log_rho))."""
+        keep = [np.ascontiguousarray(log_t, dtype=np.float64), np.ascontiguousarray(log_rho, dtype=np.float64)]
+        keep += [np.asfortranarray(a, dtype=np.float64) for a in (log_ross, log_plnk, log_abs)]
+        nt, nrh = keep[0].size, keep[1].size
+        if any(a.shape != (nt, nrh) for a in keep[2:]):
+            raise ValueError("opacity arrays must be (len(log_t), len(log_rho))")
+        t = _ffi.OpacityTable(nt, nrh, *[a.ctypes.data for a in keep])
+        check("ttfld_set_opacity_table", self.L.ttfld_set_opacity_table(self.h, ctypes.byref(t)))
+
     def sor_sweeps(self, n: int):
         r, b = ctypes.c_double(), ctypes.c_double()
         check("sor_sweeps", self.L.ttfld_sor_sweeps(self.h, n, ctypes.byref(r), ctypes.byref(b)))

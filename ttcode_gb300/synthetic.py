@@ -119,6 +119,19 @@ def make_shell(nx: int, ny: int, nz: int, seed: int = 0, delt: float = 100.0,
     return Shell(g, fields, params, seed)
 
 
+def analytic_opacity_table(kap0: float = 1e-2, nt: int = 50, nrh: int = 50):
+    """A table in BurrowsOPC's layout (log10 T, log10 rho nodes spanning the
+    range its clamps allow, pprphy.f:1045-1049; log10 means, T index
+    fastest) holding the analytic model kappa = kap0 sqrt(rho) (T/1000)^1.5
+    for all three means.  log10 kappa is linear in log10 T and log10 rho, so
+    the bilinear interpolation reproduces the model up to rounding."""
+    lt = np.linspace(1.69896, 3.69889, nt)
+    lr = np.linspace(-11.9996, -1.99993, nrh)
+    k = math.log10(kap0) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    k = np.asfortranarray(k)
+    return lt, lr, k, k.copy(order="F"), k.copy(order="F")
+
+
 def shell(name: str, seed: int = 0) -> Shell:
     cfg = SHELLS[name]
     return make_shell(cfg["nx"], cfg["ny"], cfg["nz"], seed=seed, delt=cfg["delt"],
