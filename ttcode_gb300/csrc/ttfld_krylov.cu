@@ -816,7 +816,11 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     if (total >= budget) { status = TTFLD_MAXITER; break; }
     // an anchor that does not halve the residual twice in a row: the
     // symmetric part is too far from the rows (or FP32 cannot resolve them)
-    if (ratio > 0.5 * prev && ++slow >= 2) { status = TTFLD_MAXITER; break; }
+    if (ratio > 0.5 * prev) {
+      if (++slow >= 2) { status = TTFLD_MAXITER; break; }
+    } else {
+      slow = 0;
+    }
     prev = ratio;
     double target = 0.3 * tol / ratio;
     if (target < kInnerReduce) target = kInnerReduce;
