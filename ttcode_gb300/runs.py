@@ -18,6 +18,9 @@ with its solver and initial guess:
     pcg_zero        FP32 conjugate gradients (radial line preconditioner) in
                     FP64 defect correction, zero guess
     pcg_previous    ... each step's first solve from the previous solution
+    pcg_learned     ... the run's first solve from the learned guess (kept if
+                    its preconditioned residual is below zero's), later ones
+                    from the previous solution
 
 One JSON line per variant: mean and total device time per step (CUDA events
 inside the library), outer iterations, solves, sweeps and fallbacks per step,
@@ -49,6 +52,7 @@ VARIANTS = {
     "mixed_learned": dict(solver="mixed", guess="learned"),
     "pcg_zero": dict(solver="pcg", guess="zero"),
     "pcg_previous": dict(solver="pcg", guess="previous"),
+    "pcg_learned": dict(solver="pcg", guess="learned"),
 }
 
 
@@ -159,7 +163,7 @@ def main(argv=None):
         s["variant"] = "reference_fp64_exact_1e-12"
         print(json.dumps({"config": args.config, **s}), flush=True)
     blob = None
-    if "mixed_learned" in names:
+    if "mixed_learned" in names or "pcg_learned" in names:
         lo, hi = (float(x) for x in args.dt_range.split(","))
         blob, info = train_guess(sh, args.pairs, args.epochs, args.lr, (lo, hi), args.steps_per_case)
         print(json.dumps({"config": args.config, "training": info}), flush=True)
