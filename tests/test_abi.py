@@ -62,7 +62,8 @@ def test_struct_layout_matches_c():
     from ttcode_gb300 import _ffi
     structs = {"ttfld_dims": _ffi.Dims, "ttfld_metrics": _ffi.Metrics, "ttfld_params": _ffi.Params,
                "ttfld_solve_opts": _ffi.SolveOpts, "ttfld_solve_stats": _ffi.SolveStats,
-               "ttfld_step_stats": _ffi.StepStats}
+               "ttfld_step_stats": _ffi.StepStats, "ttfld_energy": _ffi.Energy,
+               "ttfld_raddif_params": _ffi.RaddifParams, "ttfld_opacity_table": _ffi.OpacityTable}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
