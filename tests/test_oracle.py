@@ -510,3 +510,47 @@ def test_pcg_design_restated_on_the_cpu(shell):
     o.set("epsmat", 1e-10)
     assert o.call("solve_with_sor", 0, 0) == 0
     assert its < int(o.get("sor_iter")) // 2, (its, int(o.get("sor_iter")))
+
+
+def test_hypre_laplacian_toggle_known_answer():
+    """pphypre.f:251-258 (and ppenergy.f:1017-1025) turn the system into the
+    6/-1 Laplacian; with b = 1 (pphypre.f:136-137) FILLHYPREMATRIX /
+    FILLHYPREVECTORS must give the Laplacian whose boundary cells (i = 1,
+    i = NX, i >= upperbnd, k = 1, k = NZ) are identity rows with b = 0 and
+    whose phi direction ends at the grid (no periodic coupling), built here
+    independently."""
+    from oracle import Oracle
+    nx, ny, nz = 12, 8, 10
+    o = Oracle(nx, ny, nz)
+    for n in ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL8"):
+        o.f(n)[...] = 1.0
+    o.f("EVAL7")[...] = 6.0
+    o.f("EVAL_1_6")[...] = 0.0
+    o.f("UPPERBND")[...] = nx - 1
+    o.f("RHS_ER")[...] = 1.0
+    assert o.call("fill_hypre_system") == 0
+    A = hypre_matrix(o).toarray()
+    b = o.f("HYP_RHS").ravel(order="F")
+    idx = lambda i, j, k: (i - 1) + nx * ((j - 1) + ny * (k - 1))
+    n = nx * ny * nz
+    R = np.zeros((n, n))
+    rb = np.ones(n)
+    ub = nx - 1
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                r = idx(i, j, k)
+                if i == 1 or i >= ub or k == 1 or k == nz:
+                    R[r, r] = 1.0
+                    rb[r] = 0.0
+                    continue
+                R[r, r] = 6.0
+                for (ii, jj, kk) in ((i - 1, j, k), (i + 1, j, k), (i, j - 1, k), (i, j + 1, k), (i, j, k - 1),
+                                     (i, j, k + 1)):
+                    if not (1 <= jj <= ny):
+                        continue                       # outside hypre's grid
+                    if ii == 1 or ii >= ub or kk == 1 or kk == nz:
+                        continue                       # a boundary cell: its coupling is zeroed
+                    R[r, idx(ii, jj, kk)] = -1.0
+    assert np.array_equal(A, R)
+    assert np.array_equal(b, rb)
