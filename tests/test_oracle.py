@@ -554,3 +554,21 @@ def test_hypre_laplacian_toggle_known_answer():
                     R[r, idx(ii, jj, kk)] = -1.0
     assert np.array_equal(A, R)
     assert np.array_equal(b, rb)
+
+
+def test_raddif_uniform_state_is_a_fixed_point():
+    """RADDIF on an isothermal shell with a flat bottom (D_T = 0) and the top
+    held at the same temperature (IBDRAD = 4, Tirr = T): every row of SOLVMAT
+    is satisfied by the uniform E_R = arad T^4 (B E - RHS + sum of the
+    couplings times E = 0), so the solve stops at ITMIN = 5 iterations and
+    T comes back unchanged."""
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(16, 12, 10, seed=2, delt=100.0)
+    sh.fields["T"][...] = 1500.0
+    sh.fields["ER"][...] = 7.56596e-15 * 1500.0 ** 4
+    o = rad_oracle(sh, 4, 1e-10, 100)
+    o.set("tirr", 1500.0)
+    assert o.call("raddif", 0.0, 0.0, 1, 0) == 0
+    assert int(o.get("sor_iter")) == 5
+    assert o.get("global_rnorm") / o.get("global_rhsnorm") <= 1e-14
+    assert np.max(np.abs(o.f("T")[2:-2, 2:-2, 2:-2] - 1500.0)) <= 1e-9
