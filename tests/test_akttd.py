@@ -154,3 +154,32 @@ def test_step_driven_from_a_record(tmp_path):
         ctx.close()
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+
+
+def test_snapshot_of_a_device_state(sh, tmp_path):
+    """snapshot_of_fld takes what a context holds (through download) into the
+    records; with a stand-in for the context, checked on the CPU."""
+    nx, ny, nz = sh.dims
+    rng = np.random.default_rng(9)
+    arrays = {"T": sh.fields["T"], "RH": sh.fields["RH"], "ER": sh.fields["ER"],
+              "UPPERBND": np.full((ny + 4, nz + 4), nx - 1, dtype=np.int32),
+              "XKAPR": rng.random((nx + 4, ny + 4, nz + 4)), "XKAPA": rng.random((nx + 4, ny + 4, nz + 4)),
+              "XKAPP": rng.random((nx + 4, ny + 4, nz + 4)), "STELLARINPUT": rng.random((nx, ny + 4, nz + 4))}
+
+    class Ctx:
+        grid, params = sh.grid, sh.params
+
+        def download(self, name):
+            return np.asfortranarray(arrays[name])
+
+    s = A.snapshot_of_fld(Ctx(), zeit=5.0, num_iter=3)
+    f = tmp_path / "AKTTD"
+    A.write(str(f), s)
+    t = A.read(str(f))
+    assert (t.zeit, t.num_iter) == (5.0, 3)
+    assert np.array_equal(t.arrays["T"], sh.fields["T"])
+    assert np.array_equal(t.upperbnd, np.full((ny, nz), nx - 1))
+    assert np.array_equal(t.arrays["xkapP"], arrays["XKAPP"][2:nx + 2, 2:ny + 2, 2:nz + 2])
+    assert np.array_equal(t.arrays["STELLARINPUT"], arrays["STELLARINPUT"][:, 2:ny + 2, 2:nz + 2])
+    for n in ("flimx", "conv_flux1", "disfn"):
+        assert not t.arrays[n].any()

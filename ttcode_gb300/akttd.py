@@ -28,7 +28,8 @@ column-major, first index fastest.  `read` returns a `Snapshot`; `stitch`
 joins the files of a (phi, theta) decomposition by proc_coords; `grid_of`
 rebuilds GITTER's NCOSYS=2 metrics (ppinit.f:1028-1406) from the coordinate
 records; `shell_of` makes the state a `synthetic.Shell` that
-`fld.start_run` accepts, so that a ttcode state drives the solver.
+`fld.start_run` accepts, so that a ttcode state drives the solver;
+`snapshot_of_fld` writes a device state back as a record.
 """
 from __future__ import annotations
 
@@ -363,4 +364,32 @@ def snapshot_of(sh, zeit: float = 0.0, num_iter: int = 0, upperbnd=None) -> Snap
                   else np.asarray(upperbnd, dtype=np.int32))
     s.scalars = {n: 0.0 for n in SCALARS}
     s.ncosys = 2
+    return s
+
+
+def snapshot_of_fld(f, zeit: float = 0.0, num_iter: int = 0) -> Snapshot:
+    """A one-rank snapshot of a device state (an `fld.FLD`, or anything with
+    its `grid`, `params` and `download`): T, RH, ER and UPPERBND as PRINTOUT
+    writes them, and the interior records xkapR, xkapA, STELLARINPUT, xkapP
+    (ppprt.f:46-117; the records it has no counterpart for are zero)."""
+    g = f.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    s = Snapshot(nx, ny, nz, (nx, ny, nz), 1, 0, (0, 0, 0), (1, 1, 1), zeit, f.params["delt"], num_iter)
+    for name in COORDS:
+        lo = COORD_LO[name]
+        n = {"x": nx, "y": ny, "z": nz}[name[1]]
+        s.coords[name] = np.array([g.at(name, i) for i in range(lo, n + 3)])
+    for name in FIELDS3:
+        if name in ("RH", "T", "ER"):
+            s.arrays[name] = np.asfortranarray(f.download(name))
+        else:
+            s.arrays[name] = np.zeros(_shape(field_bounds(name, nx, ny, nz)), order="F")
+    s.upperbnd = np.asfortranarray(f.download("UPPERBND")[2:ny + 2, 2:nz + 2].astype(np.int32))
+    s.scalars = {n: 0.0 for n in SCALARS}
+    s.ncosys = 2
+    inner = lambda a: np.asfortranarray(a[2:nx + 2, 2:ny + 2, 2:nz + 2])
+    for rec, src in (("xkapR", "XKAPR"), ("xkapA", "XKAPA"), ("xkapP", "XKAPP")):
+        s.arrays[rec] = inner(f.download(src))
+    si = f.download("STELLARINPUT")                 # (1:NX, -1:NY+2, -1:NZ+2)
+    s.arrays["STELLARINPUT"] = np.asfortranarray(si[:, 2:ny + 2, 2:nz + 2])
     return s
