@@ -109,7 +109,7 @@ typedef struct {
   int32_t f_incident; /* F_INCIDENT, ipp:12 (0..5)                        */
   int32_t ieta;     /* IETA, ipp:8                                        */
   int32_t isigtyp;  /* ISIGTYP, ipp:10 (0, 1)                             */
-  int32_t iii;      /* the driver's step counter III                      */
+  int32_t iii;      /* the main program's step counter III                */
   int32_t adjust_sor; /* call ADJUST_SOR_PARAM where the reference would  */
   int32_t kappa_model; /* 0 = synthetic analytic (stand-in for the tables) */
                        /* 1 = prescribed: XKAP* are uploaded, KAPPA no-op  */

@@ -22,7 +22,7 @@ def have_gpu() -> bool:
 
 
 def oracle_from_shell(sh, eps=1e-10, itmax=200000, start=True):
-    """An oracle state loaded with a synthetic shell (and the driver's set-up
+    """An oracle state loaded with a synthetic shell (and the main program's set-up
     BOUNDS at III=0 followed by KAPPA when start=True)."""
     from oracle import Oracle
     from ttcode_gb300.grid import full_1d

@@ -233,7 +233,7 @@ class FLD:
 
 def start_run(shell, device: int = 0) -> FLD:
     """Context loaded with a synthetic shell and the initial BOUNDS/KAPPA of
-    the driver's set-up (pp.f:419-463): BOUNDS at III=0, then KAPPA."""
+    the main program's set-up (pp.f:419-463): BOUNDS at III=0, then KAPPA."""
     f = FLD(shell.grid, shell.params, device)
     f.load_shell(shell)
     f.set_params(iii=0)
