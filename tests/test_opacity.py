@@ -1,0 +1,210 @@
+"""The Burrows table reader (ttcode_gb300.opacity) against READBURROWSOPCTABLE
+(pprphy.f:1231-1541), the file selection of ppplanets.f:36-213 and the node
+grid of ppmod.f:735-757; a table file driving the oracle's KAPPA."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import oracle_from_shell, rel_l2
+from ttcode_gb300 import opacity as O
+from ttcode_gb300.synthetic import RGAS, make_shell
+
+
+def _random_table(rng, ikaptyp):
+    s = (O.NODES, O.NODES)
+    a = {n: rng.uniform(-4.0, 2.0, s) for n in ("plnk", "ross", "absk")}
+    for n in ("waveopac", "localwave", "local_bb"):
+        a[n] = rng.uniform(-4.0, 2.0, s + (O.WAVE_BINS,))
+    return a
+
+
+def test_nodes_are_the_single_precision_literals():
+    assert O.BURROWS_LOG_T.size == O.NODES and O.BURROWS_LOG_RHO.size == O.NODES
+    assert O.BURROWS_LOG_T[0] == float(np.float32(1.69896)) != 1.69896
+    assert O.BURROWS_LOG_RHO[-1] == float(np.float32(-1.99993))
+    assert np.all(np.diff(O.BURROWS_LOG_T) > 0) and np.all(np.diff(O.BURROWS_LOG_RHO) > 0)
+    # BurrowsOPC's clamps (pprphy.f:1045-1049) keep log T and log rho strictly
+    # inside the nodes, so the bracketing search never runs off either end
+    f = lambda x: float(np.float32(x))
+    assert O.BURROWS_LOG_T[0] < f(1.69897) and f(3.69888) < O.BURROWS_LOG_T[-1]
+    assert O.BURROWS_LOG_RHO[0] < f(-11.9995) and f(-1.99994) < O.BURROWS_LOG_RHO[-1]
+    # the nodes are the logs of the commented-out linear table (ppmod.f:714-733)
+    assert abs(10 ** O.BURROWS_LOG_T[-1] / 4999.04 - 1) < 1e-4
+    assert abs(10 ** O.BURROWS_LOG_RHO[0] / 1.00102e-12 - 1) < 1e-4
+
+
+def test_list_directed_reads():
+    rd = O.ListDirected([
+        "  header, with a comma\n",
+        "1.5 2.5d0\n",                 # a read of 4 continues on the next record
+        "3.0E+1, 4 9 9 9\n",           # ... and drops the rest of it
+        "2*7.0 ,, 1.0-3\n",            # repeat count, a null value, a signed exponent
+        "8.0 / 5.0\n",                 # a slash ends the read
+        "\n",                          # a blank record gives no value
+        "'quoted text' rest\n",
+    ])
+    assert rd.read_text() == "header"
+    assert rd.read(4) == [1.5, 2.5, 30.0, 4.0]
+    assert rd.read(4) == [7.0, 7.0, None, 1.0e-3]
+    assert rd.read(3) == [8.0, None, None]
+    assert rd.read_text() == "quoted text"
+    with pytest.raises(O.OpacityFileError):
+        rd.read(1)
+
+
+@pytest.mark.parametrize("ikaptyp", [10, 21, 23])
+def test_table_round_trip(tmp_path, ikaptyp):
+    a = _random_table(np.random.default_rng(ikaptyp), ikaptyp)
+    p = tmp_path / "t.dat"
+    O.write_burrows_table(p, ikaptyp, 5040.0, **a)
+    t = O.read_burrows_table(p, ikaptyp)
+    assert t.t_absorption == 5040.0 and t.ikaptyp == ikaptyp
+    for n in ("plnk", "ross", "absk"):
+        assert np.array_equal(getattr(t, n), a[n]), n
+    wave = ikaptyp in O.WAVELENGTH_TYPES
+    local = ikaptyp in O.LOCAL_WAVE_TYPES
+    assert np.array_equal(t.waveopac, a["waveopac"]) if wave else np.all(t.waveopac == O.MISSING)
+    for n in ("localwave", "local_bb"):
+        assert np.array_equal(getattr(t, n), a[n]) if local else np.all(getattr(t, n) == O.MISSING)
+    assert np.array_equal(t.log_t, O.BURROWS_LOG_T) and np.array_equal(t.log_rho, O.BURROWS_LOG_RHO)
+
+
+def test_records_may_span_lines_and_hold_null_values(tmp_path):
+    """List-directed records: a node's values split over two lines, and a
+    null value keeping the value of the record before it."""
+    a = _random_table(np.random.default_rng(7), 10)
+    p = tmp_path / "t.dat"
+    O.write_burrows_table(p, 10, 6070.0, **a)
+    lines = open(p).read().splitlines()
+    v = lines[11].split()
+    lines[11] = " ".join(v[:2])
+    lines.insert(12, " ".join(v[2:]) + " 123.0")
+    w = lines[13].split()
+    lines[13] = ", ".join(w[:3]) + ", , " + w[4]          # node (1, 2): the Rosseland mean is null
+    t = O.read_burrows_table(lines, 10)
+    assert np.array_equal(t.plnk, a["plnk"])
+    assert t.ross[0, 1] == a["ross"][0, 0]
+    ross = a["ross"].copy()
+    ross[0, 1] = a["ross"][0, 0]
+    assert np.array_equal(t.ross, ross)
+    with pytest.raises(O.OpacityFileError):
+        O.read_burrows_table(lines[:-1], 10)                 # a node short
+
+
+def test_type_adjustments(tmp_path):
+    rng = np.random.default_rng(3)
+    a = _random_table(rng, 25)
+    gamma, mu = 0.7, 2.3
+    p = tmp_path / "t.dat"
+    # 12: the absorption mean from the Planck mean and gamma; 14: Rosseland too
+    O.write_burrows_table(p, 12, 6000.0, **a)
+    t12 = O.read_burrows_table(p, 12, gamma_opc=gamma)
+    assert np.array_equal(t12.absk, a["plnk"] + 4.0 * math.log10(gamma))
+    assert np.array_equal(t12.ross, a["ross"])
+    O.write_burrows_table(p, 14, 6000.0, **a)
+    t14 = O.read_burrows_table(p, 14, gamma_opc=gamma)
+    assert np.array_equal(t14.ross, a["plnk"]) and np.array_equal(t14.absk, t12.absk)
+    # 11: the planet's extra absorber where the gas pressure is <= 0.03 bar
+    O.write_burrows_table(p, 11, 6000.0, **a)
+    t11 = O.read_burrows_table(p, 11, planet_num=2, mu_gas=mu)
+    T = 10.0 ** O.BURROWS_LOG_T[:, None]
+    R = 10.0 ** O.BURROWS_LOG_RHO[None, :]
+    low = (RGAS * T * R / mu) * 1e-6 <= float(np.float32(0.03))
+    assert 0 < low.sum() < low.size
+    kext = float(np.float32(0.035))
+    np.testing.assert_allclose(t11.absk[low], np.log10(10.0 ** a["absk"][low] + kext), rtol=0, atol=1e-14)
+    assert np.array_equal(t11.absk[~low], a["absk"][~low])
+    # 24: the extra absorber in the stellar bins only; 25: in the local bins too
+    O.write_burrows_table(p, 24, 6070.0, **a)
+    t24 = O.read_burrows_table(p, 24, planet_num=1)
+    kext = float(np.float32(0.1))
+    np.testing.assert_allclose(t24.waveopac, np.log10(10.0 ** a["waveopac"] + kext), rtol=0, atol=1e-14)
+    assert np.array_equal(t24.localwave, a["localwave"]) and np.array_equal(t24.absk, a["absk"])
+    O.write_burrows_table(p, 25, 5040.0, **a)
+    t25 = O.read_burrows_table(p, 25, planet_num=2)
+    kext = float(np.float32(0.035))
+    np.testing.assert_allclose(t25.localwave, np.log10(10.0 ** a["localwave"] + kext), rtol=0, atol=1e-14)
+    assert np.array_equal(t25.local_bb, a["local_bb"])
+    # SETPLANETKAPEXTRA stops for planets without a value
+    with pytest.raises(O.OpacityFileError):
+        O.read_burrows_table(p, 25, planet_num=6)
+
+
+def test_file_selection():
+    assert O.burrows_file_name(1, 21) == "BURROWS6070_woTiVO_wavelth.dat"
+    assert O.burrows_file_name(1, 24) == "BURROWS6070_woTiVO_radtransfer.dat"
+    assert O.burrows_file_name(1, 10) == "BURROWS6117_woutTiVO.dat"
+    assert O.burrows_file_name(1, 20) == "BURROWS6070_wTiVO_wavelth.dat"
+    assert O.burrows_file_name(1, 9) == "BURROWS6117_wTiVO.dat"
+    assert O.burrows_file_name(2, 25) == "BURROWS5040_Ray_woTiVO_radtransfer.dat"
+    assert O.burrows_file_name(2, 9) == "BURROWS5040_wTiVO.dat"
+    assert O.burrows_file_name(3, 21) == "BURROWS5226_woutTiVO.dat"
+    assert O.burrows_file_name(5, 23) == "BURROWS6300_woTiVO_radtransfer.dat"
+    assert O.burrows_file_name(8, 10) == "BURROWS6350_woutTiVO.dat"
+    for planet, kt in ((1, 22), (1, 13), (3, 9), (5, 10), (9, 10), (9, 20)):
+        with pytest.raises(O.OpacityFileError):
+            O.burrows_file_name(planet, kt)
+    assert O.bstar_file_name(2) == "BSTAR_WAVEBINS_TS5040.dat"
+    with pytest.raises(O.OpacityFileError):
+        O.bstar_file_name(3)
+    assert O.planet_kap_extra(1) == float(np.float32(0.1))
+
+
+def _write_bins(path, n, tstar=5040.0):
+    with open(path, "w") as fh:
+        fh.write("bins\nof the star\nin the wavelength bins\n")
+        fh.write(f"{tstar}\n{n}\n")
+        for i in range(n):
+            fh.write(f"{1.0 + i} {float(i) * 0.5 + 0.25!r}\n")
+
+
+def test_bstar_bins(tmp_path):
+    p = tmp_path / "b.dat"
+    _write_bins(p, O.WAVE_BINS)
+    tstar, bins = O.read_bstar_bins(p)
+    assert tstar == 5040.0 and np.array_equal(bins, np.arange(O.WAVE_BINS) * 0.5 + 0.25)
+    _write_bins(p, O.WAVE_BINS - 1)
+    with pytest.raises(O.OpacityFileError):
+        O.read_bstar_bins(p)
+
+
+def test_table_file_drives_kappa(tmp_path):
+    """The analytic opacity written as an IKAPTYP 21 file on the reference's
+    nodes, read back, set into the oracle's BurrowsOPC: KAPPA reproduces the
+    analytic model inside the table's range; FLD.set_burrows_table passes the
+    same arrays."""
+    sh = make_shell(20, 16, 8, seed=2, delt=100.0)
+    o = oracle_from_shell(sh, start=False)
+    o.f("KMUL")[...] = 1.0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    ref = {n: o.f(n).copy() for n in ("XKAPR", "XKAPP", "XKAPA")}
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    k = math.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    wave = np.zeros(k.shape + (O.WAVE_BINS,))
+    O.write_burrows_table(tmp_path / O.burrows_file_name(1, 21), 21, 6070.0, k, k, k, waveopac=wave)
+    _write_bins(tmp_path / O.bstar_file_name(1), O.WAVE_BINS, 6070.0)
+    t = O.read_opacity_tables(tmp_path, 1, 21)
+    assert t.bin_tstar == 6070.0 and t.bstar_bin.size == O.WAVE_BINS
+    keep = [np.ascontiguousarray(t.log_t), np.ascontiguousarray(t.log_rho)]
+    keep += [np.asfortranarray(x) for x in (t.ross, t.plnk, t.absk)]
+    lib = __import__("oracle")._load()
+    assert lib.ttor_set_opacity_table(o.h, O.NODES, O.NODES, *[x.ctypes.data for x in keep]) == 0
+    assert o.call("kappa") == 0
+    lrho, ltem = np.log10(o.f("RH")), np.log10(o.f("T"))
+    inside = (lrho < -1.99994) & (lrho > -11.9995) & (ltem > 1.69897) & (ltem < 3.69888)
+    assert inside.sum() > 0.5 * inside.size
+    for n, x in ref.items():
+        assert rel_l2(o.f(n)[inside], x[inside]) <= 1e-12, n
+
+    class Stand:                              # FLD without a device
+        def set_opacity_table(self, *arrays):
+            self.arrays = arrays
+    from ttcode_gb300.fld import FLD
+    s = Stand()
+    FLD.set_burrows_table(s, t)
+    assert [x is y for x, y in zip(s.arrays, (t.log_t, t.log_rho, t.ross, t.plnk, t.absk))] == [True] * 5
+    t.ikaptyp = 10
+    with pytest.raises(ValueError):
+        FLD.set_burrows_table(s, t)

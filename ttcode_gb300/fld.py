@@ -181,6 +181,14 @@ class FLD:
         t = _ffi.OpacityTable(nt, nrh, *[a.ctypes.data for a in keep])
         check("ttfld_set_opacity_table", self.L.ttfld_set_opacity_table(self.h, ctypes.byref(t)))
 
+    def set_burrows_table(self, table):
+        """A table of ``opacity.read_burrows_table`` for KAPPA's IKAPTYP 20:25
+        branch (pprphy.f:321-351; ``kappa_model`` 2): its nodes and its
+        Rosseland, Planck and absorption means."""
+        if table.ikaptyp not in (20, 21, 22, 23, 24, 25):
+            raise ValueError(f"IKAPTYP {table.ikaptyp}: the device implements KAPPA's 20:25 branch")
+        self.set_opacity_table(table.log_t, table.log_rho, table.ross, table.plnk, table.absk)
+
     def sor_sweeps(self, n: int):
         r, b = ctypes.c_double(), ctypes.c_double()
         check("sor_sweeps", self.L.ttfld_sor_sweeps(self.h, n, ctypes.byref(r), ctypes.byref(b)))

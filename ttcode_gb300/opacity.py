@@ -1,0 +1,386 @@
+"""Burrows (T, rho) opacity tables on the host: BurrowsOPC's node grid and the
+table files KAPPA's Burrows branches read.
+
+* ``BURROWS_LOG_T``, ``BURROWS_LOG_RHO``: the 50 + 50 interpolation nodes
+  (log10 K and log10 g/cm^3) of the module arrays BurrowsT / BurrowsRH
+  (ppmod.f:660, set by DATA statements at ppmod.f:735-757).  The DATA
+  constants are default REAL, so each node is the single-precision value of
+  its literal widened to double, as here.
+* ``read_burrows_table``: READBURROWSOPCTABLE (pprphy.f:1231-1505): ten
+  header records, the stellar temperature the absorption means were made
+  for, then one list-directed record per (T, rho) node, T outer, of 5
+  (IKAPTYP 9-14), 35 (20, 21) or 95 (22-25) values: T, rho, log10 of the
+  Planck, Rosseland and absorption means, then 30 stellar-wavelength bins,
+  30 local-wavelength bins and 30 local black-body weights.  Every array
+  starts at -7 (a missing value); the IKAPTYP 11, 12, 14, 20, 24, 25
+  adjustments follow the reads as in the reference.
+* ``read_bstar_bins``: the BSTAR_WAVEBINS file of the wavelength types
+  (pprphy.f:1507-1540).
+* ``burrows_file_name``, ``bstar_file_name``: the file a planet and IKAPTYP
+  open (OPENOPACITYFILE_WOTIOVO / OPENOPACITYFILE_WITH_TIOVO,
+  ppplanets.f:90-213; pprphy.f:1510-1527).
+* ``planet_kap_extra``: SETPLANETKAPEXTRA (ppplanets.f:36-59).
+* ``ListDirected``: the subset of Fortran list-directed input (``READ(u,*)``)
+  these files need: blank or comma separators, null values, ``r*c`` repeat
+  counts, ``/`` ending a read, D exponents; a read continues over records
+  until its items are filled and drops the rest of its last record.
+
+``FLD.set_burrows_table`` hands a table of the IKAPTYP 20:25 types to the
+device (``kappa_model`` 2).  The table files are not part of the reference
+tree; the tests write files in this layout.
+"""
+from __future__ import annotations
+
+import math
+import os
+import re
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .synthetic import RGAS
+
+WAVE_BINS = 30          # nwave_bins, ppmod.f:489
+NODES = 50              # BurrowsT(50), BurrowsRH(50), ppmod.f:660
+MISSING = -7.0          # pprphy.f:1285-1288
+
+# DATA BurrowsT / BurrowsRH, ppmod.f:735-757 (default-REAL constants)
+BURROWS_LOG_T = np.array([
+    1.69896, 1.73978, 1.78061, 1.82143, 1.86225, 1.90308, 1.94390, 1.98473, 2.02555, 2.06637,
+    2.10720, 2.14802, 2.18884, 2.22967, 2.27049, 2.31132, 2.35214, 2.39296, 2.43379, 2.47461,
+    2.51543, 2.55626, 2.59708, 2.63790, 2.67873, 2.71955, 2.76038, 2.80120, 2.84202, 2.88285,
+    2.92367, 2.96406, 3.00488, 3.04571, 3.08653, 3.12735, 3.16818, 3.20900, 3.24983, 3.29065,
+    3.33147, 3.37230, 3.41312, 3.45394, 3.49477, 3.53559, 3.57642, 3.61724, 3.65806, 3.69889,
+], dtype=np.float32).astype(np.float64)
+BURROWS_LOG_RHO = np.array([
+    -11.9996, -11.7954, -11.5913, -11.3872, -11.1831, -10.9790, -10.7748, -10.5707, -10.3666, -10.1625,
+    -9.95837, -9.75425, -9.55014, -9.34602, -9.14190, -8.93778, -8.73366, -8.52954, -8.32543, -8.12131,
+    -7.91719, -7.71307, -7.50895, -7.30483, -7.10071, -6.89660, -6.69248, -6.48836, -6.28424, -6.08012,
+    -5.87600, -5.67189, -5.46777, -5.26365, -5.05953, -4.85541, -4.65129, -4.44718, -4.24479, -4.04068,
+    -3.83656, -3.63244, -3.42875, -3.22464, -3.02052, -2.81640, -2.61228, -2.40816, -2.20404, -1.99993,
+], dtype=np.float32).astype(np.float64)
+
+WITH_TIOVO = (9, 20)                               # pprphy.f:1273
+WITHOUT_TIOVO = (10, 11, 12, 14, 21, 23, 24, 25)   # pprphy.f:1275-1277
+WAVELENGTH_TYPES = (20, 21, 22, 23, 24, 25)        # pprphy.f:1299-1301, 1508-1509
+LOCAL_WAVE_TYPES = (22, 23, 24, 25)                # pprphy.f:1363-1364
+
+
+def _f32(x: float) -> float:
+    return float(np.float32(x))
+
+
+class OpacityFileError(ValueError):
+    """A table the reference's reader would stop on (clean_stop or a Fortran
+    runtime error)."""
+
+
+# ---- list-directed input ---------------------------------------------------
+_NULL = object()
+_SLASH = object()
+_EXP = re.compile(r"^([+-]?(?:\d+\.?\d*|\.\d+))([+-]\d+)$")
+
+
+def _tokens(record: str):
+    """Values of one record: strings, _NULL for an empty value between
+    commas, _SLASH for a slash (which ends the read)."""
+    out, i, n = [], 0, len(record)
+    after_value = False
+    while True:
+        while i < n and record[i] in " \t":
+            i += 1
+        if i >= n:
+            break
+        ch = record[i]
+        if ch == ",":
+            if not after_value:
+                out.append(_NULL)
+            after_value = False
+            i += 1
+            continue
+        if ch == "/":
+            out.append(_SLASH)
+            break
+        if ch in "'\"":
+            j, s = i + 1, []
+            while j < n:
+                if record[j] == ch:
+                    if j + 1 < n and record[j + 1] == ch:
+                        s.append(ch)
+                        j += 2
+                        continue
+                    break
+                s.append(record[j])
+                j += 1
+            out.append("".join(s))
+            i = j + 1
+        else:
+            j = i
+            while j < n and record[j] not in " \t,/":
+                j += 1
+            tok = record[i:j]
+            m = re.match(r"^(\d+)\*(.*)$", tok)
+            if m:
+                reps, val = int(m.group(1)), m.group(2)
+                out.extend([val if val else _NULL] * reps)
+            else:
+                out.append(tok)
+            i = j
+        after_value = True
+    return out
+
+
+def _real(tok: str) -> float:
+    t = tok.translate(str.maketrans("dDqQ", "eeee"))
+    try:
+        return float(t)
+    except ValueError:
+        m = _EXP.match(t)
+        if not m:
+            raise OpacityFileError(f"not a real number: {tok!r}") from None
+        return float(f"{m.group(1)}e{m.group(2)}")
+
+
+class ListDirected:
+    """Sequential list-directed reads over the records of a text file."""
+
+    def __init__(self, lines, name: str = "<table>"):
+        self.lines = list(lines)
+        self.pos = 0
+        self.name = name
+
+    def _record(self):
+        if self.pos >= len(self.lines):
+            raise OpacityFileError(f"{self.name}: end of file at record {self.pos + 1}")
+        rec = self.lines[self.pos].rstrip("\r\n")
+        self.pos += 1
+        return rec
+
+    def read(self, n: int, conv=_real):
+        """Up to n values; None where the input gave a null value or a slash
+        ended the read (the Fortran variable keeps its value there)."""
+        vals = []
+        while len(vals) < n:
+            toks = _tokens(self._record())
+            for t in toks:
+                if t is _SLASH:
+                    return vals + [None] * (n - len(vals))
+                vals.append(None if t is _NULL else conv(t))
+                if len(vals) == n:
+                    break
+        return vals
+
+    def read_text(self, length: int = 20) -> str:
+        """One character item (``character text*20``); a blank record
+        counts as no value, so the read moves on to the next record."""
+        v = self.read(1, conv=str)[0]
+        return "" if v is None else v[:length]
+
+
+# ---- file selection ----------------------------------------------------------
+def planet_kap_extra(planet_num: int) -> float:
+    """SETPLANETKAPEXTRA (ppplanets.f:36-59): the extra absorber in cm^2/g
+    (default-REAL constants)."""
+    table = {1: 0.1, 2: 0.035, 3: 0.0, 4: 0.0, 5: 0.0}
+    if planet_num not in table:
+        raise OpacityFileError(f"planet_num notavail:readbur,extra {planet_num}")
+    return _f32(table[planet_num])
+
+
+def burrows_file_name(planet_num: int, ikaptyp: int) -> str:
+    """The table file READBURROWSOPCTABLE opens (pprphy.f:1273-1282 with
+    ppplanets.f:90-213)."""
+    if ikaptyp in WITH_TIOVO:
+        if planet_num == 1:
+            return "BURROWS6070_wTiVO_wavelth.dat" if ikaptyp == 20 else "BURROWS6117_wTiVO.dat"
+        if planet_num == 2:
+            return "BURROWS5040_wTiVO.dat"
+        if 3 <= planet_num <= 8:
+            raise OpacityFileError(f"no w/TiVO opacity file created for this planet {planet_num}")
+        raise OpacityFileError(f"planet_num not avail {planet_num}")
+    if ikaptyp not in WITHOUT_TIOVO:
+        raise OpacityFileError(f"ikaptyp= {ikaptyp} not avail in readburrowsopctable")
+    if planet_num == 1:
+        if ikaptyp == 21:
+            return "BURROWS6070_woTiVO_wavelth.dat"
+        if ikaptyp in (23, 24):
+            return "BURROWS6070_woTiVO_radtransfer.dat"
+        return "BURROWS6117_woutTiVO.dat"
+    if planet_num == 2:
+        if ikaptyp == 21:
+            return "BURROWS5040_woTiVO_wavelth.dat"
+        if ikaptyp in (23, 24):
+            return "BURROWS5040_woTiVO_radtransfer.dat"
+        if ikaptyp == 25:
+            return "BURROWS5040_Ray_woTiVO_radtransfer.dat"
+        return "BURROWS5040_woutTiVO.dat"
+    if planet_num == 5:
+        if ikaptyp == 21:
+            return "BURROWS6300_woTiVO_wavelth.dat"
+        if ikaptyp in (23, 24):
+            return "BURROWS6300_woTiVO_radtransfer.dat"
+        raise OpacityFileError("check opacity file for WASP-12b")
+    fixed = {3: "BURROWS5226_woutTiVO.dat", 4: "BURROWS6147_woutTiVO.dat", 6: "BURROWS6079_woutTiVO.dat",
+             7: "BURROWS6290_woutTiVO.dat", 8: "BURROWS6350_woutTiVO.dat"}
+    if planet_num in fixed:
+        return fixed[planet_num]
+    raise OpacityFileError(f"planet_num not avail {planet_num}")
+
+
+def bstar_file_name(planet_num: int) -> str:
+    """The stellar wavelength-bin file of the wavelength types
+    (pprphy.f:1510-1527)."""
+    names = {1: "BSTAR_WAVEBINS_TS6070.dat", 2: "BSTAR_WAVEBINS_TS5040.dat", 5: "BSTAR_WAVEBINS_TS6300.dat"}
+    if planet_num not in names:
+        raise OpacityFileError("Need to create a BSTAR_WAVEBIN file for this Tstar")
+    return names[planet_num]
+
+
+# ---- the table -----------------------------------------------------------------
+def _values_per_record(ikaptyp: int) -> int:
+    if ikaptyp in (20, 21):
+        return 5 + WAVE_BINS
+    if ikaptyp in LOCAL_WAVE_TYPES:
+        return 5 + 3 * WAVE_BINS
+    return 5
+
+
+@dataclass
+class BurrowsTable:
+    """The arrays READBURROWSOPCTABLE fills (ppmod.f:660-666): log10 means in
+    cm^2/g, index [T node, rho node] (and [..., bin])."""
+    ikaptyp: int
+    t_absorption: float
+    plnk: np.ndarray
+    ross: np.ndarray
+    absk: np.ndarray
+    waveopac: np.ndarray
+    localwave: np.ndarray
+    local_bb: np.ndarray
+    bin_tstar: float | None = None
+    bstar_bin: np.ndarray | None = None
+    log_t: np.ndarray = field(default_factory=lambda: BURROWS_LOG_T.copy())
+    log_rho: np.ndarray = field(default_factory=lambda: BURROWS_LOG_RHO.copy())
+
+
+def _add_absorber(v: float, kap_ext: float) -> float:
+    # LOG10(10.d0**v + kap_ext), pprphy.f:1451-1454, 1467-1470, 1482-1489
+    return math.log10(math.pow(10.0, v) + kap_ext)
+
+
+def read_burrows_table(source, ikaptyp: int, planet_num: int = 1, gamma_opc: float = 1.0,
+                       mu_gas: float = 2.3) -> BurrowsTable:
+    """READBURROWSOPCTABLE's table part (pprphy.f:1283-1505).  ``source`` is
+    a path or the file's lines; ``gamma_opc`` and ``mu_gas`` are the input
+    file's gamma_OPC and mu_gas (ppmod.f:52-53)."""
+    if ikaptyp not in WITH_TIOVO + WITHOUT_TIOVO:
+        raise OpacityFileError(f"ikaptyp= {ikaptyp} not avail in readburrowsopctable")
+    if isinstance(source, (str, os.PathLike)):
+        with open(source) as fh:
+            lines, name = fh.readlines(), os.fspath(source)
+    else:
+        lines, name = list(source), "<table>"
+    rd = ListDirected(lines, name)
+    shape = (NODES, NODES)
+    plnk, ross, absk = (np.full(shape, MISSING) for _ in range(3))
+    wave, lwave, lbb = (np.full(shape + (WAVE_BINS,), MISSING) for _ in range(3))
+    for _ in range(10):
+        rd.read_text()
+    t_abs = rd.read(1)[0]
+    if t_abs is None:
+        raise OpacityFileError(f"{name}: no value for T_star")
+    nval = _values_per_record(ikaptyp)
+    held = [None] * nval          # a null value keeps the variable's last value
+    kap_ext = planet_kap_extra(planet_num) if ikaptyp in (11, 20, 24, 25) else 0.0
+    gamma_term = 4.0 * math.log10(gamma_opc) if ikaptyp in (12, 14) else 0.0
+    for it in range(NODES):
+        for ir in range(NODES):
+            vals = rd.read(nval)
+            for m, v in enumerate(vals):
+                if v is not None:
+                    held[m] = v
+            if any(v is None for v in held):
+                raise OpacityFileError(f"{name}: undefined value in the record of node ({it + 1}, {ir + 1})")
+            t_read, rh_read, kp, kr, ka = held[:5]
+            plnk[it, ir], ross[it, ir], absk[it, ir] = kp, kr, ka
+            if ikaptyp in WAVELENGTH_TYPES:
+                wave[it, ir, :] = held[5:5 + WAVE_BINS]
+                if ikaptyp in LOCAL_WAVE_TYPES:
+                    lwave[it, ir, :] = held[5 + WAVE_BINS:5 + 2 * WAVE_BINS]
+                    lbb[it, ir, :] = held[5 + 2 * WAVE_BINS:5 + 3 * WAVE_BINS]
+            if ikaptyp in (12, 14):                     # pprphy.f:1434-1437
+                absk[it, ir] = kp + gamma_term
+            if ikaptyp == 14:                           # pprphy.f:1438-1440
+                ross[it, ir] = kp
+            if ikaptyp == 11:                           # pprphy.f:1442-1456
+                pg_test = (RGAS * t_read * rh_read / mu_gas) * 1e-6
+                if pg_test <= _f32(0.03):
+                    absk[it, ir] = _add_absorber(absk[it, ir], kap_ext)
+            if ikaptyp in (20, 24, 25):                 # pprphy.f:1458-1490
+                wave[it, ir, :] = [_add_absorber(v, kap_ext) for v in wave[it, ir, :]]
+            if ikaptyp == 25:
+                lwave[it, ir, :] = [_add_absorber(v, kap_ext) for v in lwave[it, ir, :]]
+    return BurrowsTable(ikaptyp, t_abs, plnk, ross, absk, wave, lwave, lbb)
+
+
+def read_bstar_bins(source, nwave_bins: int = WAVE_BINS):
+    """The BSTAR_WAVEBINS file (pprphy.f:1528-1539): three header records,
+    the stellar temperature, the bin count (which must equal nwave_bins),
+    then one record per bin whose second value is kept."""
+    if isinstance(source, (str, os.PathLike)):
+        with open(source) as fh:
+            lines, name = fh.readlines(), os.fspath(source)
+    else:
+        lines, name = list(source), "<bins>"
+    rd = ListDirected(lines, name)
+    for _ in range(3):
+        rd.read_text()
+    tstar = rd.read(1)[0]
+    nbin = rd.read(1, conv=int)[0]
+    if nbin != nwave_bins:
+        raise OpacityFileError("Some problem with the number of bins in file")
+    bins = np.empty(nwave_bins)
+    held = [None, None]
+    for i in range(nwave_bins):
+        for m, v in enumerate(rd.read(2)):
+            if v is not None:
+                held[m] = v
+        if held[1] is None:
+            raise OpacityFileError(f"{name}: undefined value in bin {i + 1}")
+        bins[i] = held[1]
+    return tstar, bins
+
+
+def read_opacity_tables(directory, planet_num: int, ikaptyp: int, gamma_opc: float = 1.0,
+                        mu_gas: float = 2.3) -> BurrowsTable:
+    """READBURROWSOPCTABLE as a whole: the planet's table file from
+    ``directory`` and, for the wavelength types, its BSTAR bins."""
+    t = read_burrows_table(os.path.join(directory, burrows_file_name(planet_num, ikaptyp)), ikaptyp,
+                           planet_num, gamma_opc, mu_gas)
+    if ikaptyp in WAVELENGTH_TYPES:
+        t.bin_tstar, t.bstar_bin = read_bstar_bins(os.path.join(directory, bstar_file_name(planet_num)))
+    return t
+
+
+def write_burrows_table(path, ikaptyp: int, t_absorption: float, plnk, ross, absk, waveopac=None,
+                        localwave=None, local_bb=None, header=None):
+    """A table file in the layout read_burrows_table reads: node values
+    written as T and rho in cgs (10**node), means as given (log10), every
+    value with 17 significant digits."""
+    nval = _values_per_record(ikaptyp)
+    hdr = list(header or [f"table{i + 1}" for i in range(10)])
+    if len(hdr) != 10:
+        raise ValueError("the header is ten records")
+    with open(path, "w") as fh:
+        for h in hdr:
+            fh.write(f"{h}\n")
+        fh.write(f"{t_absorption!r}\n")
+        for it in range(NODES):
+            for ir in range(NODES):
+                row = [10.0 ** BURROWS_LOG_T[it], 10.0 ** BURROWS_LOG_RHO[ir], plnk[it, ir], ross[it, ir],
+                       absk[it, ir]]
+                if nval > 5:
+                    row += list(waveopac[it, ir, :])
+                if nval > 5 + WAVE_BINS:
+                    row += list(localwave[it, ir, :]) + list(local_bb[it, ir, :])
+                fh.write(" ".join(f"{float(v):.17g}" for v in row) + "\n")
