@@ -183,3 +183,178 @@ def test_snapshot_of_a_device_state(sh, tmp_path):
     assert np.array_equal(t.arrays["STELLARINPUT"], arrays["STELLARINPUT"][:, 2:ny + 2, 2:nz + 2])
     for n in ("flimx", "conv_flux1", "disfn"):
         assert not t.arrays[n].any()
+
+
+# ---- the global restart file (PRINTGLOBAL / READRESTART) ---------------------
+def _full_snapshot(sh):
+    s = A.snapshot_of(sh, zeit=2.5, num_iter=11)
+    rng = np.random.default_rng(12)
+    for n in ("V", "G", "H", "PG", "CS"):
+        s.arrays[n] = np.asfortranarray(rng.random(s.arrays[n].shape))
+    for n in A.EXTRAS:
+        s.arrays[n] = np.asfortranarray(rng.random((s.nx, s.ny, s.nz)))
+    s.upperbnd = np.asfortranarray(rng.integers(2, s.nx, (s.ny, s.nz)).astype(np.int32))
+    s.scalars = {n: float(q + 1) for q, n in enumerate(A.SCALARS)}
+    return s
+
+
+def _inner(s, name):
+    (li, _), (lj, _), (lk, _) = A.field_bounds(name, s.nx, s.ny, s.nz)
+    return s.arrays[name][1 - li:1 - li + s.nx, 1 - lj:1 - lj + s.ny, 1 - lk:1 - lk + s.nz]
+
+
+def test_restart_record_layout(sh, tmp_path):
+    """PRINTGLOBAL's records (ppcombine.f:607-657), the first twenty of which
+    READRESTART reads (ppinit.f:1566-1598)."""
+    s = _full_snapshot(sh)
+    g = A.combine([s])
+    f = tmp_path / "AKTTD"
+    A.write_restart(str(f), g)
+    r = _raw_records(str(f))
+    nx, ny, nz = 12, 16, 8
+    n3 = 8 * nx * ny * nz
+    assert [struct.unpack("<i", r[q])[0] for q in range(3)] == [nx, ny, nz]
+    assert struct.unpack("<4i", r[3]) == (nx, ny, nz, 1)
+    assert struct.unpack("<2di", r[4]) == (2.5, 100.0, 11)
+    assert [len(r[q]) for q in (5, 6, 7)] == [8 * nx, 8 * ny, 8 * nz]
+    assert np.array_equal(np.frombuffer(r[5], "<f8"), s.coords["xxb"][2:nx + 2])
+    assert all(len(r[q]) == n3 for q in range(8, 16))
+    T = np.frombuffer(r[12], "<f8").reshape((nx, ny, nz), order="F")
+    assert np.array_equal(T, sh.fields["T"][2:-2, 2:-2, 2:-2])
+    assert np.array_equal(np.frombuffer(r[15], "<f8").reshape((nx, ny, nz), order="F"), _inner(s, "CS"))
+    assert np.array_equal(np.frombuffer(r[16], "<i4").reshape((ny, nz), order="F"), s.upperbnd)
+    assert struct.unpack("<6d", r[17]) == (1.0, 2.0, 3.0, 4.0, 5.0, 6.0)
+    assert struct.unpack("<i", r[18]) == (2,)
+    assert len(r) == 19 + 9 and all(len(x) == n3 for x in r[19:])
+    # the extras by position; xkapP is written as zero (ppcombine.f:706-707)
+    assert np.array_equal(np.frombuffer(r[21], "<f8").reshape((nx, ny, nz), order="F"), s.arrays["conv_flux1"])
+    assert np.array_equal(np.frombuffer(r[26], "<f8").reshape((nx, ny, nz), order="F"), s.arrays["disfn"])
+    assert not np.frombuffer(r[27], "<f8").any()
+
+
+@pytest.mark.parametrize("max_sub", [2**31 - 1, 999])
+def test_restart_round_trip(sh, tmp_path, max_sub):
+    g = A.combine([_full_snapshot(sh)])
+    f = tmp_path / "AKTTD"
+    A.write_restart(str(f), g, max_sub=max_sub)
+    t = A.read_restart(str(f))
+    assert (t.nx, t.ny, t.nz, t.loc_dims, t.numprocs, t.zeit, t.delt, t.num_iter, t.ncosys) == \
+        (12, 16, 8, (12, 16, 8), 1, 2.5, 100.0, 11, 2)
+    for n in ("xxb", "xyb", "xzb"):
+        assert np.array_equal(t.xb[n], g.xb[n]), n
+    for n in A.GLOBAL3 + A.GLOBAL_EXTRAS:
+        assert np.array_equal(t.arrays[n], g.arrays[n]), n
+    assert np.array_equal(t.upperbnd, g.upperbnd) and t.scalars == g.scalars
+    # the twenty records a restart reads are a complete file too
+    g.ncosys = None
+    A.write_restart(str(f), g)
+    t = A.read_restart(str(f))
+    assert t.ncosys is None and set(t.arrays) == set(A.GLOBAL3)
+
+
+def test_ascii_restart(sh, tmp_path):
+    """AKTTD_ASCII (ppinit.f:1599-1632): the same items, list-directed; a
+    READ spans as many lines as its items need."""
+    g = A.combine([_full_snapshot(sh)])
+    f = tmp_path / "AKTTD_ASCII"
+
+    def vals(a, fmt="{!r}"):
+        flat = np.ravel(a, order="F")
+        return "\n".join(" ".join(fmt.format(v.item()) for v in flat[q:q + 5]) for q in range(0, flat.size, 5))
+
+    with open(f, "w") as fh:
+        fh.write(f"{g.nx}\n{g.ny}\n{g.nz}\n")
+        fh.write(" ".join(str(v) for v in (*g.loc_dims, g.numprocs)) + "\n")
+        fh.write(f"{g.zeit!r}, {g.delt!r} {g.num_iter}\n")
+        for n in ("xxb", "xyb", "xzb"):
+            fh.write(vals(g.xb[n], "{:.17E}").replace("E", "D") + "\n")
+        for n in A.GLOBAL3:
+            fh.write(vals(g.arrays[n]) + "\n")
+        fh.write(vals(g.upperbnd, "{}") + "\n")
+        fh.write(" ".join(repr(g.scalars[n]) for n in A.SCALARS) + "\n")
+    t = A.read_restart_ascii(str(f))
+    assert (t.nx, t.ny, t.nz, t.zeit, t.delt, t.num_iter) == (12, 16, 8, 2.5, 100.0, 11)
+    for n in ("xxb", "xyb", "xzb"):
+        assert np.array_equal(t.xb[n], g.xb[n]), n
+    for n in A.GLOBAL3:
+        assert np.array_equal(t.arrays[n], g.arrays[n]), n
+    assert np.array_equal(t.upperbnd, g.upperbnd) and t.scalars == g.scalars
+
+
+def _split_radial(s, px):
+    """Per-rank snapshots of a radial split into px ranks (interior and
+    coordinates; ppcombine joins interiors only)."""
+    out = []
+    lx = s.nx // px
+    for cx in range(px):
+        p = A.Snapshot(lx, s.ny, s.nz, s.global_dims, px, cx, (cx, 0, 0), (px, 1, 1), s.zeit, s.delt,
+                       s.num_iter)
+        p.scalars, p.ncosys = dict(s.scalars), s.ncosys
+        for name in A.COORDS:
+            lo = A.COORD_LO[name]
+            a = s.coords[name]
+            p.coords[name] = (np.array([a[cx * lx + l - lo] for l in range(lo, lx + 3)]) if name[1] == "x"
+                              else a.copy())
+        for name, a in s.arrays.items():
+            if name in A.EXTRAS:
+                p.arrays[name] = np.asfortranarray(a[cx * lx:(cx + 1) * lx])
+                continue
+            b = A.field_bounds(name, lx, s.ny, s.nz)
+            (li, _), (lj, _), (lk, _) = b
+            sub = np.zeros(A._shape(b), order="F")
+            sub[1 - li:1 - li + lx, 1 - lj:1 - lj + s.ny, 1 - lk:1 - lk + s.nz] = \
+                _inner(s, name)[cx * lx:(cx + 1) * lx]
+            p.arrays[name] = sub
+        p.upperbnd = s.upperbnd.copy(order="F")
+        out.append(p)
+    return out
+
+
+@pytest.mark.parametrize("split", ["phi_theta", "radial"])
+def test_combine_joins_the_ranks(sh, tmp_path, split):
+    """ppcombine's FILLGLOBAL over the ranks' files equals the one-rank
+    combine (a radial split included, which ppcombine allows)."""
+    s = _full_snapshot(sh)
+    whole = A.combine([s])
+    parts = _split(s, 2, 2) if split == "phi_theta" else _split_radial(s, 3)
+    read_back = []
+    for q, p in enumerate(parts):
+        f = tmp_path / f"AKTTD_{q:03d}"
+        A.write(str(f), p)
+        read_back.append(A.read(str(f)))
+    g = A.combine(read_back[::-1])
+    for n in ("xxb", "xyb", "xzb"):
+        assert np.array_equal(g.xb[n], whole.xb[n]), n
+    for n in A.GLOBAL3 + A.GLOBAL_EXTRAS:
+        assert np.array_equal(g.arrays[n], whole.arrays[n]), n
+    assert np.array_equal(g.upperbnd, whole.upperbnd)
+    with pytest.raises(ValueError):
+        A.combine(read_back[1:])
+
+
+def test_restart_drives_the_step(tmp_path):
+    """A state written as AKTTD and restarted (READRESTART, LOCALINIT's copy,
+    BOUNDS) takes the same implicit step as the state itself, bit for bit,
+    in the oracle; the ghost values the file does not hold are rebuilt or
+    never read.  The state's RH below the bottom holds RH(1), the value the
+    restart gives it."""
+    from conftest import oracle_from_shell
+    s0 = make_shell(16, 24, 12, seed=3, delt=100.0)
+    s0.fields["KMUL"][...] = 1.0
+    rh = s0.fields["RH"]
+    rh[0], rh[1] = rh[2], rh[2]
+    f = tmp_path / "AKTTD"
+    A.write_restart(str(f), A.combine([A.snapshot_of(s0)]))
+    s1 = A.shell_of_restart(A.read_restart(str(f)), s0.grid)
+    for n in ("T", "RH", "ER"):
+        assert np.array_equal(s1.fields[n][2:-2, 2:-2, 2:-2], s0.fields[n][2:-2, 2:-2, 2:-2])
+    assert not np.array_equal(s1.fields["ER"], s0.fields["ER"])       # the ghosts differ
+    o0, o1 = oracle_from_shell(s0, eps=1e-12), oracle_from_shell(s1, eps=1e-12)
+    assert o0.call("coupled_energy_eqs", 1) == 0 and o1.call("coupled_energy_eqs", 1) == 0
+    assert o0.get("energy_iter") == o1.get("energy_iter")
+    for n in ("T", "ER"):
+        assert np.array_equal(o0.f(n)[2:-2, 2:-2, 2:-2], o1.f(n)[2:-2, 2:-2, 2:-2]), n
+    # the grid comes from the run's parameters; a different one is refused
+    from ttcode_gb300.grid import gitter
+    with pytest.raises(ValueError):
+        A.shell_of_restart(A.read_restart(str(f)), gitter(16, 24, 12, 1.0e9, 1.2e9))

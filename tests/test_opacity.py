@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from conftest import oracle_from_shell, rel_l2
+from ttcode_gb300 import fortio
 from ttcode_gb300 import opacity as O
 from ttcode_gb300.synthetic import RGAS, make_shell
 
@@ -35,7 +36,7 @@ def test_nodes_are_the_single_precision_literals():
 
 
 def test_list_directed_reads():
-    rd = O.ListDirected([
+    rd = fortio.ListDirected([
         "  header, with a comma\n",
         "1.5 2.5d0\n",                 # a read of 4 continues on the next record
         "3.0E+1, 4 9 9 9\n",           # ... and drops the rest of it
@@ -49,7 +50,13 @@ def test_list_directed_reads():
     assert rd.read(4) == [7.0, 7.0, None, 1.0e-3]
     assert rd.read(3) == [8.0, None, None]
     assert rd.read_text() == "quoted text"
-    with pytest.raises(O.OpacityFileError):
+    with pytest.raises(fortio.ListDirectedError):
+        rd.read(1)
+    # a READ of mixed types (ZEIT, DELT, NUM_ITER) and a bad item
+    rd = fortio.ListDirected(["1.5d3, 2.0 17\n", "x\n"])
+    v = rd.read(3, conv=(fortio.real, fortio.real, fortio.integer))
+    assert v == [1500.0, 2.0, 17] and isinstance(v[2], int)
+    with pytest.raises(fortio.ListDirectedError):
         rd.read(1)
 
 

@@ -1,5 +1,11 @@
-"""ttcode's restart records (AKTTD / SNAP.xxx) read into, and written from,
-the arrays this library works on.
+"""ttcode's restart and snapshot files read into, and written from, the
+arrays this library works on.
+
+Two layouts.  Each rank writes its own file with PRINTOUT(1): SNAP_r.nnn and
+RSRT_r.nnn during a run (pp.f:565-582), AKTTD_r at its end (pp.f:827-831).
+ppcombine joins the ranks' files into one global file, GLOB.nnn or AKTTD
+(PRINTGLOBAL, ppcombine.f:603-657), and a restart reads that global AKTTD
+(READRESTART, ppinit.f:1544-1646, or its list-directed AKTTD_ASCII form).
 
 PRINTOUT(1) (ppprt.f:13-124) writes, on unit 12, one Fortran unformatted
 sequential file per rank; each WRITE is one record framed by its byte
@@ -30,6 +36,14 @@ rebuilds GITTER's NCOSYS=2 metrics (ppinit.f:1028-1406) from the coordinate
 records; `shell_of` makes the state a `synthetic.Shell` that
 `fld.start_run` accepts, so that a ttcode state drives the solver;
 `snapshot_of_fld` writes a device state back as a record.
+
+The global file holds interior cells only: the three global extents (one
+record each), the local extents and rank count, ZEIT/DELT/NUM_ITER, XXB,
+XYB, XZB on 1..N, V G H RH T ER PG CS on (1:NX,1:NY,1:NZ), UPPERBND, the six
+boundary scalars, then NCOSYS and nine interior extras that a restart does
+not read.  `read_restart` / `read_restart_ascii` / `write_restart` handle it,
+`combine` is ppcombine's FILLGLOBAL over the ranks' files, and
+`shell_of_restart` starts a run from it as READRESTART and LOCALINIT do.
 """
 from __future__ import annotations
 
@@ -132,7 +146,7 @@ def _doubles(rec: bytes, shape, e: str) -> np.ndarray:
 
 
 def read(path: str, endian: str = "<") -> Snapshot:
-    """One rank's AKTTD / SNAP.xxx file."""
+    """One rank's file (SNAP_r.nnn, RSRT_r.nnn, AKTTD_r)."""
     with open(path, "rb") as f:
         r = _Records(f.read(), endian)
     e = endian
@@ -393,3 +407,212 @@ def snapshot_of_fld(f, zeit: float = 0.0, num_iter: int = 0) -> Snapshot:
     si = f.download("STELLARINPUT")                 # (1:NX, -1:NY+2, -1:NZ+2)
     s.arrays["STELLARINPUT"] = np.asfortranarray(si[:, 2:ny + 2, 2:nz + 2])
     return s
+
+
+# ---- the global restart file: AKTTD as READRESTART reads it ------------------
+GLOBAL3 = ("V", "G", "H", "RH", "T", "ER", "PG", "CS")
+GLOBAL_EXTRAS = ("xkapR", "flimx", "EdepFor", "EdepAdv", "EdepRad", "xkapA", "stellarinput", "delta_ER",
+                 "xkapP")
+# the per-rank record each global extra is filled from (ppcombine.f:695-707
+# reads PRINTOUT's records in this order; xkapP is set to zero there)
+EXTRA_SOURCE = dict(zip(GLOBAL_EXTRAS, EXTRAS[:8] + (None,)))
+
+
+@dataclass
+class Restart:
+    """The global file PRINTGLOBAL writes (ppcombine.f:603-657: GLOB.xxx, and
+    AKTTD when ppcombine joins the ranks' AKTTD_xxx files) and READRESTART
+    reads (ppinit.f:1544-1646).  Interior cells only, (1:NX,1:NY,1:NZ),
+    column-major; NX, NY, NZ are the global extents."""
+    nx: int
+    ny: int
+    nz: int
+    loc_dims: tuple
+    numprocs: int
+    zeit: float
+    delt: float
+    num_iter: int
+    xb: dict = field(default_factory=dict)        # xxb, xyb, xzb on 1..N
+    arrays: dict = field(default_factory=dict)    # GLOBAL3 and extras, (NX, NY, NZ)
+    upperbnd: np.ndarray | None = None            # (NY, NZ) int32
+    scalars: dict = field(default_factory=dict)
+    ncosys: int | None = None
+
+
+def read_restart(path: str, endian: str = "<") -> Restart:
+    """READRESTART's binary branch (ppinit.f:1563-1598): the global extents
+    (one record each), the local extents and rank count, ZEIT/DELT/NUM_ITER,
+    XXB, XYB, XZB, V, G, H, RH, T, ER, PG, CS, UPPERBND and the six boundary
+    scalars; then, when present, the records PRINTGLOBAL appends that a
+    restart does not read (NCOSYS and the extras)."""
+    with open(path, "rb") as f:
+        r = _Records(f.read(), endian)
+    e = endian
+    (nx,), (ny,), (nz,) = (_ints(r.next(), 1, e) for _ in range(3))
+    lx, ly, lz, nprocs = _ints(r.next(), 4, e)
+    rec = r.next()
+    if len(rec) != 20:
+        raise ValueError("ZEIT, DELT, NUM_ITER record is not 8+8+4 bytes")
+    zeit, delt = struct.unpack_from(e + "2d", rec, 0)
+    (num_iter,) = struct.unpack_from(e + "i", rec, 16)
+    out = Restart(nx, ny, nz, (lx, ly, lz), nprocs, zeit, delt, num_iter)
+    for name, n in (("xxb", nx), ("xyb", ny), ("xzb", nz)):
+        out.xb[name] = _doubles(r.next(), (n,), e)
+    for name in GLOBAL3:
+        out.arrays[name] = _doubles(r.next(), (nx, ny, nz), e)
+    rec = r.next()
+    if len(rec) != 4 * ny * nz:
+        raise ValueError("UPPERBND record size")
+    out.upperbnd = np.frombuffer(rec, dtype=np.dtype(e + "i4")).astype(np.int32).reshape((ny, nz), order="F")
+    out.scalars = dict(zip(SCALARS, struct.unpack(e + "6d", r.next())))
+    if r.done():
+        return out
+    (out.ncosys,) = _ints(r.next(), 1, e)
+    for name in GLOBAL_EXTRAS:
+        if r.done():
+            break
+        out.arrays[name] = _doubles(r.next(), (nx, ny, nz), e)
+    return out
+
+
+def read_restart_ascii(path: str) -> Restart:
+    """READRESTART's AKTTD_ASCII branch (ppinit.f:1599-1632): the same items
+    as list-directed reads, one READ per binary record."""
+    from .fortio import ListDirected, integer, real
+    with open(path) as fh:
+        rd = ListDirected(fh.readlines(), path, ValueError)
+
+    def one(conv):
+        v = rd.read(1, conv)[0]
+        if v is None:
+            raise ValueError(f"{path}: null value at record {rd.pos}")
+        return v
+
+    def many(n, conv=real):
+        v = rd.read(n, conv)
+        if any(x is None for x in v):
+            raise ValueError(f"{path}: null value before record {rd.pos}")
+        return v
+
+    nx, ny, nz = one(integer), one(integer), one(integer)
+    lx, ly, lz, nprocs = many(4, integer)
+    zeit, delt, num_iter = many(3, (real, real, integer))
+    out = Restart(nx, ny, nz, (lx, ly, lz), nprocs, zeit, delt, num_iter)
+    for name, n in (("xxb", nx), ("xyb", ny), ("xzb", nz)):
+        out.xb[name] = np.array(many(n))
+    for name in GLOBAL3:
+        out.arrays[name] = np.array(many(nx * ny * nz)).reshape((nx, ny, nz), order="F")
+    out.upperbnd = np.array(many(ny * nz, integer), dtype=np.int32).reshape((ny, nz), order="F")
+    out.scalars = dict(zip(SCALARS, many(6)))
+    return out
+
+
+def write_restart(path: str, g: Restart, endian: str = "<", max_sub: int = 2**31 - 1):
+    """PRINTGLOBAL's record sequence (ppcombine.f:603-657); the extras
+    follow NCOSYS when ``ncosys`` is set, missing ones before the last present
+    written as zeros."""
+    e = endian
+    F = lambda a: np.asarray(a, dtype=np.float64).astype(np.dtype(e + "f8")).tobytes(order="F")
+    recs = [struct.pack(e + "i", g.nx), struct.pack(e + "i", g.ny), struct.pack(e + "i", g.nz),
+            struct.pack(e + "4i", *g.loc_dims, g.numprocs), struct.pack(e + "2di", g.zeit, g.delt, g.num_iter)]
+    recs += [F(g.xb[n]) for n in ("xxb", "xyb", "xzb")]
+    recs += [F(g.arrays[n]) for n in GLOBAL3]
+    recs.append(np.asarray(g.upperbnd, dtype=np.dtype(e + "i4")).tobytes(order="F"))
+    recs.append(struct.pack(e + "6d", *[g.scalars.get(n, 0.0) for n in SCALARS]))
+    if g.ncosys is not None:
+        recs.append(struct.pack(e + "i", g.ncosys))
+        last = max((q for q, n in enumerate(GLOBAL_EXTRAS) if n in g.arrays), default=-1)
+        zero = np.zeros((g.nx, g.ny, g.nz))
+        recs += [F(g.arrays.get(n, zero)) for n in GLOBAL_EXTRAS[:last + 1]]
+    with open(path, "wb") as f:
+        for rec in recs:
+            f.write(_record(rec, e, max_sub))
+
+
+def combine(parts: list[Snapshot]) -> Restart:
+    """ppcombine's FILLGLOBAL (ppcombine.f:370-457, EXCLUDEREGION off) over
+    the ranks' files: every rank's interior at its offset locN*proc_coords
+    (a radial split included), the coordinate of each axis from the ranks on
+    that axis, the per-rank extras by position with xkapP zero (ppcombine.f
+    :706-707 does not read it)."""
+    if not parts:
+        raise ValueError("no files")
+    p0 = parts[0]
+    nx, ny, nz = p0.global_dims
+    lx, ly, lz = p0.nx, p0.ny, p0.nz
+    if len(parts) != p0.numprocs:
+        raise ValueError(f"{len(parts)} files for {p0.numprocs} ranks")
+    g = Restart(nx, ny, nz, (lx, ly, lz), p0.numprocs, p0.zeit, p0.delt, p0.num_iter)
+    g.xb = {n: np.zeros(m) for n, m in (("xxb", nx), ("xyb", ny), ("xzb", nz))}
+    g.arrays = {n: np.zeros((nx, ny, nz), order="F") for n in GLOBAL3 + GLOBAL_EXTRAS}
+    g.upperbnd = np.zeros((ny, nz), dtype=np.int32, order="F")
+    seen = np.zeros((nx, ny, nz), dtype=bool)
+    for p in parts:
+        if (p.nx, p.ny, p.nz) != (lx, ly, lz) or tuple(p.global_dims) != (nx, ny, nz):
+            raise ValueError("the ranks' files disagree on the extents")
+        cx, cy, cz = p.proc_coords
+        ox, oy, oz = lx * cx, ly * cy, lz * cz
+        if ox + lx > nx or oy + ly > ny or oz + lz > nz or min(ox, oy, oz) < 0:
+            raise ValueError(f"rank {p.myid}: proc_coords {p.proc_coords} outside the global grid")
+        if cy == 0 and cz == 0:
+            g.xb["xxb"][ox:ox + lx] = p.coords["xxb"][2:lx + 2]
+        if cx == 0 and cz == 0:
+            g.xb["xyb"][oy:oy + ly] = p.coords["xyb"][2:ly + 2]
+        if cx == 0 and cy == 0:
+            g.xb["xzb"][oz:oz + lz] = p.coords["xzb"][2:lz + 2]
+        sl = np.s_[ox:ox + lx, oy:oy + ly, oz:oz + lz]
+        for name in GLOBAL3:
+            (li, _), (lj, _), (lk, _) = field_bounds(name, lx, ly, lz)
+            a = p.arrays[name]
+            g.arrays[name][sl] = a[1 - li:1 - li + lx, 1 - lj:1 - lj + ly, 1 - lk:1 - lk + lz]
+        for name in GLOBAL_EXTRAS:
+            src = EXTRA_SOURCE[name]
+            if src is not None and src in p.arrays:
+                g.arrays[name][sl] = p.arrays[src]
+        g.upperbnd[oy:oy + ly, oz:oz + lz] = p.upperbnd
+        seen[sl] = True
+    if not seen.all():
+        raise ValueError("the ranks' files do not cover the global grid")
+    g.scalars = dict(p0.scalars)
+    g.ncosys = p0.ncosys if p0.ncosys is not None else 2
+    return g
+
+
+def _halo_of_interior(a: np.ndarray) -> np.ndarray:
+    """(NX,NY,NZ) -> (-1:NX+2,-1:NY+2,-1:NZ+2): the one-rank PLANETSHIFT copy
+    in phi (j = -1, 0 from NY-1, NY; NY+1, NY+2 from 1, 2), the nearest
+    interior value in r and theta."""
+    b = np.concatenate([a[:, -2:, :], a, a[:, :2, :]], axis=1)
+    return np.asfortranarray(np.pad(b, ((2, 2), (0, 0), (2, 2)), mode="edge"))
+
+
+def shell_of_restart(g: Restart, grid: Grid, params: dict | None = None, check_grid: bool = True):
+    """A restart file as a `synthetic.Shell` for `fld.start_run`, following
+    READRESTART + LOCALINIT (ppinit.f:1544-1646, 1-69): T, ER, RH of the
+    interior from the file, the grid from GITTER and the run's parameters
+    (READRESTART reads the coordinates into dummies), c_v of GASINIT.  The
+    ghost layers take the periodic copy in phi and the nearest interior
+    value in r and theta; BOUNDS (run by `start_run`) then sets those of T
+    and RH, and the step sets those of ER.  RH below the bottom (i = 0, -1),
+    which BOUNDXMIN(9) leaves alone (ppinit.f:62-69), keeps RH(1).  With
+    ``check_grid`` the grid's cell centres must agree with the file's
+    XXB/XYB/XZB to 1e-12."""
+    from . import synthetic as S
+    if (grid.nx, grid.ny, grid.nz) != (g.nx, g.ny, g.nz):
+        raise ValueError(f"grid {(grid.nx, grid.ny, grid.nz)} vs file {(g.nx, g.ny, g.nz)}")
+    if check_grid:
+        for name, n in (("xxb", g.nx), ("xyb", g.ny), ("xzb", g.nz)):
+            mine = np.array([grid.at(name, i) for i in range(1, n + 1)])
+            scale = max(np.max(np.abs(mine)), 1e-300)
+            if np.max(np.abs(mine - g.xb[name])) > 1e-12 * scale:
+                raise ValueError(f"{name}: the grid's cell centres differ from the file's")
+    p = dict(S.default_params(g.delt))
+    if params:
+        p.update(params)
+    shape = (g.nx + 4, g.ny + 4, g.nz + 4)
+    gamma, mu = p.pop("gamma", 1.4), p.pop("mu", 2.3)
+    fields = {n: _halo_of_interior(g.arrays[n]) for n in ("T", "RH", "ER")}
+    fields["CV"] = np.full(shape, S.RGAS / (mu * (gamma - 1.0)), order="F")
+    fields["KMUL"] = np.ones(shape, order="F")
+    fields["MU_STAR"], fields["TINCIDENT"] = S.mu_star_tincident(grid, p["tirr"], p["f_incident"])
+    return S.Shell(grid, fields, p, seed=-1)

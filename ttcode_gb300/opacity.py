@@ -20,10 +20,6 @@ table files KAPPA's Burrows branches read.
   open (OPENOPACITYFILE_WOTIOVO / OPENOPACITYFILE_WITH_TIOVO,
   ppplanets.f:90-213; pprphy.f:1510-1527).
 * ``planet_kap_extra``: SETPLANETKAPEXTRA (ppplanets.f:36-59).
-* ``ListDirected``: the subset of Fortran list-directed input (``READ(u,*)``)
-  these files need: blank or comma separators, null values, ``r*c`` repeat
-  counts, ``/`` ending a read, D exponents; a read continues over records
-  until its items are filled and drops the rest of its last record.
 
 ``FLD.set_burrows_table`` hands a table of the IKAPTYP 20:25 types to the
 device (``kappa_model`` 2).  The table files are not part of the reference
@@ -33,11 +29,11 @@ from __future__ import annotations
 
 import math
 import os
-import re
 from dataclasses import dataclass, field
 
 import numpy as np
 
+from .fortio import ListDirected, ListDirectedError, integer
 from .synthetic import RGAS
 
 WAVE_BINS = 30          # nwave_bins, ppmod.f:489
@@ -70,111 +66,9 @@ def _f32(x: float) -> float:
     return float(np.float32(x))
 
 
-class OpacityFileError(ValueError):
+class OpacityFileError(ListDirectedError):
     """A table the reference's reader would stop on (clean_stop or a Fortran
     runtime error)."""
-
-
-# ---- list-directed input ---------------------------------------------------
-_NULL = object()
-_SLASH = object()
-_EXP = re.compile(r"^([+-]?(?:\d+\.?\d*|\.\d+))([+-]\d+)$")
-
-
-def _tokens(record: str):
-    """Values of one record: strings, _NULL for an empty value between
-    commas, _SLASH for a slash (which ends the read)."""
-    out, i, n = [], 0, len(record)
-    after_value = False
-    while True:
-        while i < n and record[i] in " \t":
-            i += 1
-        if i >= n:
-            break
-        ch = record[i]
-        if ch == ",":
-            if not after_value:
-                out.append(_NULL)
-            after_value = False
-            i += 1
-            continue
-        if ch == "/":
-            out.append(_SLASH)
-            break
-        if ch in "'\"":
-            j, s = i + 1, []
-            while j < n:
-                if record[j] == ch:
-                    if j + 1 < n and record[j + 1] == ch:
-                        s.append(ch)
-                        j += 2
-                        continue
-                    break
-                s.append(record[j])
-                j += 1
-            out.append("".join(s))
-            i = j + 1
-        else:
-            j = i
-            while j < n and record[j] not in " \t,/":
-                j += 1
-            tok = record[i:j]
-            m = re.match(r"^(\d+)\*(.*)$", tok)
-            if m:
-                reps, val = int(m.group(1)), m.group(2)
-                out.extend([val if val else _NULL] * reps)
-            else:
-                out.append(tok)
-            i = j
-        after_value = True
-    return out
-
-
-def _real(tok: str) -> float:
-    t = tok.translate(str.maketrans("dDqQ", "eeee"))
-    try:
-        return float(t)
-    except ValueError:
-        m = _EXP.match(t)
-        if not m:
-            raise OpacityFileError(f"not a real number: {tok!r}") from None
-        return float(f"{m.group(1)}e{m.group(2)}")
-
-
-class ListDirected:
-    """Sequential list-directed reads over the records of a text file."""
-
-    def __init__(self, lines, name: str = "<table>"):
-        self.lines = list(lines)
-        self.pos = 0
-        self.name = name
-
-    def _record(self):
-        if self.pos >= len(self.lines):
-            raise OpacityFileError(f"{self.name}: end of file at record {self.pos + 1}")
-        rec = self.lines[self.pos].rstrip("\r\n")
-        self.pos += 1
-        return rec
-
-    def read(self, n: int, conv=_real):
-        """Up to n values; None where the input gave a null value or a slash
-        ended the read (the Fortran variable keeps its value there)."""
-        vals = []
-        while len(vals) < n:
-            toks = _tokens(self._record())
-            for t in toks:
-                if t is _SLASH:
-                    return vals + [None] * (n - len(vals))
-                vals.append(None if t is _NULL else conv(t))
-                if len(vals) == n:
-                    break
-        return vals
-
-    def read_text(self, length: int = 20) -> str:
-        """One character item (``character text*20``); a blank record
-        counts as no value, so the read moves on to the next record."""
-        v = self.read(1, conv=str)[0]
-        return "" if v is None else v[:length]
 
 
 # ---- file selection ----------------------------------------------------------
@@ -280,7 +174,7 @@ def read_burrows_table(source, ikaptyp: int, planet_num: int = 1, gamma_opc: flo
             lines, name = fh.readlines(), os.fspath(source)
     else:
         lines, name = list(source), "<table>"
-    rd = ListDirected(lines, name)
+    rd = ListDirected(lines, name, OpacityFileError)
     shape = (NODES, NODES)
     plnk, ross, absk = (np.full(shape, MISSING) for _ in range(3))
     wave, lwave, lbb = (np.full(shape + (WAVE_BINS,), MISSING) for _ in range(3))
@@ -332,11 +226,11 @@ def read_bstar_bins(source, nwave_bins: int = WAVE_BINS):
             lines, name = fh.readlines(), os.fspath(source)
     else:
         lines, name = list(source), "<bins>"
-    rd = ListDirected(lines, name)
+    rd = ListDirected(lines, name, OpacityFileError)
     for _ in range(3):
         rd.read_text()
     tstar = rd.read(1)[0]
-    nbin = rd.read(1, conv=int)[0]
+    nbin = rd.read(1, conv=integer)[0]
     if nbin != nwave_bins:
         raise OpacityFileError("Some problem with the number of bins in file")
     bins = np.empty(nwave_bins)
