@@ -358,3 +358,30 @@ def test_restart_drives_the_step(tmp_path):
     from ttcode_gb300.grid import gitter
     with pytest.raises(ValueError):
         A.shell_of_restart(A.read_restart(str(f)), gitter(16, 24, 12, 1.0e9, 1.2e9))
+
+
+def test_file_names_and_crash_dump(sh, tmp_path):
+    assert A.rank_file_name("SNAP", 3, 17) == "SNAP_003.017"
+    assert A.rank_file_name("RSRT", 0, 0) == "RSRT_000.000"
+    assert A.rank_file_name("AKTTD", 12) == "AKTTD_012"
+    assert A.rank_file_name("CRSH", 0) == "CRSH_000"
+    for bad in (("SNAP", 1, None), ("SNAP", 1000, 1), ("GLOB", 0, 1)):
+        with pytest.raises(ValueError):
+            A.rank_file_name(*bad)
+    nx, ny, nz = sh.dims
+
+    class Ctx:                                  # a context after a CLEAN_STOP status
+        grid, params = sh.grid, sh.params
+
+        def download(self, name):
+            if name == "UPPERBND":
+                return np.full((ny + 4, nz + 4), nx - 1, dtype=np.int32)
+            if name == "STELLARINPUT":
+                return np.zeros((nx, ny + 4, nz + 4))
+            return np.asfortranarray(sh.fields.get(name, np.zeros((nx + 4, ny + 4, nz + 4))))
+
+    path = A.write_crash_dump(Ctx(), str(tmp_path), rank=2, zeit=7.5, num_iter=9)
+    assert path.endswith("CRSH_002")
+    t = A.read(path)
+    assert (t.myid, t.zeit, t.num_iter) == (2, 7.5, 9)
+    assert np.array_equal(t.arrays["T"], sh.fields["T"])

@@ -409,6 +409,38 @@ def snapshot_of_fld(f, zeit: float = 0.0, num_iter: int = 0) -> Snapshot:
     return s
 
 
+
+def _i33(n: int) -> str:
+    if not 0 <= n <= 999:
+        raise ValueError(f"{n} does not fit the I3.3 of the file names")
+    return f"{n:03d}"
+
+
+def rank_file_name(kind: str, rank: int, num: int | None = None) -> str:
+    """The names a rank's files get: SNAP_rrr.nnn (every IREA/10 steps) and
+    RSRT_rrr.nnn (the first of a restarted run), pp.f:565-575; AKTTD_rrr at
+    the end of a run, pp.f:827; CRSH_rrr from CLEAN_STOP, ppsub.f:718-719.
+    rrr and nnn are written with I3.3."""
+    if kind in ("SNAP", "RSRT"):
+        if num is None:
+            raise ValueError(f"{kind} files carry a print number")
+        return f"{kind}_{_i33(rank)}.{_i33(num)}"
+    if kind in ("AKTTD", "CRSH"):
+        return f"{kind}_{_i33(rank)}"
+    raise ValueError(f"unknown file kind {kind!r}")
+
+
+def write_crash_dump(f, directory: str = ".", rank: int = 0, zeit: float = 0.0, num_iter: int = 0) -> str:
+    """CLEAN_STOP's dump (ppsub.f:707-735): the rank's state as PRINTOUT(1)
+    records in CRSH_rrr.  The library returns a CLEAN_STOP status (-7)
+    instead of stopping; the caller writes the dump from the context."""
+    import os
+    path = os.path.join(directory, rank_file_name("CRSH", rank))
+    s = snapshot_of_fld(f, zeit, num_iter)
+    s.myid = rank
+    write(path, s)
+    return path
+
 # ---- the global restart file: AKTTD as READRESTART reads it ------------------
 GLOBAL3 = ("V", "G", "H", "RH", "T", "ER", "PG", "CS")
 GLOBAL_EXTRAS = ("xkapR", "flimx", "EdepFor", "EdepAdv", "EdepRad", "xkapA", "stellarinput", "delta_ER",

@@ -239,10 +239,14 @@ class FLD:
         check("synchronize", self.L.ttfld_synchronize(self.h))
 
 
-def start_run(shell, device: int = 0) -> FLD:
+def start_run(shell, device: int = 0, opacity_table=None) -> FLD:
     """Context loaded with a synthetic shell and the initial BOUNDS/KAPPA of
-    the main program's set-up (pp.f:419-463): BOUNDS at III=0, then KAPPA."""
+    the main program's set-up (pp.f:419-463): BOUNDS at III=0, then KAPPA.
+    ``opacity_table`` (an ``opacity.BurrowsTable``) is set before them, as
+    READBURROWSOPCTABLE runs before the set-up; kappa_model 2 needs it."""
     f = FLD(shell.grid, shell.params, device)
+    if opacity_table is not None:
+        f.set_burrows_table(opacity_table)
     f.load_shell(shell)
     f.set_params(iii=0)
     f.bounds()

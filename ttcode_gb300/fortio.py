@@ -128,6 +128,10 @@ class ListDirected:
                     break
         return vals
 
+    def skip(self):
+        """A READ with no items: the next record is passed over."""
+        self._record()
+
     def read_text(self, length: int = 20) -> str:
         """One character item (``character text*20``); a blank record
         counts as no value, so the read moves on to the next record."""
