@@ -6,7 +6,7 @@ import pytest
 
 from conftest import oracle_from_shell
 from ttcode_gb300 import akttd as A
-from ttcode_gb300.ipp import IppError, grid_of_ipp, params_of_ipp, read_ipp
+from ttcode_gb300.ipp import IppError, grid_of_ipp, misc_checks, params_of_ipp, read_ipp
 from ttcode_gb300.grid import RJUP, gitter
 from ttcode_gb300.synthetic import default_params, make_shell
 
@@ -98,6 +98,16 @@ def test_params_and_grid():
         grid_of_ipp(read_ipp(_ipp(l24="200 8.50e9 1.03e10 0.1")))
     with pytest.raises(IppError):
         grid_of_ipp(read_ipp(_ipp(l19="1 0")))
+
+
+def test_misc_checks():
+    """MISC_CHECKS (ppsub.f:863-880), run by params_of_ipp."""
+    misc_checks(read_ipp(SHIPPED.splitlines()))
+    for repl in ({"l2": "1 0 0"}, {"l9": "16 0 1.0 0.1", "l20": "1 3 1"}, {"l11": "10 2 2 9 15844.230"},
+                 {"l11": "10 2 2 9 15844.230", "l9": "20 0 1.0 0.1"}):
+        with pytest.raises(IppError):
+            params_of_ipp(read_ipp(_ipp(**repl)), 100.0, poles_off=True, kappa_model=0)
+    misc_checks(read_ipp(_ipp(l9="16 0 1.0 0.1")))              # Eliza's tables with MODTYP 2
 
 
 def test_synthetic_defaults_are_the_shipped_run():

@@ -6,9 +6,10 @@ input_init variable the file sets, by its Fortran name in lower case
 (``int_tmp1``, ``dbl_tmp3``, ... for the scratch record), and ``poles``
 from inc_poles (ppmod.f:73-77).  A value the file leaves null is None.
 
-``params_of_ipp`` gives the parameters of an ``fld.FLD`` context and
-``grid_of_ipp`` the grid GITTER builds from XMIN..ZMAX, so that a ttcode run
-directory (ipp plus its AKTTD) drives the library:
+``params_of_ipp`` gives the parameters of an ``fld.FLD`` context (after
+MISC_CHECKS, ``misc_checks``) and ``grid_of_ipp`` the grid GITTER builds from
+XMIN..ZMAX, so that a ttcode run directory (ipp plus its AKTTD) drives the
+library:
 
     ipp = read_ipp("ipp")
     f = start_run(akttd.shell_of_restart(akttd.read_restart("AKTTD"), grid_of_ipp(ipp),
@@ -78,6 +79,21 @@ def read_ipp(source) -> dict:
     return out
 
 
+def misc_checks(ipp: dict) -> None:
+    """MISC_CHECKS (ppsub.f:816-881) on the settings: IETOT was removed,
+    IKAPTYP 15-19 needs MODTYP 2, and IBDRAD 10 stops whatever IKAPTYP is
+    (the reference's test, IKAPTYP.ne.20 .or. IKAPTYP.ne.21, always holds).
+    Its first test, open y boundaries, cannot fail for one rank with a
+    periodic phi axis."""
+    if ipp.get("ietot") is not None and ipp["ietot"] >= 1:
+        raise IppError("removed from ttadv (IETOT >= 1)")
+    kt = ipp.get("ikaptyp")
+    if kt is not None and 15 <= kt <= 19 and ipp.get("modtyp") != 2:
+        raise IppError("Elizas opacities only available for modtyp=2")
+    if ipp.get("ibdrad") == 10 and (kt != 20 or kt != 21):
+        raise IppError("wavelength dependent source term only available for ikaptyp=20")
+
+
 def _need(ipp: dict, *names):
     missing = [n for n in names if ipp.get(n) is None]
     if missing:
@@ -107,6 +123,7 @@ def params_of_ipp(ipp: dict, delt: float, poles_off: bool = False, **overrides) 
     library has no poles: inc_poles >= 1 is refused unless ``poles_off``."""
     _need(ipp, "sorparam", "epsmat", "itmax", "fbot", "tirr", "xnue", "pr_num", "ibdrad", "iflimtyp",
           "f_incident", "bcxmin", "ieta", "isigtyp", "ikaptyp", "irad")
+    misc_checks(ipp)
     if ipp["poles"] and not poles_off:
         raise IppError("inc_poles >= 1: the library implements poles = .false. only (pass poles_off=True "
                        "to run without them)")
