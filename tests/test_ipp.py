@@ -6,7 +6,8 @@ import pytest
 
 from conftest import oracle_from_shell
 from ttcode_gb300 import akttd as A
-from ttcode_gb300.ipp import IppError, grid_of_ipp, misc_checks, params_of_ipp, read_ipp
+from ttcode_gb300.ipp import (IppError, bottom_gradients, grid_of_ipp, initial_bottom, misc_checks, params_of_ipp,
+                              read_ipp)
 from ttcode_gb300.grid import RJUP, gitter
 from ttcode_gb300.synthetic import default_params, make_shell
 
@@ -143,3 +144,52 @@ def test_run_directory_drives_the_step(tmp_path):
     assert o0.get("energy_iter") == o1.get("energy_iter")
     for n in ("T", "ER"):
         assert np.array_equal(o0.f(n)[2:-2, 2:-2, 2:-2], o1.f(n)[2:-2, 2:-2, 2:-2]), n
+
+
+def test_bottom_gradients():
+    """LOCALINIT's D_RH and D_T (ppinit.f:149-245): default-REAL expressions
+    rounded to single precision, MODVER 4 / planet 1 in double, unset cases
+    None; MODVER 3 from the Burrows table, pinned bit for bit to the oracle's
+    BOUNDXMIN(9) at III = 0 (the same gradient sets T below the bottom)."""
+    from ttcode_gb300 import opacity as O
+    f32 = lambda x: float(np.float32(x))
+    d = read_ipp(SHIPPED.splitlines())
+    mv = lambda m, nx=200, planet=1: dict(d, modver=m, global_nx=nx, planet_num=planet)
+    d_rh, d_t = bottom_gradients(mv(0), 0.0, 0.0)
+    assert d_t == -float(np.float32(1.3611882) * np.float32(1e-6)) and d_t != -1.3611882e-6
+    assert d_rh == -float(np.float32(2.1870361) * np.float32(1e-12))
+    assert bottom_gradients(mv(1), 0.0, 0.0)[1] == f32(-0.00097568917)
+    assert bottom_gradients(mv(4, 100, 1), 0.0, 0.0) == (-(f32(2.1976300) * 1e-10), -(f32(5.0305445) * 1e-6))
+    assert bottom_gradients(mv(4, 200, 1), 0.0, 0.0) == (None, None)
+    assert bottom_gradients(mv(5, 60), 0.0, 0.0)[1] == -float(np.float32(6.2500764) * np.float32(1e-6))
+    assert bottom_gradients(mv(6), 0.0, 0.0) == (None, None)
+    with pytest.raises(IppError):
+        bottom_gradients(mv(4, 100, 3), 0.0, 0.0)
+    with pytest.raises(IppError):
+        bottom_gradients(mv(3), 2000.0, 1e-3)                  # no table
+
+    sh = make_shell(12, 16, 8, seed=2, delt=100.0)
+    o = oracle_from_shell(sh, start=False)
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    k = np.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    rest = np.full(k.shape + (O.WAVE_BINS,), -7.0)
+    t = O.BurrowsTable(21, 6070.0, k.copy(), k + 0.01, k - 0.02, rest, rest, rest)
+    keep = [np.ascontiguousarray(lt), np.ascontiguousarray(lr)] + [np.asfortranarray(x) for x in (t.ross, t.plnk, t.absk)]
+    assert __import__("oracle")._load().ttor_set_opacity_table(o.h, 50, 50, *[x.ctypes.data for x in keep]) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0
+    T, RH = o.f("T"), o.f("RH")
+    tb, rb = initial_bottom(dict(d, irea=10000), t=T[2:-2, 2:-2, 2:-2], rh=RH[2:-2, 2:-2, 2:-2])
+    assert (tb, rb) == (T[2, 2, 2], RH[2, 2, 2])
+    d_rh, d_t = bottom_gradients(dict(d, modver=3, fbot=sh.params["fbottom"]), tb, rb, t)
+    assert d_rh == 0.0 and d_t < 0.0
+    g = sh.grid
+    for j in range(16 + 4):
+        assert T[1, j, 5] == T[2, j, 5] - d_t * (g.at("xxb", 1) - g.at("xxb", 0))
+        assert T[0, j, 5] == T[2, j, 5] - d_t * (g.at("xxb", 1) - g.at("xxb", -1))
+    # a restarted run takes them from its AKTTD
+    r = A.combine([A.snapshot_of(sh)])
+    r.scalars.update(TinitBottom=1234.5, rhinitbottom=6.5e-3)
+    assert initial_bottom(dict(d, irea=10001), restart=r) == (1234.5, 6.5e-3)
+    with pytest.raises(IppError):
+        initial_bottom(dict(d, irea=10001))

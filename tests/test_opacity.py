@@ -215,3 +215,40 @@ def test_table_file_drives_kappa(tmp_path):
     t.ikaptyp = 10
     with pytest.raises(ValueError):
         FLD.set_burrows_table(s, t)
+
+
+def test_host_burrows_opc_equals_the_oracle():
+    """opacity.burrows_opc, the host restatement, gives the oracle's KAPPA
+    output bit for bit at every cell KAPPA interpolates (i < UPPERBND),
+    ghosts outside the table's range (clamped) included; its stops raise."""
+    sh = make_shell(20, 16, 8, seed=4, delt=100.0)
+    o = oracle_from_shell(sh, start=False)
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    rng = np.random.default_rng(8)
+    base = math.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    a = {n: base + 0.05 * rng.standard_normal(base.shape) for n in ("plnk", "ross", "absk")}
+    t = O.BurrowsTable(21, 6070.0, a["plnk"], a["ross"], a["absk"],
+                       rng.uniform(-3, 1, base.shape + (O.WAVE_BINS,)), np.full(base.shape + (O.WAVE_BINS,), -7.0),
+                       np.full(base.shape + (O.WAVE_BINS,), -7.0))
+    keep = [np.ascontiguousarray(t.log_t), np.ascontiguousarray(t.log_rho)]
+    keep += [np.asfortranarray(x) for x in (t.ross, t.plnk, t.absk)]
+    lib = __import__("oracle")._load()
+    assert lib.ttor_set_opacity_table(o.h, O.NODES, O.NODES, *[x.ctypes.data for x in keep]) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    T, RH, ub = o.f("T"), o.f("RH"), o.f("UPPERBND")
+    nx, ny, nz = sh.dims
+    checked = 0
+    for k in range(nz + 4):
+        for j in range(ny + 4):
+            for i in range(0, ub[j, k] + 1):          # i = -1 .. upperbnd(j,k) - 1
+                p = O.burrows_opc(t, T[i, j, k], RH[i, j, k])
+                got = (p.kap_r, p.kap_p, p.kap_a, p.dkap_p_dt, p.dkap_a_dt)
+                want = tuple(o.f(n)[i, j, k] for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT"))
+                assert got == want, (i, j, k, got, want)
+                checked += 1
+    assert checked == int((ub.astype(np.int64) + 1).sum()) > (nx - 2) * (ny + 4) * (nz + 4)
+    p = O.burrows_opc(t, 1500.0, 1e-6)
+    assert p.wave.shape == (O.WAVE_BINS,) and np.all(p.wave > 0) and np.all(p.localwave == -7.0)
+    with pytest.raises(O.OpacityFileError):
+        O.burrows_opc(t, 0.0, 1e-6)

@@ -7,8 +7,10 @@ input_init variable the file sets, by its Fortran name in lower case
 from inc_poles (ppmod.f:73-77).  A value the file leaves null is None.
 
 ``params_of_ipp`` gives the parameters of an ``fld.FLD`` context (after
-MISC_CHECKS, ``misc_checks``) and ``grid_of_ipp`` the grid GITTER builds from
-XMIN..ZMAX, so that a ttcode run directory (ipp plus its AKTTD) drives the
+MISC_CHECKS, ``misc_checks``), ``grid_of_ipp`` the grid GITTER builds from
+XMIN..ZMAX, and ``initial_bottom`` / ``bottom_gradients`` the bottom values
+LOCALINIT sets (TinitBottom, RHinitbottom, D_RH, D_T; the IRAD=1 step's
+boundary), so that a ttcode run directory (ipp plus its AKTTD) drives the
 library:
 
     ipp = read_ipp("ipp")
@@ -140,3 +142,77 @@ def params_of_ipp(ipp: dict, delt: float, poles_off: bool = False, **overrides) 
         raise IppError(f"not FLD parameters: {sorted(unknown)}")
     p.update(overrides)
     return p
+
+
+# ---- LOCALINIT's bottom boundary values (ppinit.f:113-245) -------------------
+def _f32(x: float) -> float:
+    import numpy as np
+    return float(np.float32(x))
+
+
+def _f32_neg_product(a: float, e: float) -> float:
+    """-a*(10.**e) with default-REAL operands: the power folded to the
+    single-precision value of 10**e, the product rounded to single."""
+    import numpy as np
+    return -float(np.float32(np.float32(a) * np.float32(10.0 ** e)))
+
+
+def initial_bottom(ipp: dict, restart=None, t=None, rh=None) -> tuple[float, float]:
+    """TinitBottom and RHinitbottom: a restarted run (IREA mod 10 = 1) takes
+    them from the restart file's scalars (READRESTART); a new run from the
+    state's first cell, T(1,1,1) and RH(1,1,1) (ppinit.f:113-118), with
+    ``t`` and ``rh`` given as (NX, NY, NZ) interior arrays."""
+    _need(ipp, "irea")
+    if ipp["irea"] % 10 == 1:
+        if restart is None:
+            raise IppError("a restarted run (IREA mod 10 = 1) takes TinitBottom from its AKTTD")
+        return restart.scalars["TinitBottom"], restart.scalars["rhinitbottom"]
+    if t is None or rh is None:
+        raise IppError("a new run takes TinitBottom and RHinitbottom from T(1,1,1) and RH(1,1,1)")
+    return float(t[0, 0, 0]), float(rh[0, 0, 0])
+
+
+def bottom_gradients(ipp: dict, tinit_bottom: float, rhinit_bottom: float, table=None):
+    """D_RH and D_T as LOCALINIT sets them for MODTYP = 2 (ppinit.f:149-245):
+    the constants of MODVER 0-2, 4, 5 (default-REAL expressions evaluated in
+    single precision, MODVER 4 / planet 1 in double), and for MODVER 3 the
+    radiative gradient -3 Fbot kappa_R rho / (4 a c T^3) at the bottom with
+    kappa_R from BurrowsOPC (``table``, an ``opacity.BurrowsTable``).  Where
+    the reference leaves them unset (a MODVER/NX/planet without values,
+    MODVER >= 6) the result is None."""
+    from .opacity import burrows_opc
+    from .synthetic import ARAD
+    _need(ipp, "modtyp", "modver", "planet_num", "global_nx", "fbot")
+    if ipp["modtyp"] != 2:
+        raise IppError(f"MODTYP={ipp['modtyp']}: only the planet models (MODTYP 2) are implemented")
+    mv, nx, planet = ipp["modver"], ipp["global_nx"], ipp["planet_num"]
+    if mv == 0:
+        return _f32_neg_product(2.1870361, -12.0), _f32_neg_product(1.3611882, -6.0)
+    if mv == 1:
+        return _f32_neg_product(2.7934540, -9.0), _f32(-0.00097568917)
+    if mv == 2:
+        return _f32_neg_product(2.3748328, -11.0), _f32_neg_product(4.0182995, -6.0)
+    if mv == 3:
+        if table is None:
+            raise IppError("MODVER 3 takes kappa_R at the bottom from the Burrows table")
+        kr = burrows_opc(table, tinit_bottom, rhinit_bottom).kap_r
+        fd = _f32(2.99792458e10)
+        t3 = (tinit_bottom * tinit_bottom) * tinit_bottom
+        return 0.0, -(3.0 * ipp["fbot"] * kr * rhinit_bottom / (4.0 * ARAD * fd * t3))
+    if mv == 4:
+        if planet == 1:
+            return ((-(_f32(2.1976300) * 10.0 ** -10.0), -(_f32(5.0305445) * 10.0 ** -6.0)) if nx == 100
+                    else (None, None))
+        if planet == 2:
+            return ((_f32_neg_product(4.1081340, -10.0), _f32_neg_product(4.6779189, -5.0)) if nx == 100
+                    else (None, None))
+        if planet == 5:
+            return (_f32(-5.5412161e-12), _f32(-4.1841993e-06)) if nx == 100 else (None, None)
+        raise IppError(f"No initiliation file defined for planet_num {planet}")
+    if mv == 5:
+        if nx == 60:
+            return _f32_neg_product(1.9417530, -10.0), _f32_neg_product(6.2500764, -6.0)
+        if nx == 100:
+            return _f32_neg_product(1.9756314, -10.0), _f32_neg_product(5.9942251, -6.0)
+        return None, None
+    return None, None

@@ -20,6 +20,8 @@ table files KAPPA's Burrows branches read.
   open (OPENOPACITYFILE_WOTIOVO / OPENOPACITYFILE_WITH_TIOVO,
   ppplanets.f:90-213; pprphy.f:1510-1527).
 * ``planet_kap_extra``: SETPLANETKAPEXTRA (ppplanets.f:36-59).
+* ``burrows_opc``: BurrowsOPC's interpolation at one (T, rho) on the host,
+  the wavelength bins included (the device interpolates the three means).
 
 ``FLD.set_burrows_table`` hands a table of the IKAPTYP 20:25 types to the
 device (``kappa_model`` 2).  The table files are not part of the reference
@@ -243,6 +245,91 @@ def read_bstar_bins(source, nwave_bins: int = WAVE_BINS):
             raise OpacityFileError(f"{name}: undefined value in bin {i + 1}")
         bins[i] = held[1]
     return tstar, bins
+
+
+@dataclass
+class OpacityPoint:
+    """What BurrowsOPC returns for one (T, rho): the three means in cm^2/g,
+    the dkappa/dT stand-ins, and per wavelength bin the stellar and local
+    opacities and the local black-body weights (-7 where the type has none)."""
+    kap_p: float
+    kap_r: float
+    kap_a: float
+    dkap_p_dt: float
+    dkap_a_dt: float
+    wave: np.ndarray
+    localwave: np.ndarray
+    local_bb: np.ndarray
+
+
+def _log10_or_limit(x: float) -> float:
+    if x > 0.0:
+        return math.log10(x)
+    return -math.inf if x == 0.0 else math.nan
+
+
+def _bracket(nodes: np.ndarray, v: float, what: str) -> tuple[int, int]:
+    # DO K = 1,50: the first node above v (pprphy.f:1050-1052, 1087-1089)
+    for k in range(nodes.size):
+        if nodes[k] > v:
+            if k == 0:
+                raise OpacityFileError(f"underflow in opacity {what} array")
+            return k, k - 1
+    raise OpacityFileError(f"Overflow in opacity {what} array")
+
+
+def burrows_opc(table: BurrowsTable, t_in: float, rh_in: float) -> OpacityPoint:
+    """BurrowsOPC (pprphy.f:1005-1229) on the host, operation for operation:
+    log10 T and log10 rho clamped inside the nodes (default-REAL limits),
+    the bracketing nodes, bilinear weights in log10, 10** of the
+    interpolated log means; the dkappa/dT stand-ins from the bracketing T
+    nodes at the upper rho node.  The reference's stops (T <= 0, a search
+    off the table, a non-positive mean) raise OpacityFileError."""
+    if not t_in > 0.0:
+        raise OpacityFileError(f"NEG. T. IN BURROWS OPC= {t_in}")
+    rh1, tm1 = _log10_or_limit(rh_in), math.log10(t_in)
+    if tm1 < _f32(1.69896):
+        tm1 = _f32(1.69897)
+    if tm1 > _f32(3.69889):
+        tm1 = _f32(3.69888)
+    if rh1 < _f32(-11.9996):
+        rh1 = _f32(-11.9995)
+    if rh1 > _f32(-1.99993):
+        rh1 = _f32(-1.99994)
+    bt, br = table.log_t, table.log_rho
+    it, it1 = _bracket(bt, tm1, "temperature")
+    iw, iw1 = _bracket(br, rh1, "pressure")
+    ws1 = bt[it1] - tm1
+    ws = bt[it1] - bt[it]
+    ws1 = ws1 / ws
+    ws = 1.0 - ws1
+    ws2 = rh1 - br[iw1]
+    ws3 = br[iw] - br[iw1]
+    ws2 = ws2 / ws3
+    ws3 = 1.0 - ws2
+
+    def interp(a):      # a[IT,IW], a[IT,IW1], a[IT1,IW1], a[IT1,IW] -> log value
+        v00, v10, v11, v01 = a[it, iw], a[it, iw1], a[it1, iw1], a[it1, iw]
+        return ws2 * (ws1 * v00 + ws * v01) + ws3 * (ws1 * v10 + ws * v11)
+
+    kr = math.pow(10.0, interp(table.ross))
+    kp = math.pow(10.0, interp(table.plnk))
+    ka = math.pow(10.0, interp(table.absk))
+    nb = table.waveopac.shape[2]
+    kt = table.ikaptyp
+    wave = (np.array([math.pow(10.0, interp(table.waveopac[:, :, m])) for m in range(nb)])
+            if kt in WAVELENGTH_TYPES else np.full(nb, MISSING))
+    if kt in LOCAL_WAVE_TYPES:
+        lwave = np.array([math.pow(10.0, interp(table.localwave[:, :, m])) for m in range(nb)])
+        lbb = np.array([interp(table.local_bb[:, :, m]) for m in range(nb)])
+    else:
+        lwave, lbb = np.full(nb, MISSING), np.full(nb, MISSING)
+    dT = math.pow(10.0, bt[it]) - math.pow(10.0, bt[it1])
+    dkp = (math.pow(10.0, table.plnk[it, iw]) - math.pow(10.0, table.plnk[it1, iw])) / dT
+    dka = (math.pow(10.0, table.absk[it, iw]) - math.pow(10.0, table.absk[it1, iw])) / dT
+    if kr <= 0.0 or kp <= 0.0 or ka <= 0.0:
+        raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
+    return OpacityPoint(kp, kr, ka, dkp, dka, wave, lwave, lbb)
 
 
 def read_opacity_tables(directory, planet_num: int, ikaptyp: int, gamma_opc: float = 1.0,
