@@ -235,8 +235,11 @@ void* ttfld_stream(ttfld_ctx* ctx);
 /* ---- the reference subroutines, device-resident ------------------------ */
 /* BOUNDS, ppbou.f:1-92 (MODTYP=2) restricted to T, RH and UPPERBND. */
 int ttfld_bounds(ttfld_ctx* ctx);
-/* KAPPA, pprphy.f:1-360 (synthetic analytic opacity with the IKAPTYP
- * 20:25 extents, pprphy.f:321-351) and SUBSIG, pprphy.f:567-583. */
+/* KAPPA, pprphy.f:1-360, and SUBSIG, pprphy.f:567-583, by kappa_model:
+ * 0 the synthetic analytic opacity on the extents of the IKAPTYP 20:25
+ * branch (pprphy.f:321-351); 1 nothing (XKAP* are the caller's); 2 that
+ * branch with BurrowsOPC on the table of ttfld_set_opacity_table
+ * (TTFLD_E_OPACITY where the reference stops). */
 int ttfld_kappa(ttfld_ctx* ctx);
 /* CALCMUSTAR ppsub.f:156-179 and CALC_TINCIDENT pprad.f:296-405 are
  * evaluated by the caller and uploaded as MU_STAR / TINCIDENT. */
@@ -279,7 +282,7 @@ int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
  * the context accepts (4, 7, 9) with MODVER <= 5 (MODVER > 5: status -3). */
 typedef struct {
   double d_t;           /* D_T, the bottom temperature gradient of the model
-                           (ppinit.f:121-171)                               */
+                           (LOCALINIT, ppinit.f:149-245)                    */
   double tinit_bottom;  /* TinitBottom (the bottom T when BCXMIN = 6)      */
   int32_t modver;       /* MODVER                                           */
   int32_t energy_iter;  /* energy_iter as DIFF/FLIM read it (<= 1: KAPPA,
