@@ -89,6 +89,7 @@ def test_params_and_grid():
     with pytest.raises(IppError):
         params_of_ipp(d3, 100.0, poles_off=True)
     assert params_of_ipp(d3, 100.0, poles_off=True, kappa_model=0)["kappa_model"] == 0
+    assert params_of_ipp(read_ipp(_ipp(l9="5 0 1.0 0.1")), 100.0, poles_off=True)["kappa_model"] == 1
     with pytest.raises(IppError):
         params_of_ipp(d, 100.0, poles_off=True, omega=1.7)
     g = grid_of_ipp(d)

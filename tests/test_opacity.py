@@ -252,3 +252,79 @@ def test_host_burrows_opc_equals_the_oracle():
     assert p.wave.shape == (O.WAVE_BINS,) and np.all(p.wave > 0) and np.all(p.localwave == -7.0)
     with pytest.raises(O.OpacityFileError):
         O.burrows_opc(t, 0.0, 1e-6)
+
+
+# ---- Freedman (T, P) tables -------------------------------------------------
+def _freedman_file(path, logk, skip=()):
+    with open(path, "w") as fh:
+        for q in range(10):
+            fh.write(f"header{q}\n")
+        fh.write("6117.0\n")
+        n = 0
+        for ip in range(O.FREEDMAN_P.size)[::-1]:           # any order: entries are placed by value
+            for it in range(O.FREEDMAN_T.size):
+                if (it, ip) in skip:
+                    continue
+                row = (O.FREEDMAN_T[it], O.FREEDMAN_P[ip], logk[0][it, ip], logk[1][it, ip], logk[2][it, ip])
+                fh.write(" ".join(repr(float(v)) for v in row) + "\n")
+                n += 1
+    return n
+
+
+def test_freedman_table_reader(tmp_path):
+    rng = np.random.default_rng(5)
+    shape = (O.FREEDMAN_T.size, O.FREEDMAN_P.size)
+    logk = [rng.uniform(-4, 1, shape) for _ in range(3)]
+    skip = {(q, q % 18) for q in range(20)}
+    p = tmp_path / O.freedman_file_name(5)
+    n = _freedman_file(p, logk, skip)
+    assert n == O.FREEDMAN_ENTRIES
+    t = O.read_freedman_table(p, 5)
+    assert t.t_absorption == 6117.0
+    for got, want in zip((t.plnk, t.ross, t.absk), logk):
+        mask = np.ones(shape, bool)
+        for s in skip:
+            mask[s] = False
+        assert np.array_equal(got[mask], want[mask]) and np.all(got[~mask] == O.MISSING)
+    lines = open(p).read().splitlines()
+    lines[11] = "76.0 " + " ".join(lines[11].split()[1:])       # a T that is no node
+    with pytest.raises(O.OpacityFileError):
+        O.read_freedman_table(lines, 5)
+    with pytest.raises(O.OpacityFileError):
+        O.read_freedman_table(p, 9)
+    assert O.freedman_file_name(4) == "Freedman6117.dat"
+
+
+def test_freedman_interpolation_and_kappa_branch():
+    """FreedmanOPC is bilinear in T and P: a table linear in both is
+    reproduced to rounding; the clamps, the derivative stand-ins, the stops;
+    KAPPA's 4:5 branch on a shell (ideal-gas pressure, values above
+    UPPERBND from UPPERBND)."""
+    T_, P_ = np.meshgrid(O.FREEDMAN_T, O.FREEDMAN_P, indexing="ij")
+    lin = -2.0 + 3e-4 * T_ + 2e-6 * P_
+    t = O.FreedmanTable(4, 6117.0, lin + 0.1, lin, lin - 0.2)
+    for tq, pq in ((320.0, 4.5e3), (1234.5, 2.0e5), (3999.0, 2.9e5)):
+        kp, kr, ka, dkp, dka = O.freedman_opc(t, tq, pq * 1000.0)
+        assert abs(math.log10(kr) - (-2.0 + 3e-4 * tq + 2e-6 * pq)) < 1e-12
+        assert abs(math.log10(kp) - math.log10(kr) - 0.1) < 1e-12
+    # clamps (pprphy.f:830-833): below 75 K as 75.001 K, above 3e5 mbar as 299999.9 mbar
+    assert O.freedman_opc(t, 50.0, 1e6) == O.freedman_opc(t, 75.001, 1e6)
+    assert O.freedman_opc(t, 500.0, 1e12) == O.freedman_opc(t, 500.0, 299999.9 * 1000.0)
+    kp, kr, ka, dkp, dka = O.freedman_opc(t, 450.0, 5e4)       # T nodes 400, 500; P node above 50 mbar: 100
+    it, it1, iw = 20, 19, 10
+    assert dkp == (10.0 ** t.plnk[it, iw] - 10.0 ** t.plnk[it1, iw]) / (O.FREEDMAN_T[it] - O.FREEDMAN_T[it1])
+    with pytest.raises(O.OpacityFileError):
+        O.freedman_opc(t, -1.0, 1e6)
+
+    sh = make_shell(10, 8, 6, seed=1, delt=100.0)
+    T, RH = sh.fields["T"], sh.fields["RH"]
+    ub = np.full((8 + 4, 6 + 4), 9, dtype=np.int32)
+    ub[3, 4] = 6
+    out = O.freedman_kappa(t, T, RH, ub, 2.3)
+    from ttcode_gb300.synthetic import RGAS
+    for (q, j, k) in ((0, 0, 0), (5, 3, 4), (7, 3, 4), (10, 2, 2)):
+        got = tuple(out[n][q, j, k] for n in ("XKAPP", "XKAPR", "XKAPA", "DXKAPP_DT", "DXKAPA_DT"))
+        assert got == O.freedman_opc(t, T[q, j, k], RGAS * T[q, j, k] * RH[q, j, k] / 2.3), (q, j, k)
+    assert np.all(out["XKAPR"][8:, 3, 4] == out["XKAPR"][7, 3, 4])     # above i = UPPERBND = 6
+    assert out["XKAPR"][8, 3, 4] != O.freedman_opc(t, T[8, 3, 4], RGAS * T[8, 3, 4] * RH[8, 3, 4] / 2.3)[1]
+    assert np.all(out["XKAPR"][11:, 2, 2] == out["XKAPR"][10, 2, 2])   # above i = 9

@@ -22,6 +22,11 @@ table files KAPPA's Burrows branches read.
 * ``planet_kap_extra``: SETPLANETKAPEXTRA (ppplanets.f:36-59).
 * ``burrows_opc``: BurrowsOPC's interpolation at one (T, rho) on the host,
   the wavelength bins included (the device interpolates the three means).
+* Freedman (T, P) tables of IKAPTYP 4-7: ``read_freedman_table``
+  (READFREEDMANOPCTABLE, pprphy.f:944-1002), ``freedman_opc`` (FreedmanOPC,
+  pprphy.f:800-942) and ``freedman_kappa`` (KAPPA's 4:5 branch with the
+  ideal-gas pressure) on the host; the opacities reach the device as
+  prescribed arrays (``kappa_model`` 1).
 
 ``FLD.set_burrows_table`` hands a table of the IKAPTYP 20:25 types to the
 device (``kappa_model`` 2).  The table files are not part of the reference
@@ -330,6 +335,147 @@ def burrows_opc(table: BurrowsTable, t_in: float, rh_in: float) -> OpacityPoint:
     if kr <= 0.0 or kp <= 0.0 or ka <= 0.0:
         raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
     return OpacityPoint(kp, kr, ka, dkp, dka, wave, lwave, lbb)
+
+
+# ---- Freedman (T, P) tables (IKAPTYP 4-7) -------------------------------------
+# DATA FreedmanTVAL (K) and FreedmanPVAL (mbar), ppmod.f:686-697 (double constants)
+FREEDMAN_T = np.array([
+    75.0, 100.0, 110.0, 120.0, 130.0, 140.0, 150.0, 160.0, 170.0, 180.0, 190.0, 200.0, 210.0, 220.0,
+    230.0, 240.0, 250.0, 275.0, 300.0, 400.0, 500.0, 575.0, 650.0, 725.0, 800.0, 900.0, 1000.0, 1100.0,
+    1200.0, 1300.0, 1400.0, 1500.0, 1600.0, 1700.0, 1800.0, 1900.0, 2000.0, 2300.0, 2600.0, 3000.0,
+    3500.0, 4000.0])
+FREEDMAN_P = np.array([
+    0.001, 0.003, 0.01, 0.03, 0.1, 0.3, 1.0, 3.0, 10.0, 30.0, 100.0, 300.0, 1000.0, 3000.0, 10000.0,
+    30000.0, 100000.0, 300000.0])
+FREEDMAN_ENTRIES = 736          # N_entries, pprphy.f:974
+
+
+def freedman_file_name(ikaptyp: int) -> str:
+    """The table READFREEDMANOPCTABLE opens (pprphy.f:961-970)."""
+    if ikaptyp in (4, 6):
+        return "Freedman6117.dat"
+    if ikaptyp in (5, 7):
+        return "Freedman6117_noTIVO.dat"
+    raise OpacityFileError(f"ikaptyp= {ikaptyp} not avail in readfreedmanopctable")
+
+
+@dataclass
+class FreedmanTable:
+    """FreedmanXKAP_plnk/_ross/_abs (ppmod.f:653-655): log10 means,
+    index [T node, P node], -7 where the file gives no entry."""
+    ikaptyp: int
+    t_absorption: float
+    plnk: np.ndarray
+    ross: np.ndarray
+    absk: np.ndarray
+
+
+def read_freedman_table(source, ikaptyp: int, entries: int = FREEDMAN_ENTRIES) -> FreedmanTable:
+    """READFREEDMANOPCTABLE (pprphy.f:944-1002): ten header records, the
+    stellar temperature, then ``entries`` records T, P, log kappa_P,
+    log kappa_R, log kappa_abs, each placed at the node its T and P equal
+    exactly.  A T or P that is no node (the reference would then store
+    outside the arrays) raises OpacityFileError."""
+    freedman_file_name(ikaptyp)
+    if isinstance(source, (str, os.PathLike)):
+        with open(source) as fh:
+            lines, name = fh.readlines(), os.fspath(source)
+    else:
+        lines, name = list(source), "<table>"
+    rd = ListDirected(lines, name, OpacityFileError)
+    shape = (FREEDMAN_T.size, FREEDMAN_P.size)
+    plnk, ross, absk = (np.full(shape, MISSING) for _ in range(3))
+    for _ in range(10):
+        rd.read_text()
+    t_abs = rd.read(1)[0]
+    held = [None] * 5
+    for q in range(entries):
+        for m, v in enumerate(rd.read(5)):
+            if v is not None:
+                held[m] = v
+        if any(v is None for v in held):
+            raise OpacityFileError(f"{name}: undefined value in entry {q + 1}")
+        t, p, kp, kr, ka = held
+        it = np.flatnonzero(FREEDMAN_T == t)
+        ip = np.flatnonzero(FREEDMAN_P == p)
+        if it.size == 0 or ip.size == 0:
+            raise OpacityFileError(f"{name}: entry {q + 1} (T={t}, P={p}) is not a node of the table")
+        plnk[it[0], ip[0]], ross[it[0], ip[0]], absk[it[0], ip[0]] = kp, kr, ka
+    return FreedmanTable(ikaptyp, t_abs, plnk, ross, absk)
+
+
+def freedman_opc(table: FreedmanTable, t_in: float, pg_in: float):
+    """FreedmanOPC (pprphy.f:800-942) at one (T, P_gas in dyn/cm^2),
+    operation for operation: P in mbar, T and P clamped inside the nodes,
+    bilinear in T and P (linear nodes) of the log means, 10** of the
+    result; the dkappa/dT stand-ins from the bracketing T nodes.  Returns
+    (kap_p, kap_r, kap_a, dkap_p_dt, dkap_a_dt); the reference's stops
+    raise OpacityFileError."""
+    if not t_in > 0.0:
+        raise OpacityFileError(f"NEG. T. IN FREEDMAN OPC= {t_in}")
+    pg1 = pg_in * 0.001
+    tm1 = t_in
+    if tm1 < 75.0:
+        tm1 = 75.001
+    if tm1 > 4000.0:
+        tm1 = 3999.9
+    if pg1 < 0.001:
+        pg1 = 0.001001
+    if pg1 > 300000.0:
+        pg1 = 299999.9
+    it, it1 = _bracket(FREEDMAN_T, tm1, "temperature")
+    iw, iw1 = _bracket(FREEDMAN_P, pg1, "pressure")
+    bt, bp = FREEDMAN_T, FREEDMAN_P
+    ws1 = bt[it1] - tm1
+    ws = bt[it1] - bt[it]
+    ws1 = ws1 / ws
+    ws = 1.0 - ws1
+    ws2 = pg1 - bp[iw1]
+    ws3 = bp[iw] - bp[iw1]
+    ws2 = ws2 / ws3
+    ws3 = 1.0 - ws2
+
+    def interp(a):
+        v00, v10, v11, v01 = a[it, iw], a[it, iw1], a[it1, iw1], a[it1, iw]
+        return ws2 * (ws1 * v00 + ws * v01) + ws3 * (ws1 * v10 + ws * v11)
+
+    kr = math.pow(10.0, interp(table.ross))
+    kp = math.pow(10.0, interp(table.plnk))
+    ka = math.pow(10.0, interp(table.absk))
+    dT = bt[it] - bt[it1]
+    dkp = (math.pow(10.0, table.plnk[it, iw]) - math.pow(10.0, table.plnk[it1, iw])) / dT
+    dka = (math.pow(10.0, table.absk[it, iw]) - math.pow(10.0, table.absk[it1, iw])) / dT
+    if kr <= 0.0 or kp <= 0.0 or ka <= 0.0:
+        raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
+    return kp, kr, ka, dkp, dka
+
+
+def freedman_kappa(table: FreedmanTable, T: np.ndarray, RH: np.ndarray, upperbnd: np.ndarray,
+                   mu_gas: float) -> dict:
+    """KAPPA's IKAPTYP 4:5 branch for MODTYP 2 (pprphy.f:88-110) on the
+    host: PRESSG's ideal-gas pressure PG = Rgas T RH / mu_gas
+    (ppphy.f:17-20), FreedmanOPC at i = -1..UPPERBND(j,k), the values of
+    UPPERBND(j,k) above it.  T and RH are halo arrays (-1:NX+2,...),
+    UPPERBND the plane (-1:NY+2,-1:NZ+2) after BOUNDS; the result holds
+    XKAPR, XKAPP, XKAPA, DXKAPP_DT, DXKAPA_DT for ``FLD.upload`` with
+    kappa_model 1 (KAPPA freezes the opacities after an implicit step's
+    first outer iteration, so opacities formed at the step's start are the
+    ones the reference uses)."""
+    shape = T.shape
+    out = {n: np.zeros(shape, order="F") for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT")}
+    nxh = shape[0]
+    for k in range(shape[2]):
+        for j in range(shape[1]):
+            ub = int(upperbnd[j, k])
+            top = min(ub + 1, nxh - 1)            # array index of i = UPPERBND
+            for q in range(0, top + 1):
+                pg = RGAS * T[q, j, k] * RH[q, j, k] / mu_gas
+                kp, kr, ka, dkp, dka = freedman_opc(table, T[q, j, k], pg)
+                out["XKAPP"][q, j, k], out["XKAPR"][q, j, k], out["XKAPA"][q, j, k] = kp, kr, ka
+                out["DXKAPP_DT"][q, j, k], out["DXKAPA_DT"][q, j, k] = dkp, dka
+            for n in out:
+                out[n][top + 1:, j, k] = out[n][top, j, k]
+    return out
 
 
 def read_opacity_tables(directory, planet_num: int, ikaptyp: int, gamma_opc: float = 1.0,
