@@ -328,3 +328,30 @@ def test_freedman_interpolation_and_kappa_branch():
     assert np.all(out["XKAPR"][8:, 3, 4] == out["XKAPR"][7, 3, 4])     # above i = UPPERBND = 6
     assert out["XKAPR"][8, 3, 4] != O.freedman_opc(t, T[8, 3, 4], RGAS * T[8, 3, 4] * RH[8, 3, 4] / 2.3)[1]
     assert np.all(out["XKAPR"][11:, 2, 2] == out["XKAPR"][10, 2, 2])   # above i = 9
+
+
+@pytest.mark.gpu
+def test_table_file_reaches_the_device(tmp_path):
+    """A Burrows table file read on the host and handed over by
+    start_run(opacity_table=...), the path a run directory takes: the
+    device's BOUNDS and KAPPA equal the oracle's on the same table."""
+    from ttcode_gb300.fld import start_run
+    sh = make_shell(24, 32, 16, seed=6, delt=100.0)
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    k = math.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    O.write_burrows_table(tmp_path / O.burrows_file_name(1, 21), 21, 6070.0, k + 0.01, k, k - 0.02,
+                          waveopac=np.zeros(k.shape + (O.WAVE_BINS,)))
+    _write_bins(tmp_path / O.bstar_file_name(1), O.WAVE_BINS, 6070.0)
+    t = O.read_opacity_tables(tmp_path, 1, 21)
+    o = oracle_from_shell(sh, start=False)
+    keep = [np.ascontiguousarray(t.log_t), np.ascontiguousarray(t.log_rho)]
+    keep += [np.asfortranarray(x) for x in (t.ross, t.plnk, t.absk)]
+    assert __import__("oracle")._load().ttor_set_opacity_table(o.h, O.NODES, O.NODES,
+                                                               *[x.ctypes.data for x in keep]) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    sh.params = dict(sh.params, kappa_model=2)
+    f = start_run(sh, opacity_table=t)
+    for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= 1e-13, n
+    f.close()
