@@ -323,11 +323,22 @@ def test_freedman_interpolation_and_kappa_branch():
     out = O.freedman_kappa(t, T, RH, ub, 2.3)
     from ttcode_gb300.synthetic import RGAS
     for (q, j, k) in ((0, 0, 0), (5, 3, 4), (7, 3, 4), (10, 2, 2)):
-        got = tuple(out[n][q, j, k] for n in ("XKAPP", "XKAPR", "XKAPA", "DXKAPP_DT", "DXKAPA_DT"))
-        assert got == O.freedman_opc(t, T[q, j, k], RGAS * T[q, j, k] * RH[q, j, k] / 2.3), (q, j, k)
+        got = np.array([out[n][q, j, k] for n in ("XKAPP", "XKAPR", "XKAPA", "DXKAPP_DT", "DXKAPA_DT")])
+        want = np.array(O.freedman_opc(t, T[q, j, k], RGAS * T[q, j, k] * RH[q, j, k] / 2.3))
+        np.testing.assert_allclose(got, want, rtol=1e-14, atol=0, err_msg=str((q, j, k)))
     assert np.all(out["XKAPR"][8:, 3, 4] == out["XKAPR"][7, 3, 4])     # above i = UPPERBND = 6
-    assert out["XKAPR"][8, 3, 4] != O.freedman_opc(t, T[8, 3, 4], RGAS * T[8, 3, 4] * RH[8, 3, 4] / 2.3)[1]
+    assert abs(out["XKAPR"][8, 3, 4] / O.freedman_opc(t, T[8, 3, 4], RGAS * T[8, 3, 4] * RH[8, 3, 4] / 2.3)[1]
+               - 1.0) > 1e-6
     assert np.all(out["XKAPR"][11:, 2, 2] == out["XKAPR"][10, 2, 2])   # above i = 9
+    # every cell against the scalar restatement (numpy's power: last-bit differences)
+    for j in range(12):
+        for k in range(10):
+            top = min(int(ub[j, k]) + 1, 13)
+            for q in range(14):
+                c = min(q, top)
+                want = O.freedman_opc(t, T[c, j, k], RGAS * T[c, j, k] * RH[c, j, k] / 2.3)
+                got = [out[n][q, j, k] for n in ("XKAPP", "XKAPR", "XKAPA", "DXKAPP_DT", "DXKAPA_DT")]
+                np.testing.assert_allclose(got, want, rtol=1e-14, atol=0)
 
 
 @pytest.mark.gpu

@@ -460,22 +460,53 @@ def freedman_kappa(table: FreedmanTable, T: np.ndarray, RH: np.ndarray, upperbnd
     XKAPR, XKAPP, XKAPA, DXKAPP_DT, DXKAPA_DT for ``FLD.upload`` with
     kappa_model 1 (KAPPA freezes the opacities after an implicit step's
     first outer iteration, so opacities formed at the step's start are the
-    ones the reference uses)."""
-    shape = T.shape
-    out = {n: np.zeros(shape, order="F") for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT")}
-    nxh = shape[0]
-    for k in range(shape[2]):
-        for j in range(shape[1]):
-            ub = int(upperbnd[j, k])
-            top = min(ub + 1, nxh - 1)            # array index of i = UPPERBND
-            for q in range(0, top + 1):
-                pg = RGAS * T[q, j, k] * RH[q, j, k] / mu_gas
-                kp, kr, ka, dkp, dka = freedman_opc(table, T[q, j, k], pg)
-                out["XKAPP"][q, j, k], out["XKAPR"][q, j, k], out["XKAPA"][q, j, k] = kp, kr, ka
-                out["DXKAPP_DT"][q, j, k], out["DXKAPA_DT"][q, j, k] = dkp, dka
-            for n in out:
-                out[n][top + 1:, j, k] = out[n][top, j, k]
-    return out
+    ones the reference uses).  Vectorised: the operations of
+    ``freedman_opc`` in its order, with numpy's power (which may differ
+    from the C library's in the last bit)."""
+    T = np.asarray(T, dtype=np.float64)
+    RH = np.asarray(RH, dtype=np.float64)
+    nxh = T.shape[0]
+    q = np.arange(nxh)[:, None, None]
+    top = np.minimum(np.asarray(upperbnd, dtype=np.int64) + 1, nxh - 1)[None, :, :]   # index of i = UPPERBND
+    src = np.minimum(q, top)                       # cells above UPPERBND take its values
+    Ts = np.take_along_axis(T, np.broadcast_to(src, T.shape), axis=0)
+    Rs = np.take_along_axis(RH, np.broadcast_to(src, T.shape), axis=0)
+    if not np.all(Ts > 0.0):
+        raise OpacityFileError("NEG. T. IN FREEDMAN OPC")
+    pg1 = (RGAS * Ts * Rs / mu_gas) * 0.001
+    tm1 = np.where(Ts < 75.0, 75.001, Ts)
+    tm1 = np.where(tm1 > 4000.0, 3999.9, tm1)
+    pg1 = np.where(pg1 < 0.001, 0.001001, pg1)
+    pg1 = np.where(pg1 > 300000.0, 299999.9, pg1)
+    bt, bp = FREEDMAN_T, FREEDMAN_P
+    it = np.searchsorted(bt, tm1, side="right")      # the first node above, as the DO loops find it
+    iw = np.searchsorted(bp, pg1, side="right")
+    if np.any(it == 0) or np.any(iw == 0):
+        raise OpacityFileError("underflow in opacity temperature/pressure array")
+    if np.any(it == bt.size) or np.any(iw == bp.size):
+        raise OpacityFileError("Overflow in opacity temperature/pressure array")
+    it1, iw1 = it - 1, iw - 1
+    ws1 = bt[it1] - tm1
+    ws = bt[it1] - bt[it]
+    ws1 = ws1 / ws
+    ws = 1.0 - ws1
+    ws2 = pg1 - bp[iw1]
+    ws3 = bp[iw] - bp[iw1]
+    ws2 = ws2 / ws3
+    ws3 = 1.0 - ws2
+
+    def interp(a):
+        v00, v10, v11, v01 = a[it, iw], a[it, iw1], a[it1, iw1], a[it1, iw]
+        return ws2 * (ws1 * v00 + ws * v01) + ws3 * (ws1 * v10 + ws * v11)
+
+    out = {"XKAPR": np.power(10.0, interp(table.ross)), "XKAPP": np.power(10.0, interp(table.plnk)),
+           "XKAPA": np.power(10.0, interp(table.absk))}
+    dT = bt[it] - bt[it1]
+    out["DXKAPP_DT"] = (np.power(10.0, table.plnk[it, iw]) - np.power(10.0, table.plnk[it1, iw])) / dT
+    out["DXKAPA_DT"] = (np.power(10.0, table.absk[it, iw]) - np.power(10.0, table.absk[it1, iw])) / dT
+    if not (np.all(out["XKAPR"] > 0) and np.all(out["XKAPP"] > 0) and np.all(out["XKAPA"] > 0)):
+        raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
+    return {n: np.asfortranarray(a) for n, a in out.items()}
 
 
 def read_opacity_tables(directory, planet_num: int, ikaptyp: int, gamma_opc: float = 1.0,
