@@ -366,3 +366,33 @@ def test_table_file_reaches_the_device(tmp_path):
     for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT", "T"):
         assert rel_l2(f.download(n), o.f(n)) <= 1e-13, n
     f.close()
+
+
+def test_burrows_kappa_branch_9_14():
+    """KAPPA's IKAPTYP 9:12/14 branch on the host: BurrowsOPC up to
+    UPPERBND, the UPPERBND values above it; every cell against the scalar
+    restatement (numpy's log10/power: last-bit differences)."""
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    rng = np.random.default_rng(2)
+    base = math.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    rest = np.full(base.shape + (O.WAVE_BINS,), -7.0)
+    t = O.BurrowsTable(10, 6117.0, base + 0.05 * rng.standard_normal(base.shape), base.copy(), base - 0.3, rest,
+                       rest, rest)
+    sh = make_shell(10, 8, 6, seed=1, delt=100.0)
+    T, RH = sh.fields["T"], sh.fields["RH"]
+    ub = np.full((12, 10), 9, dtype=np.int32)
+    ub[5, 5] = 4
+    out = O.burrows_kappa(t, T, RH, ub)
+    for j in range(12):
+        for k in range(10):
+            top = min(int(ub[j, k]) + 1, 13)
+            for q in range(14):
+                c = min(q, top)
+                p = O.burrows_opc(t, T[c, j, k], RH[c, j, k])
+                want = [p.kap_p, p.kap_r, p.kap_a, p.dkap_p_dt, p.dkap_a_dt]
+                got = [out[n][q, j, k] for n in ("XKAPP", "XKAPR", "XKAPA", "DXKAPP_DT", "DXKAPA_DT")]
+                np.testing.assert_allclose(got, want, rtol=1e-14, atol=0)
+    assert np.all(out["XKAPR"][6:, 5, 5] == out["XKAPR"][5, 5, 5])
+    t.ikaptyp = 21
+    with pytest.raises(O.OpacityFileError):
+        O.burrows_kappa(t, T, RH, ub)

@@ -120,9 +120,10 @@ def params_of_ipp(ipp: dict, delt: float, poles_off: bool = False, **overrides) 
     FBOT, TIRR, XNUE, PR_NUM, IBDRAD, IFLIMTYP, F_INCIDENT, BCXMIN, IETA,
     ISIGTYP as read; ADJUST_SOR_PARAM where the IRAD=3 step calls it
     (ppenergy.f:372-374); the opacity source from IKAPTYP (20-25: the table
-    of ``set_burrows_table``; 4-5: prescribed, the arrays of
-    ``opacity.freedman_kappa`` uploaded before each step; any other IKAPTYP
-    needs ``kappa_model`` among the overrides).  DELT is the run's (the restart file's) time step.  The
+    of ``set_burrows_table``; 4-5 and 9-12, 14: prescribed, the arrays of
+    ``opacity.freedman_kappa`` / ``opacity.burrows_kappa`` uploaded before
+    each step; any other IKAPTYP needs ``kappa_model`` among the
+    overrides).  DELT is the run's (the restart file's) time step.  The
     library has no poles: inc_poles >= 1 is refused unless ``poles_off``."""
     _need(ipp, "sorparam", "epsmat", "itmax", "fbot", "tirr", "xnue", "pr_num", "ibdrad", "iflimtyp",
           "f_incident", "bcxmin", "ieta", "isigtyp", "ikaptyp", "irad")
@@ -136,7 +137,7 @@ def params_of_ipp(ipp: dict, delt: float, poles_off: bool = False, **overrides) 
              ieta=ipp["ieta"], isigtyp=ipp["isigtyp"], iii=1, adjust_sor=int(ipp["irad"] == 3))
     if 20 <= ipp["ikaptyp"] <= 25:
         p["kappa_model"] = 2
-    elif ipp["ikaptyp"] in (4, 5):
+    elif ipp["ikaptyp"] in (4, 5, 9, 10, 11, 12, 14):
         p["kappa_model"] = 1
     elif "kappa_model" not in overrides:
         raise IppError(f"IKAPTYP={ipp['ikaptyp']}: give kappa_model (0 analytic, 1 prescribed) among the overrides")

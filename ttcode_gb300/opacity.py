@@ -21,7 +21,9 @@ table files KAPPA's Burrows branches read.
   ppplanets.f:90-213; pprphy.f:1510-1527).
 * ``planet_kap_extra``: SETPLANETKAPEXTRA (ppplanets.f:36-59).
 * ``burrows_opc``: BurrowsOPC's interpolation at one (T, rho) on the host,
-  the wavelength bins included (the device interpolates the three means).
+  the wavelength bins included (the device interpolates the three means);
+  ``burrows_kappa``: KAPPA's IKAPTYP 9:12 and 14 branches on the host, for
+  prescribed opacities (``kappa_model`` 1).
 * Freedman (T, P) tables of IKAPTYP 4-7: ``read_freedman_table``
   (READFREEDMANOPCTABLE, pprphy.f:944-1002), ``freedman_opc`` (FreedmanOPC,
   pprphy.f:800-942) and ``freedman_kappa`` (KAPPA's 4:5 branch with the
@@ -335,6 +337,61 @@ def burrows_opc(table: BurrowsTable, t_in: float, rh_in: float) -> OpacityPoint:
     if kr <= 0.0 or kp <= 0.0 or ka <= 0.0:
         raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
     return OpacityPoint(kp, kr, ka, dkp, dka, wave, lwave, lbb)
+
+
+def burrows_kappa(table: BurrowsTable, T: np.ndarray, RH: np.ndarray, upperbnd: np.ndarray) -> dict:
+    """KAPPA's IKAPTYP 9:12 and 14 branches for MODTYP 2 (pprphy.f:199-275)
+    on the host: BurrowsOPC at i = -1..UPPERBND(j,k) and the values of
+    UPPERBND(j,k) above it (the 20:25 branch, which the device runs, copies
+    from UPPERBND-1 instead).  Arguments and result as ``freedman_kappa``;
+    vectorised with numpy's log10 and power (last-bit differences from the
+    C library's)."""
+    if table.ikaptyp not in (9, 10, 11, 12, 14):
+        raise OpacityFileError(f"IKAPTYP {table.ikaptyp}: burrows_kappa is KAPPA's 9:12 and 14 branches")
+    T = np.asarray(T, dtype=np.float64)
+    RH = np.asarray(RH, dtype=np.float64)
+    nxh = T.shape[0]
+    q = np.arange(nxh)[:, None, None]
+    top = np.minimum(np.asarray(upperbnd, dtype=np.int64) + 1, nxh - 1)[None, :, :]
+    src = np.broadcast_to(np.minimum(q, top), T.shape)
+    Ts = np.take_along_axis(T, src, axis=0)
+    Rs = np.take_along_axis(RH, src, axis=0)
+    if not np.all(Ts > 0.0):
+        raise OpacityFileError("NEG. T. IN BURROWS OPC")
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rh1 = np.log10(Rs)
+    tm1 = np.log10(Ts)
+    tm1 = np.where(tm1 < _f32(1.69896), _f32(1.69897), tm1)
+    tm1 = np.where(tm1 > _f32(3.69889), _f32(3.69888), tm1)
+    rh1 = np.where(rh1 < _f32(-11.9996), _f32(-11.9995), rh1)
+    rh1 = np.where(rh1 > _f32(-1.99993), _f32(-1.99994), rh1)
+    bt, br = table.log_t, table.log_rho
+    it = np.searchsorted(bt, tm1, side="right")
+    iw = np.searchsorted(br, rh1, side="right")
+    if np.any(it == 0) or np.any(iw == 0) or np.any(it == bt.size) or np.any(iw == br.size):
+        raise OpacityFileError("(T, rho) outside the opacity table")
+    it1, iw1 = it - 1, iw - 1
+    ws1 = bt[it1] - tm1
+    ws = bt[it1] - bt[it]
+    ws1 = ws1 / ws
+    ws = 1.0 - ws1
+    ws2 = rh1 - br[iw1]
+    ws3 = br[iw] - br[iw1]
+    ws2 = ws2 / ws3
+    ws3 = 1.0 - ws2
+
+    def interp(a):
+        v00, v10, v11, v01 = a[it, iw], a[it, iw1], a[it1, iw1], a[it1, iw]
+        return ws2 * (ws1 * v00 + ws * v01) + ws3 * (ws1 * v10 + ws * v11)
+
+    out = {"XKAPR": np.power(10.0, interp(table.ross)), "XKAPP": np.power(10.0, interp(table.plnk)),
+           "XKAPA": np.power(10.0, interp(table.absk))}
+    dT = np.power(10.0, bt[it]) - np.power(10.0, bt[it1])
+    out["DXKAPP_DT"] = (np.power(10.0, table.plnk[it, iw]) - np.power(10.0, table.plnk[it1, iw])) / dT
+    out["DXKAPA_DT"] = (np.power(10.0, table.absk[it, iw]) - np.power(10.0, table.absk[it1, iw])) / dT
+    if not (np.all(out["XKAPR"] > 0) and np.all(out["XKAPP"] > 0) and np.all(out["XKAPA"] > 0)):
+        raise OpacityFileError("neg/zero BKAP_R,BKAP_P,BKAP_A")
+    return {n: np.asfortranarray(a) for n, a in out.items()}
 
 
 # ---- Freedman (T, P) tables (IKAPTYP 4-7) -------------------------------------
