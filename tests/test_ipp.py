@@ -6,8 +6,8 @@ import pytest
 
 from conftest import oracle_from_shell
 from ttcode_gb300 import akttd as A
-from ttcode_gb300.ipp import (IppError, bottom_gradients, grid_of_ipp, initial_bottom, misc_checks, params_of_ipp,
-                              read_ipp)
+from ttcode_gb300.ipp import (IppError, bottom_gradients, grid_of_ipp, initial_bottom, misc_checks,
+                              open_run_directory, params_of_ipp, read_ipp)
 from ttcode_gb300.grid import RJUP, gitter
 from ttcode_gb300.synthetic import default_params, make_shell
 
@@ -194,3 +194,35 @@ def test_bottom_gradients():
     assert initial_bottom(dict(d, irea=10001), restart=r) == (1234.5, 6.5e-3)
     with pytest.raises(IppError):
         initial_bottom(dict(d, irea=10001))
+
+
+def test_open_run_directory(tmp_path):
+    """ipp + AKTTD + the Burrows tables of a run directory (IKAPTYP 21):
+    the shell, the table, the parameters, as the set-up reads them."""
+    from ttcode_gb300 import opacity as O
+    ipp = _ipp(l19="2 0", l24=f"16 {RJUP!r} {1.1 * RJUP!r} 0.0", l25="24 0.0 1.0 0.0", l26="12 -0.95 0.95 0.0")
+    (tmp_path / "ipp").write_text("\n".join(ipp) + "\n")
+    s0 = make_shell(16, 24, 12, seed=5, delt=250.0)
+    A.write_restart(str(tmp_path / "AKTTD"), A.combine([A.snapshot_of(s0, zeit=10.0, num_iter=4)]))
+    lt, lr = O.BURROWS_LOG_T, O.BURROWS_LOG_RHO
+    k = np.log10(1e-2) + 0.5 * lr[None, :] + 1.5 * (lt[:, None] - 3.0)
+    O.write_burrows_table(tmp_path / O.burrows_file_name(1, 21), 21, 6070.0, k, k, k,
+                          waveopac=np.zeros(k.shape + (O.WAVE_BINS,)))
+    with open(tmp_path / O.bstar_file_name(1), "w") as fh:
+        fh.write("a\nb\nc\n6070.0\n30\n" + "".join(f"{i} 1.0\n" for i in range(30)))
+    sh, table, d, r = open_run_directory(str(tmp_path))
+    assert table is not None and table.ikaptyp == 21 and r.num_iter == 4
+    assert sh.params["delt"] == 250.0 and sh.params["kappa_model"] == 2 and sh.params["adjust_sor"] == 1
+    assert np.array_equal(sh.fields["T"][2:-2, 2:-2, 2:-2], s0.fields["T"][2:-2, 2:-2, 2:-2])
+    # the ASCII restart file when there is no binary one; IKAPTYP 3 needs kappa_model
+    (tmp_path / "AKTTD").unlink()
+    with pytest.raises(FileNotFoundError):
+        open_run_directory(str(tmp_path))
+    A.write_restart(str(tmp_path / "AKTTD"), A.combine([A.snapshot_of(s0)]))
+    ipp3 = list(ipp)
+    ipp3[9] = "3 0 1.0 0.1"
+    (tmp_path / "ipp").write_text("\n".join(ipp3) + "\n")
+    with pytest.raises(IppError):
+        open_run_directory(str(tmp_path))
+    sh, table, _, _ = open_run_directory(str(tmp_path), kappa_model=0)
+    assert table is None and sh.params["kappa_model"] == 0

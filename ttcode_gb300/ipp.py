@@ -220,3 +220,28 @@ def bottom_gradients(ipp: dict, tinit_bottom: float, rhinit_bottom: float, table
             return _f32_neg_product(1.9756314, -10.0), _f32_neg_product(5.9942251, -6.0)
         return None, None
     return None, None
+
+
+def open_run_directory(directory: str, poles_off: bool = False, **overrides):
+    """A ttcode run directory as the set-up reads it: ``ipp`` (readinitfile),
+    the restart file ``AKTTD`` (or ``AKTTD_ASCII``, READRESTART) on GITTER's
+    grid, and for IKAPTYP 20-25 the Burrows tables (READBURROWSOPCTABLE).
+    Returns (shell, table, ipp, restart): ``fld.start_run(shell,
+    opacity_table=table)`` starts a context from them (for IKAPTYP 4-5 and
+    9-14 the caller uploads ``opacity.freedman_kappa`` /
+    ``opacity.burrows_kappa`` arrays as prescribed opacities).  DELT is the
+    restart file's; ``overrides`` go to ``params_of_ipp``."""
+    from . import akttd, opacity
+    ipp = read_ipp(os.path.join(directory, "ipp"))
+    binary = os.path.join(directory, "AKTTD")
+    if os.path.exists(binary):
+        rst = akttd.read_restart(binary)
+    else:
+        rst = akttd.read_restart_ascii(os.path.join(directory, "AKTTD_ASCII"))
+    params = params_of_ipp(ipp, rst.delt, poles_off=poles_off, **overrides)
+    table = None
+    if params["kappa_model"] == 2:
+        table = opacity.read_opacity_tables(directory, ipp["planet_num"], ipp["ikaptyp"], ipp["gamma_opc"],
+                                            ipp["mu_gas"])
+    shell = akttd.shell_of_restart(rst, grid_of_ipp(ipp), params)
+    return shell, table, ipp, rst
