@@ -8,7 +8,7 @@ keeps its working memory in one fixed-size __device__ array.  This test
 checks, twice in a row (the array keeps the previous call's contents), that
 its result equals the context-based exact FP64 solve bit for bit with the
 same sweep count, and that a grid too large for the fixed array is refused.
-The file is collected last so a failure here comes after every other test.
+The file is collected at the end, after the tests of the other paths.
 """
 import ctypes
 
