@@ -45,9 +45,12 @@ enum ttfld_status {
   TTFLD_E_NONPOSITIVE_Q = -7, /* Q+conv*dQ <= 0, ppenergy.f:411-521       */
   TTFLD_E_NONFINITE = -8,   /* NaN/Inf found in a solver norm             */
   TTFLD_E_NOMODEL = -9,     /* learned guess requested without a model    */
-  TTFLD_E_OPACITY = -10     /* KAPPA from a table: T <= 0, (T, rho) outside
+  TTFLD_E_OPACITY = -10,    /* KAPPA from a table: T <= 0, (T, rho) outside
                                the table, or a non-positive interpolated
                                opacity, where the reference stops          */
+  TTFLD_E_INTERNAL = -11    /* a loop of the library broke its own
+                               invariant (e.g. ran past ITMAX without its
+                               stopping flag); a bug, please report it     */
 };
 
 /* Fields addressable through ttfld_upload / ttfld_download. */
@@ -429,8 +432,12 @@ int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
  * with NY*NZ > 131072 are rejected with TTFLD_E_ARGS.  All calls on a device
  * share that array (each clears what it needs at its start), so calls whose
  * GPU work overlaps race and must be serialised by the caller.  The first
- * call on a device looks up the array's device address; make that first call
- * before any stream capture.  NY must be even. */
+ * call on a device (in each CUDA context: a caller's own context on the
+ * device counts as a new one) looks up the array's device address in that
+ * context; make that first call before any stream capture.  Every call
+ * returns only after its solve has finished on the GPU: it waits on
+ * `stream` to read the stopping flag between chunks of sweeps.  NY must be
+ * even. */
 int ttfld_sor_solve_noalloc(const double* sor_a, const double* sor_b, const double* sor_c,
                             const double* sor_d, const double* sor_e, const double* sor_f,
                             const double* sor_g, const double* rhs, double* x, int nx, int ny,

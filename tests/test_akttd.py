@@ -50,7 +50,7 @@ def test_record_layout_follows_printout(sh, tmp_path):
     assert np.array_equal(np.frombuffer(r[25], "<f8").reshape((nx, ny, nz), order="F"), s.arrays["xkapR"])
 
 
-@pytest.mark.parametrize("max_sub", [2**31 - 1, 1000])
+@pytest.mark.parametrize("max_sub", [A.MAX_SUBRECORD, 1000])
 def test_round_trip(sh, tmp_path, max_sub):
     s = A.snapshot_of(sh, zeit=3.0, num_iter=2)
     s.arrays["V"][...] = np.random.default_rng(2).random(s.arrays["V"].shape)
@@ -65,6 +65,26 @@ def test_round_trip(sh, tmp_path, max_sub):
     for n in list(A.FIELDS3) + list(A.EXTRAS):
         assert np.array_equal(t.arrays[n], s.arrays[n]), n
     assert np.array_equal(t.upperbnd, s.upperbnd)
+
+
+def test_subrecord_markers_are_gfortrans():
+    """A record split into three sub-records: head markers negative while
+    another sub-record follows, tail markers negative after the first (the
+    layout gfortran writes for records over 2**31-9 bytes)."""
+    import struct
+    payload = bytes(range(10))
+    b = A._record(payload, "<", max_sub=4)
+    marks, data, p = [], b"", 0
+    for n in (4, 4, 2):
+        marks.append(struct.unpack_from("<i", b, p)[0])
+        data += b[p + 4:p + 4 + n]
+        marks.append(struct.unpack_from("<i", b, p + 4 + n)[0])
+        p += 8 + n
+    assert p == len(b) and data == payload
+    assert marks == [-4, 4, -4, -4, 2, -2]
+    assert A._record(payload, "<", max_sub=16) == struct.pack("<i", 10) + payload + struct.pack("<i", 10)
+    assert A.MAX_SUBRECORD == 2**31 - 9
+    assert A._Records(b, "<").next() == payload
 
 
 def test_truncated_file_is_an_error(sh, tmp_path):
@@ -232,7 +252,7 @@ def test_restart_record_layout(sh, tmp_path):
     assert not np.frombuffer(r[27], "<f8").any()
 
 
-@pytest.mark.parametrize("max_sub", [2**31 - 1, 999])
+@pytest.mark.parametrize("max_sub", [A.MAX_SUBRECORD, 999])
 def test_restart_round_trip(sh, tmp_path, max_sub):
     g = A.combine([_full_snapshot(sh)])
     f = tmp_path / "AKTTD"

@@ -102,7 +102,7 @@ GUESS = {"zero": 0, "previous": 1, "learned": 2}
 STATUS = {0: "ok", 1: "iteration limit reached", 2: "learned guess rejected",
           -1: "bad argument", -2: "CUDA error", -3: "configuration not implemented",
           -7: "non-positive Q (CLEAN_STOP)", -8: "non-finite norm", -9: "no learned-guess model",
-          -10: "opacity table: T <= 0 or outside the table"}
+          -10: "opacity table: T <= 0 or outside the table", -11: "internal invariant broken (library bug)"}
 
 EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_destroy",
            "ttfld_set_params", "ttfld_get_params", "ttfld_set_solver", "ttfld_upload",

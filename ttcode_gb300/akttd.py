@@ -9,9 +9,10 @@ ppcombine joins the ranks' files into one global file, GLOB.nnn or AKTTD
 
 PRINTOUT(1) (ppprt.f:13-124) writes, on unit 12, one Fortran unformatted
 sequential file per rank; each WRITE is one record framed by its byte
-length (a 4-byte marker before and after; records longer than 2**31-1
-bytes are split into sub-records whose leading marker is negative, as
-gfortran writes them).  The records, in order:
+length (a 4-byte marker before and after).  As gfortran writes them,
+records longer than 2**31-9 bytes are split into sub-records: a sub-record's
+leading marker is negative when another one follows, its trailing marker is
+negative on every sub-record after the first.  The records, in order:
 
      1  global_NX, global_NY, global_NZ                      INTEGER
      2  locNX, locNY, locNZ, numprocs                        INTEGER
@@ -184,16 +185,23 @@ def read(path: str, endian: str = "<") -> Snapshot:
     return s
 
 
-def _record(payload: bytes, endian: str, max_sub: int = 2**31 - 1) -> bytes:
+MAX_SUBRECORD = 2**31 - 9   # gfortran's largest sub-record with 4-byte markers
+
+
+def _record(payload: bytes, endian: str, max_sub: int = MAX_SUBRECORD) -> bytes:
+    """One Fortran unformatted sequential record in gfortran's sub-record
+    layout: head marker -len if another sub-record follows, else +len; tail
+    marker -len on every sub-record after the first, else +len."""
     out = bytearray()
     chunks = [payload[i:i + max_sub] for i in range(0, len(payload), max_sub)] or [b""]
     for q, c in enumerate(chunks):
-        m = -len(c) if q + 1 < len(chunks) else len(c)   # negative: another sub-record follows
-        out += struct.pack(endian + "i", m) + c + struct.pack(endian + "i", m)
+        head = -len(c) if q + 1 < len(chunks) else len(c)
+        tail = -len(c) if q > 0 else len(c)
+        out += struct.pack(endian + "i", head) + c + struct.pack(endian + "i", tail)
     return bytes(out)
 
 
-def write(path: str, s: Snapshot, endian: str = "<", max_sub: int = 2**31 - 1):
+def write(path: str, s: Snapshot, endian: str = "<", max_sub: int = MAX_SUBRECORD):
     """The same record sequence (restart files made from this library's
     state, and the round-trip tests)."""
     e = endian
@@ -539,7 +547,7 @@ def read_restart_ascii(path: str) -> Restart:
     return out
 
 
-def write_restart(path: str, g: Restart, endian: str = "<", max_sub: int = 2**31 - 1):
+def write_restart(path: str, g: Restart, endian: str = "<", max_sub: int = MAX_SUBRECORD):
     """PRINTGLOBAL's record sequence (ppcombine.f:603-657); the extras
     follow NCOSYS when ``ncosys`` is set, missing ones before the last present
     written as zeros."""

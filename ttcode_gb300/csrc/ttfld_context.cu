@@ -163,6 +163,7 @@ const char* ttfld_status_string(int s) {
     case TTFLD_E_NONFINITE: return "non-finite norm";
     case TTFLD_E_NOMODEL: return "no learned-guess model loaded";
     case TTFLD_E_OPACITY: return "opacity table: T <= 0, (T, rho) outside the table or a non-positive opacity";
+    case TTFLD_E_INTERNAL: return "internal invariant broken (a library bug)";
   }
   return "unknown status";
 }

@@ -24,7 +24,13 @@
 //    device) race on it and must be serialised by the caller.
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (host code must not use the symbol's name as a
-//    device pointer); make that first call before any stream capture.
+//    device pointer); make that first call before any stream capture.  The
+//    address belongs to the CUDA context the module was loaded in, so it is
+//    cached per context, keyed by the context's process-unique id
+//    (cuCtxGetId): after cudaDeviceReset, or in a context the caller made
+//    itself with the driver API, the first call there looks it up again.
+//  * Each call returns once its solve has finished on the GPU (it
+//    synchronises its stream to read the stopping flag).
 #include <mutex>
 
 #include "ttfld_internal.cuh"
@@ -33,7 +39,7 @@ namespace ttfld {
 namespace {
 
 constexpr int kNoAllocMaxRows = 131072;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocMaxContexts = 64;
 
 struct NoAllocState {
   double rhsnorm;
@@ -55,21 +61,61 @@ struct NoAllocScratch {
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 std::mutex g_noalloc_mu;
-NoAllocScratch* g_noalloc_ptr[kNoAllocMaxDevices];
+struct ScratchEntry {
+  unsigned long long ctx_id;  // 0 = free
+  NoAllocScratch* ptr;
+};
+ScratchEntry g_noalloc_cache[kNoAllocMaxContexts];
 
-// Device address of the scratch array on the current device (set up once
-// per device, with that device current).
-int noalloc_scratch(NoAllocScratch** out) {
-  int dev = 0;
-  TT_CHECK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return TTFLD_E_ARGS;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+// The driver's cuCtxGetCurrent / cuCtxGetId, reached through the runtime so
+// the library links only cudart.  Returns the current context's unique id,
+// or 0 when there is none yet or the driver does not offer the calls.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_noalloc_mu
+    looked_up = true;
     void* p = nullptr;
-    TT_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = (NoAllocScratch*)p;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)p;
+    cudaGetLastError();
   }
-  *out = g_noalloc_ptr[dev];
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of the scratch array in the current context: looked up
+// with cudaGetSymbolAddress (with the caller's device current) the first
+// time a context calls, then taken from the cache.  Without a context id the
+// address is looked up on every call.
+int noalloc_scratch(NoAllocScratch** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  unsigned long long id = current_context_id();
+  if (id) {
+    for (const ScratchEntry& e : g_noalloc_cache)
+      if (e.ctx_id == id) { *out = e.ptr; return 0; }
+  }
+  void* p = nullptr;
+  TT_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));  // makes the device's context current if none was
+  if (!id) id = current_context_id();
+  if (id) {
+    for (ScratchEntry& e : g_noalloc_cache)
+      if (e.ctx_id == 0) { e.ctx_id = id; e.ptr = (NoAllocScratch*)p; break; }
+  }
+  *out = (NoAllocScratch*)p;
   return 0;
 }
 
@@ -208,6 +254,8 @@ extern "C" int ttfld_sor_solve_noalloc(const double* sor_a, const double* sor_b,
   TT_CHECK_LAUNCH();
   NoAllocState h;
   int chunk = 4, launched = 0;
+  double ratio_prev = 0.0;
+  int iter_prev = 0;
   for (;;) {
     for (int q = 0; q < chunk; ++q) {
       noalloc_sweep_kernel<0><<<blocks, kThreads, 0, st>>>(s, sor_a, sor_b, sor_c, sor_d, sor_e, sor_f, sor_g, rhs, x,
@@ -221,8 +269,23 @@ extern "C" int ttfld_sor_solve_noalloc(const double* sor_a, const double* sor_b,
     TT_CHECK(cudaMemcpyAsync(&h, &s->st, sizeof(h), cudaMemcpyDeviceToHost, st));
     TT_CHECK(cudaStreamSynchronize(st));
     if (h.done) break;
-    if (launched >= itmax) return TTFLD_E_CUDA;  // the stopping rule fires by ITMAX
-    chunk = chunk < 128 ? chunk * 2 : 256;
+    // the kernel's stopping rule fires at sweep ITMAX at the latest
+    if (launched >= itmax) {
+      fprintf(stderr, "ttfld_sor_solve_noalloc: %d sweeps queued without the stopping flag\n", launched);
+      return TTFLD_E_INTERNAL;
+    }
+    // queue about the sweeps the last two norms predict are left (sweeps
+    // queued after the stop return at once, but each still costs a launch)
+    const double ratio = h.rhsnorm > 0.0 ? h.rnorm / h.rhsnorm : 0.0;
+    int next = chunk < 128 ? chunk * 2 : 256;
+    if (iter_prev > 0 && h.iter > iter_prev && ratio > 0.0 && ratio < ratio_prev) {
+      const double rate = pow(ratio / ratio_prev, 1.0 / (h.iter - iter_prev));
+      const double left = log(epsmat / ratio) / log(rate);
+      if (left > 0.0 && left < next) next = left < 4.0 ? 4 : (int)ceil(left);
+    }
+    ratio_prev = ratio;
+    iter_prev = h.iter;
+    chunk = next < itmax - launched ? next : itmax - launched;
   }
   noalloc_shift_kernel<<<grid_for((long long)(nx + 4) * nz), kThreads, 0, st>>>(x, nx, ny, nz);
   count_launches(1);
