@@ -12,7 +12,21 @@ sweeps, and runs FP32 red-black sweeps inside FP64 defect correction.  The
 same system from zero, and the plain FP64 red-black SOR (exact reference
 rounding, and Jacobi-scaled with FMA), are timed in the same run.
 
+Beside the headline line's timed region, the same run reports
+  * "step": ms per implicit step (COUPLED_ENERGY_EQS, ppenergy.f:2-791) of
+    the shell256 run over the same K steps for the product path (learned
+    guess, then the previous step's solution, FP32/FP64) and for the plain
+    FP64 SOR (exact rounding and scaled), with the error of each against the
+    exact FP64 SOR at EPSMAT = 1e-12 over those steps;
+  * "shell512": the 160 x 512 x 256 shell (dt = 300 s, opacity contrast 1e4):
+    30 implicit steps by the product path and by the plain scaled FP64 SOR,
+    their per-step ratio, errors after 3 steps against the FP64 SOR at
+    1e-12, and the FP32 sweep's roofline at a size beyond L2;
+  * "cpu_baseline": complete solves of the bench system by the C oracle (the
+    reference loop and stopping rule) on all host cores, and on one core.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--steps512 S] [--no-shell512] [--no-cpu]
 
 Under torchrun with N > 1 every rank solves its own replica (the path does
 not shard across GPUs here), value = max-over-ranks time / (K * N).
@@ -199,7 +213,7 @@ def run_profile_solve(args):
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
     for solver, g in (("mixed", "learned"), ("sor64_exact", "zero")):
-        f.set_solver(solver, guess=g, tol=1e-10, inner_min=16, inner_max=512)
+        f.set_solver(solver, guess=g, tol=1e-10)
         f.begin_step(new_run=True)
         st = f.solve_system()
         print(json.dumps({"solver": solver, "guess": g, "sweeps": st.sor_iter, "ms": st.solve_ms}), flush=True)
@@ -298,7 +312,7 @@ def run_gpu(args):
     f.set_params(epsmat=1e-10)
 
     def solve_timed(solver, guess="zero"):
-        f.set_solver(solver, guess=guess, tol=1e-10, inner_min=16, inner_max=512)
+        f.set_solver(solver, guess=guess, tol=1e-10)
         f.begin_step(new_run=True)   # every timed solve is a run's first: no previous solution
         flush_l2(torch, flush)
         torch.cuda.synchronize()
@@ -380,7 +394,7 @@ def run_gpu(args):
     out = torch.empty(f.download("DELTA_ER").size, dtype=torch.float64, pin_memory=True)
     h2d = sum(host[n].numel() * 8 for n in names) + ub.size * 4
     d2h = out.numel() * 8
-    f.set_solver("mixed", guess="learned", tol=1e-10, inner_min=16, inner_max=512)
+    f.set_solver("mixed", guess="learned", tol=1e-10)
     e2e = []
     for it in range(args.warmup + args.steps):
         flush_l2(torch, flush)
@@ -432,17 +446,94 @@ def run_gpu(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(f, sh, st_ref_sweeps=plain["sor64_exact"]["sweeps"])
+        line["cpu_baseline"] = cpu_baseline(f, sh)
+    from ttcode_gb300 import guess as G
+    blob = G.save_weights(f)
+    f.close()
+    # per implicit step, and the 512 x 256 x 160 configuration (not timed
+    # regions of the headline; rank 0 of a single-replica run)
+    if rank == 0 and ws == 1:
+        line["step"] = step_block(sh, args.steps, blob)
+        if not args.no_shell512 and args.steps512 > 0:
+            line["shell512"] = shell512_block(args.steps512, peak, peak_kind)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    f.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
+STEP_KEYS = ("ms_per_step", "solve_ms_per_step", "sweeps_per_solve", "outer_iter_per_step", "solves_per_step",
+             "fallbacks", "worst_status")
+
+
+def _variants(sh, names, nsteps, snap_at, ref_snap, blob):
+    from ttcode_gb300 import runs
+    out = {}
+    for name in names:
+        steps, snap = runs.run_variant(sh, name, nsteps, snap_at, blob=blob if "learned" in name else None)
+        s = runs.summarize(name, steps, snap, ref_snap, snap_at)
+        out[name] = {k: s[k] for k in STEP_KEYS + ("err_vs_fp64_1e-12",) if k in s}
+    return out
+
+
+def step_block(sh, nsteps, blob):
+    """ms per implicit step (COUPLED_ENERGY_EQS) of the shell256 run over the
+    same nsteps steps: the product path (learned guess for the run's first
+    solve, then the previous step's solution; FP32/FP64) against the plain
+    FP64 red-black SOR from zero, exact and scaled.  Errors of E_R and T
+    after the last step against the exact FP64 SOR at EPSMAT = 1e-12."""
+    from ttcode_gb300 import runs
+    _, ref_snap = runs.run_variant(sh, "fp64_exact", nsteps, nsteps, epsmat=1e-12)
+    v = _variants(sh, ("mixed_learned", "fp64_fast", "fp64_exact"), nsteps, nsteps, ref_snap, blob)
+    prod = v["mixed_learned"]["ms_per_step"]
+    return {"workload": "shell256, consecutive implicit steps from the set-up state", "steps": nsteps,
+            "reference": "exact FP64 SOR (the reference loop) at EPSMAT 1e-12 over the same steps",
+            **v, "speedup_vs_fp64_fast": v["fp64_fast"]["ms_per_step"] / prod,
+            "speedup_vs_fp64_exact": v["fp64_exact"]["ms_per_step"] / prod}
+
+
+def shell512_block(nsteps, peak, peak_kind):
+    """The 160 x 512 x 256 shell (dt 300 s, opacity contrast 1e4): nsteps
+    implicit steps by the product path (a network trained on 8 first solves
+    of other irradiations and dt in [150, 600] s of the same shell) and by
+    the plain scaled FP64 SOR from zero, errors after 3 steps against the
+    scaled FP64 SOR at EPSMAT = 1e-12, and the FP32 sweep's CUDA-event
+    roofline on the shell's first system (a working set beyond L2)."""
+    import torch
+    from ttcode_gb300 import runs
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import shell
+    sh = shell("shell512", seed=1)
+    sh.params["epsmat"] = 1e-10
+    sh.params["itmax"] = 200000
+    t0 = time.perf_counter()
+    blob, info = runs.train_guess(sh, 8, 12, 5e-4, (150.0, 600.0))
+    snap_at = min(3, nsteps)
+    _, ref_snap = runs.run_variant(sh, "fp64_fast", snap_at, snap_at, epsmat=1e-12)
+    v = _variants(sh, ("mixed_learned", "fp64_fast"), nsteps, snap_at, ref_snap, blob)
+    f = start_run(sh)
+    first_system(f)
+    nx, ny, nz = sh.dims
+    ms = f.time_sweeps("mixed", 50)
+    f.close()
+    torch.cuda.synchronize()
+    achieved = BYTES_FP32_SWEEP * nx * ny * nz / (ms * 1e-3) / 1e9
+    return {"workload": "shell512: 160x512x256 (r x phi x theta), 20971520 cells, dt=300 s, opacity contrast 1e4, "
+                        "seed 1; consecutive implicit steps from the set-up state, tol 1e-10",
+            "steps": nsteps, "training": info,
+            "reference": f"scaled FP64 SOR at EPSMAT 1e-12 over the first {snap_at} steps",
+            **v, "speedup_per_step_vs_fp64_fast": v["fp64_fast"]["ms_per_step"] / v["mixed_learned"]["ms_per_step"],
+            "roofline": {"kernel": "sweeps32_persistent (one full sweep)", "ms_per_sweep": ms,
+                         "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * nx * ny * nz, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind},
+            "wall_s": round(time.perf_counter() - t0, 1)}
+
+
 def oracle_system(sh, f=None):
-    """The same system in the CPU oracle: from the device context when given,
-    else assembled by the oracle itself (one COUPLED_ENERGY_EQS step)."""
+    """The bench system in the CPU oracle: from the device context when given,
+    else assembled by the oracle itself (the first outer iteration of
+    COUPLED_ENERGY_EQS, its solve cut to one sweep by ITMAX = 1, as the GPU
+    side assembles it)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ormod
     from ttcode_gb300.grid import full_1d
@@ -457,8 +548,6 @@ def oracle_system(sh, f=None):
         if k != "kappa_model":
             o.set(k, v)
     o.set("epsmat", 1e-10)
-    o.set("itmax", 200000)
-    assembly_ms = None
     if f is not None:
         for n in ("SOR_A", "SOR_B", "SOR_C", "SOR_D", "SOR_E", "SOR_F", "SOR_G", "RHS_ER"):
             o.f(n)[...] = f.download(n)
@@ -467,10 +556,10 @@ def oracle_system(sh, f=None):
         o.call("bounds")
         o.call("kappa")
         o.set("iii", 1)
-        t0 = time.perf_counter()
+        o.set("itmax", 1)
         o.call("coupled_energy_eqs", 1)
-        assembly_ms = (time.perf_counter() - t0) * 1e3
-    return o, assembly_ms
+    o.set("itmax", 200000)
+    return o
 
 
 def host_threads() -> int:
@@ -480,51 +569,55 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
-def time_oracle_sweeps(o, target_s=10.0, threads=None):
-    """ms per red-black sweep of the C oracle on `threads` theta slabs (the
-    reference's rank decomposition on the host cores)."""
-    threads = threads or host_threads()
-    o.f("DELTA_ER")[...] = 0.0
+def oracle_solve_ms(o, threads: int):
+    """One complete solve of the oracle's current system from zero: the
+    reference's red-black loop and stopping rule (ppsor.f:29-177), on
+    `threads` theta slabs (one thread each, the reference's rank per slab),
+    or the serial loop with threads = 1.  Returns (ms, sweeps)."""
     t0 = time.perf_counter()
-    o.call("sor_sweeps_mt", 5, threads)
-    per = (time.perf_counter() - t0) / 5
-    n = max(5, int(target_s / max(per, 1e-6)))
-    o.f("DELTA_ER")[...] = 0.0
-    t0 = time.perf_counter()
-    o.call("sor_sweeps_mt", n, threads)
-    return (time.perf_counter() - t0) / n * 1e3, n
+    if threads > 1:
+        rc = o.call("solve_with_sor_mt", threads)
+    else:
+        rc = o.call("solve_with_sor", 0, 0)
+    ms = (time.perf_counter() - t0) * 1e3
+    if rc != 0:
+        raise RuntimeError(f"oracle solve status {rc}")
+    return ms, int(o.get("sor_iter"))
 
 
-def cpu_baseline(f, sh, st_ref_sweeps):
-    o, _ = oracle_system(sh, f)
+def cpu_baseline(f, sh):
+    o = oracle_system(sh, f)
     th = host_threads()
-    ms_sweep, n = time_oracle_sweeps(o, 10.0, th)
-    return {"value": ms_sweep * st_ref_sweeps, "unit": "ms", "cores": th, "kind": "port",
-            "sample": f"{n} FP64 red-black sweeps of the same 100x256x128 system by the C oracle "
-                      f"(gcc -O2, {th} threads on theta slabs, a barrier per colour), "
-                      f"{ms_sweep:.3f} ms/sweep x {st_ref_sweeps} sweeps per solve"}
+    runs = [oracle_solve_ms(o, th) for _ in range(2)]
+    ms, sweeps = min(runs)
+    serial_ms, serial_sweeps = oracle_solve_ms(o, 1)
+    return {"value": ms, "unit": "ms", "cores": th, "kind": "port",
+            "sample": f"complete solves of the same 100x256x128 system to 1e-10 by the C oracle (gcc -O2; the "
+                      f"reference loop and stopping rule; {th} threads on theta slabs, a barrier per colour): "
+                      f"best of 2, {sweeps} sweeps",
+            "serial_1core_ms": serial_ms, "serial_sweeps": serial_sweeps}
 
 
 def run_reference(args):
     """The reference's CPU path (the C restatement of ppsor.f) on all the
     host cores, as the reference runs one serial rank per core on a slab of
-    the grid: each step times a bounded sample of red-black sweeps of the
-    shell256 system on theta slabs, one thread each, and scales it by the
-    sweep count of a full solve to 1e-10."""
+    the grid: each step is one complete solve of the shell256 system to
+    1e-10 from zero (the reference's stopping rule), one thread per theta
+    slab.  One serial solve on one core is reported beside it."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from ttcode_gb300.synthetic import shell
     sh = shell(SHELL, seed=1)
-    o, asm_ms = oracle_system(sh, None)         # one full step: assembly + solve
-    sweeps = int(o.get("sor_total"))
-    vals = []
+    o = oracle_system(sh, None)
     th = host_threads()
+    vals, sweeps = [], 0
     for it in range(args.warmup + args.steps):
-        ms_sweep, n = time_oracle_sweeps(o, 4.0, th)
+        ms, sweeps = oracle_solve_ms(o, th)
         if it >= args.warmup:
-            vals.append(ms_sweep * sweeps)
+            vals.append(ms)
     v = float(sum(vals) / len(vals))
+    serial_ms, serial_sweeps = oracle_solve_ms(o, 1)
     line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded analytic shell, no dataset)",
@@ -532,9 +625,10 @@ def run_reference(args):
                        "guess": "zero", "tol": 1e-10, "omega": sh.params["sorparam"]},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "ms", "cores": th, "kind": "port",
-                             "sample": f"per step: ~4 s of FP64 red-black sweeps by the C oracle on {th} threads "
-                                       f"(theta slabs, a barrier per colour) scaled by {sweeps} sweeps per solve; "
-                                       f"one serial step (assembly+solve) took {asm_ms:.0f} ms"},
+                             "sample": f"per step: one complete solve of the shell256 system to 1e-10 from zero "
+                                       f"by the C oracle (the reference loop and stopping rule, {sweeps} sweeps) "
+                                       f"on {th} threads (theta slabs, a barrier per colour)",
+                             "serial_1core_ms": serial_ms, "serial_sweeps": serial_sweeps},
             "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -546,6 +640,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--steps512", type=int, default=30, help="implicit steps of the 160x512x256 block")
+    ap.add_argument("--no-shell512", action="store_true", help="skip the 160x512x256 block")
     ap.add_argument("--profile-solve", action="store_true",
                     help="only build the system and run one mixed and one exact FP64 solve")
     ap.add_argument("--profile-sweeps", action="store_true",

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define TTFLD_ABI_VERSION 1
+#define TTFLD_ABI_VERSION 2
 
 enum ttfld_status {
   TTFLD_OK = 0,
@@ -150,9 +150,11 @@ typedef struct {
   int32_t solver;      /* enum ttfld_solver                                */
   int32_t guess;       /* enum ttfld_guess                                 */
   double tol;          /* mixed solver: stop at ||b-Ax||_1/||b||_1 <= tol  */
-  int32_t inner_min;   /* accepted and ignored: the mixed solver runs each  */
-  int32_t inner_max;   /* FP64 correction until its FP32 sweeps stop (target
-                          reached or rounding floor)                       */
+  int32_t inner_digits; /* mixed solver: an FP32 inner run on A e = r stops
+                          once its in-sweep norm is 10^-inner_digits of the
+                          FP64 anchor's (or at tol, or at the FP32 rounding
+                          floor); 0 = the default, 5                       */
+  int32_t reserved;    /* set to 0                                         */
   int32_t max_sweeps;  /* mixed solver sweep budget (0 = ITMAX)            */
   int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:
                             0 = the residual its first red-black sweep
@@ -188,6 +190,9 @@ typedef struct {
                               library's stream, guess included)           */
   double guess_ms;         /* of which: making and checking the initial
                               guess (network inference, fallback test)    */
+  int32_t stalls;          /* FP32 inner runs ended at their rounding floor
+                              and re-anchored in FP64 (mixed, PCG)        */
+  int32_t reserved;
 } ttfld_solve_stats;
 
 typedef struct {
@@ -196,7 +201,7 @@ typedef struct {
   int32_t solves;          /* linear solves in the step                    */
   int32_t fallbacks;       /* learned-guess rejections                     */
   int32_t status;
-  int32_t reserved;
+  int32_t stalls;          /* FP32 rounding-floor re-anchors, all solves   */
   double global_deltaq;    /* max |dQ/Q| of the last outer iteration       */
   double global_deltaer;   /* max |dER/ER| of the last outer iteration     */
   double solve_ms;         /* device time in the linear solves             */

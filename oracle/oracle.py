@@ -66,6 +66,7 @@ def _load():
         lib.ttor_solve_with_sor.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         lib.ttor_sor_sweeps.argtypes = [vp, ctypes.c_int]
         lib.ttor_sor_sweeps_mt.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        lib.ttor_solve_with_sor_mt.argtypes = [vp, ctypes.c_int]
         lib.ttor_coupled_energy_eqs.argtypes = [vp, ctypes.c_int]
         lib.ttor_raddif.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         lib.ttor_set_opacity_table.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [vp] * 5

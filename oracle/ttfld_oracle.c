@@ -1090,6 +1090,88 @@ int ttor_sor_sweeps_mt(ttor_state* s, int nsweeps, int nthreads) {
   return 0;
 }
 
+/* SOLVE_WITH_SOR (ppsor.f:2-187) from zero on theta slabs, one thread per
+ * slab as the reference runs one rank per slab: after each sweep thread 0
+ * adds the slab norms in slab order (the ranks' allreduce, ppsor.f:155-160)
+ * and applies the stopping rule (ppsor.f:161-177); the others wait for its
+ * decision at a third barrier. */
+typedef struct {
+  int stop, it, itmin, itmax, maxit;
+  double eps, rhsnorm, rnorm;
+  double* parts;
+  int nthreads;
+} mt_ctl;
+
+typedef struct {
+  ttor_state* s;
+  int k0, k1, t;
+  pthread_barrier_t* bar;
+  mt_ctl* ctl;
+} mt_solve_arg;
+
+static void* mt_solve_worker(void* p) {
+  mt_solve_arg* a = (mt_solve_arg*)p;
+  ttor_state* s = a->s;
+  mt_ctl* c = a->ctl;
+  for (;;) {
+    double r = sor_colour_k(s, s->DELTA_ER, s->RHS_ER, 0, a->k0, a->k1);
+    shift_halo_k(s, s->DELTA_ER, a->k0, a->k1);
+    pthread_barrier_wait(a->bar);
+    r = r + sor_colour_k(s, s->DELTA_ER, s->RHS_ER, 1, a->k0, a->k1);
+    shift_halo_k(s, s->DELTA_ER, a->k0, a->k1);
+    c->parts[a->t] = r;
+    pthread_barrier_wait(a->bar);
+    if (a->t == 0) {
+      double rn = 0.0;
+      for (int t = 0; t < c->nthreads; ++t) rn = rn + c->parts[t];
+      c->rnorm = rn;
+      c->it += 1;
+      if (c->it == c->itmax) { c->maxit = 1; c->stop = 1; }
+      else if (!(rn / c->rhsnorm > c->eps) && c->it >= c->itmin) c->stop = 1;
+    }
+    pthread_barrier_wait(a->bar);
+    if (c->stop) break;
+  }
+  return NULL;
+}
+
+int ttor_solve_with_sor_mt(ttor_state* s, int nthreads) {
+  if (s->poles) return -4;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > s->nz) nthreads = s->nz;
+  if (nthreads > 256) nthreads = 256;
+  for (size_t q = 0; q < nhalo(s); ++q) s->DELTA_ER[q] = 0.0;  /* ppsor.f:29 */
+  double rhsnorm = 0.0;
+  for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(s->RHS_ER[c]);
+  s->global_rhsnorm = rhsnorm;
+  pthread_barrier_t bar;
+  if (pthread_barrier_init(&bar, NULL, (unsigned)nthreads)) return -2;
+  double parts[256];
+  mt_ctl ctl = {0, 0, 1, s->itmax, 0, s->epsmat, rhsnorm, 0.0, parts, nthreads};
+  pthread_t th[256];
+  mt_solve_arg args[256];
+  int rc = 0, started = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    args[t].s = s;
+    args[t].k0 = 1 + (int)((long long)s->nz * t / nthreads);
+    args[t].k1 = (int)((long long)s->nz * (t + 1) / nthreads);
+    args[t].t = t;
+    args[t].bar = &bar;
+    args[t].ctl = &ctl;
+  }
+  for (int t = 1; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, mt_solve_worker, &args[t])) { rc = -2; break; }
+    ++started;
+  }
+  if (rc == 0) mt_solve_worker(&args[0]);
+  for (int t = 1; t <= started; ++t) pthread_join(th[t], NULL);
+  pthread_barrier_destroy(&bar);
+  if (rc) return rc;
+  s->global_rnorm = ctl.rnorm;
+  s->sor_iter = ctl.it;
+  return ctl.maxit ? 1 : 0;
+}
+
 int ttor_sor_sweeps(ttor_state* s, int nsweeps) {
   double rhsnorm = 0.0;
   for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(s->RHS_ER[c]);

@@ -88,6 +88,7 @@ int ttor_sor_sweeps(ttor_state* s, int nsweeps);
 /* The same sweeps on nthreads theta slabs (the reference's rank
  * decomposition on the host cores, for the CPU baseline). */
 int ttor_sor_sweeps_mt(ttor_state* s, int nsweeps, int nthreads);
+int ttor_solve_with_sor_mt(ttor_state* s, int nthreads);
 int ttor_adjust_sor_param(ttor_state* s);
 int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds);
 /* DIFFUSION (ppdif.f) of the field "SCALAR" with constant xnue/Pr. */

@@ -47,7 +47,7 @@ def test_ffi_export_list_matches_header():
 
 def test_abi_version_and_status_strings(libttfld):
     # host-only calls: no device is touched
-    assert libttfld.ttfld_abi_version() == 1
+    assert libttfld.ttfld_abi_version() == 2
     libttfld.ttfld_status_string.restype = ctypes.c_char_p
     assert libttfld.ttfld_status_string(-7).startswith(b"non-positive Q")
 

@@ -421,6 +421,24 @@ def test_slab_threads_give_the_serial_sweeps(shell):
     assert abs(o.get("global_rnorm") - r1) <= 1e-12 * r1
 
 
+def test_slab_threads_complete_solve(shell):
+    """The CPU baseline's complete threaded solve (slab norms added in slab
+    order, the ppsor.f:161-177 stopping rule) stops at the serial loop's
+    sweep with its iterate: a different summation order can only move the
+    stop by one sweep where the ratio ties EPSMAT in the last bits."""
+    o = oracle_from_shell(shell)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("solve_with_sor", 0, 0) == 0
+    x1, n1 = o.f("DELTA_ER").copy(), int(o.get("sor_iter"))
+    assert o.call("solve_with_sor_mt", 5) == 0
+    n2 = int(o.get("sor_iter"))
+    assert abs(n2 - n1) <= 1
+    if n2 == n1:
+        assert np.array_equal(o.f("DELTA_ER"), x1)
+    assert o.get("global_rnorm") / o.get("global_rhsnorm") <= o.get("epsmat")
+
+
 def test_opacity_table_interpolation(shell):
     """BurrowsOPC's interpolation (ttor_set_opacity_table + KAPPA) on a table
     of the analytic model reproduces the model (log kappa is linear in log T

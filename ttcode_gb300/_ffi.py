@@ -42,7 +42,7 @@ class Params(ctypes.Structure):
 
 class SolveOpts(ctypes.Structure):
     _fields_ = [("solver", c_int32), ("guess", c_int32), ("tol", c_double),
-                ("inner_min", c_int32), ("inner_max", c_int32), ("max_sweeps", c_int32),
+                ("inner_digits", c_int32), ("reserved", c_int32), ("max_sweeps", c_int32),
                 ("fallback_rule", c_int32), ("sweep_form", c_int32)]
 
 
@@ -54,7 +54,7 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("sor_iter", c_int32), ("corrections", c_int32), ("fallback", c_int32),
                 ("status", c_int32), ("rnorm", c_double), ("rhsnorm", c_double),
                 ("true_resid_l1", c_double), ("guess_resid_l1", c_double), ("solve_ms", c_double),
-                ("guess_ms", c_double)]
+                ("guess_ms", c_double), ("stalls", c_int32), ("reserved", c_int32)]
 
 
 class RaddifParams(ctypes.Structure):
@@ -76,7 +76,7 @@ class Energy(ctypes.Structure):
 
 class StepStats(ctypes.Structure):
     _fields_ = [("energy_iter", c_int32), ("sor_total", c_int32), ("solves", c_int32),
-                ("fallbacks", c_int32), ("status", c_int32), ("reserved", c_int32),
+                ("fallbacks", c_int32), ("status", c_int32), ("stalls", c_int32),
                 ("global_deltaq", c_double), ("global_deltaer", c_double),
                 ("solve_ms", c_double), ("step_ms", c_double)]
 

@@ -186,8 +186,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   c->opts.solver = TTFLD_SOLVER_SOR64_EXACT;
   c->opts.guess = TTFLD_GUESS_ZERO;
   c->opts.tol = 1e-10;
-  c->opts.inner_min = 8;
-  c->opts.inner_max = 256;
+  c->opts.inner_digits = 5;
   c->opts.fallback_rule = 3;
   c->prev_scale = 0.9;
   Dev& d = c->d;
@@ -316,8 +315,8 @@ int ttfld_set_solver(ttfld_ctx* c, const ttfld_solve_opts* o) {
   if (o->fallback_rule < 0 || o->fallback_rule > 3) return TTFLD_E_ARGS;
   if (o->sweep_form < 0 || o->sweep_form > 2) return TTFLD_E_ARGS;
   c->opts = *o;
-  if (c->opts.inner_min < 1) c->opts.inner_min = 1;
-  if (c->opts.inner_max < c->opts.inner_min) c->opts.inner_max = c->opts.inner_min;
+  if (c->opts.inner_digits <= 0) c->opts.inner_digits = 5;
+  if (c->opts.inner_digits > 12) c->opts.inner_digits = 12;
   return TTFLD_OK;
 }
 

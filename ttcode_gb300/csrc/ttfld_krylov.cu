@@ -805,7 +805,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     }
   }
   long long total = 0;
-  int anchors = 0, status = TTFLD_OK, slow = 0;
+  int anchors = 0, status = TTFLD_OK, slow = 0, stalls = 0;
   double prev = INFINITY, ratio = INFINITY;
   for (;;) {
     const SolverDev& h = *c->host_sol;
@@ -829,6 +829,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, sgs, &its))) return rc;
     total += its;
     ++anchors;
+    if (c->host_sol->stalled) ++stalls;
     kry_update_kernel<<<grid_cells(w->k.n), kThreads, 0, c->stream>>>(c->d, w->k, x);
     count_launches(1);
     TT_CHECK_LAUNCH();
@@ -846,6 +847,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     st->rnorm = l2 ? sqrt(c->host_sol->scratch[0]) : c->host_sol->true_l1;
     st->true_resid_l1 = c->host_sol->true_l1;
     st->status = status;
+    st->stalls = stalls;
   }
   return status;
 }

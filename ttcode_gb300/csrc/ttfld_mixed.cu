@@ -722,8 +722,9 @@ static int poll(ttfld_ctx* c) {
 }
 
 // Defect correction: anchor r = b - A x in FP64, run FP32 sweeps on
-// A e = r until the in-sweep norm of x + e has dropped by 1e-5 relative to
-// the anchor (well inside FP32 precision) or reached tol, x += e, repeat;
+// A e = r until the in-sweep norm of x + e has dropped by 10^-inner_digits
+// (default 1e-5, well inside FP32 precision) relative to the anchor or
+// reached tol, x += e, repeat;
 // stop when the FP64 ||b - A x||_1 / ||b||_1 <= tol.
 //
 // With guess_test = n > 0, x holds a previous or learned initial guess that
@@ -742,7 +743,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   const double tol = c->opts.tol;
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
   const int period = 8;
-  int corrections = 0, status = TTFLD_OK;
+  int corrections = 0, stalls = 0, status = TTFLD_OK;
   double tight = 1.0;  // halved each time the in-sweep norm met tol but the FP64 residual did not
   bool hit_tol = false;
   bool resume = false;  // the first anchor and its first sweeps are done already
@@ -783,7 +784,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     if (hit_tol) tight *= 0.5;
     if (c->host_sol->iter >= budget) { status = TTFLD_MAXITER; break; }
     const double anchor = l1 / bl1;
-    const double stop = fmax(tol * tight, anchor * 1e-5);
+    const double stop = fmax(tol * tight, anchor * pow(10.0, -c->opts.inner_digits));
     hit_tol = stop <= tol;
     if (!resume) TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));  // e[0], e[1] adjacent
     TT_CHECK(cudaMemsetAsync(&c->sol->done, 0, sizeof(int), c->stream));
@@ -800,6 +801,10 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
       const int n = (int)(left < (1LL << 24) ? (left > 0 ? left : 1) : (1LL << 24));
       if ((rc = launch_sweeps32(c, n, period, stop, form)) || (rc = poll(c))) return rc;
       if (c->host_sol->nonfinite) status = TTFLD_E_NONFINITE;
+      if (c->host_sol->stalled) {
+        ++stalls;
+        TT_CHECK(cudaMemsetAsync(&c->sol->stalled, 0, sizeof(int), c->stream));
+      }
     }
     for (; !one_launch;) {
       if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop, kFormSplit))) return rc;
@@ -811,7 +816,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
       // iteration has reached its rounding floor relative to this anchor
       // (stiff, high-contrast systems put it well above 1e-5), so re-anchor
       // in FP64; restarting from e = 0 continues the same iteration
-      if (have_norm && h->iter - it_prev >= 16 && !(h->ratio < 0.999 * r_prev)) break;
+      if (have_norm && h->iter - it_prev >= 16 && !(h->ratio < 0.999 * r_prev)) { ++stalls; break; }
       // predict the sweeps left from the last two norms; queue about that many
       double rate = (h->iter > it_prev && h->ratio > 0.0 && r_prev > 0.0)
                         ? pow(h->ratio / r_prev, 1.0 / (h->iter - it_prev)) : 0.0;
@@ -836,6 +841,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     st->rnorm = l1;
     st->true_resid_l1 = l1;
     st->status = status;
+    st->stalls = stalls;
   }
   return status;
 }

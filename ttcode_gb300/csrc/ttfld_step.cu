@@ -238,6 +238,7 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
     st.sor_total += ss.sor_iter;
     st.solves += 1;
     st.fallbacks += ss.fallback;
+    st.stalls += ss.stalls;
     if (rc == TTFLD_MAXITER)
       printf("MAX COUPLED SOR ITERATION %8d %8d %12.6e\n", c->params.iii, energy_iter, ss.rnorm / ss.rhsnorm);
     TT_CHECK(cudaMemsetAsync(c->stp, 0, sizeof(StepDev), c->stream));
