@@ -153,7 +153,11 @@ typedef struct {
   int32_t inner_digits; /* mixed solver: an FP32 inner run on A e = r stops
                           once its in-sweep norm is 10^-inner_digits of the
                           FP64 anchor's (or at tol, or at the FP32 rounding
-                          floor); 0 = the default, 5                       */
+                          floor); 0 = the default, 4: on the stiff
+                          160x512x256 systems 5 reaches the FP32 rounding
+                          floor before the target (8208 sweeps against
+                          the FP64 loop's 7858), 3 and 4 do not (7864,
+                          7872)                                           */
   int32_t reserved;    /* set to 0                                         */
   int32_t max_sweeps;  /* mixed solver sweep budget (0 = ITMAX)            */
   int32_t fallback_rule; /* when a previous/learned guess is replaced by 0:

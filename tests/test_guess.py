@@ -199,3 +199,26 @@ def test_tcgen05_and_mma_sync_convolutions_agree():
     finally:
         f.L.ttfld_guess_set_conv(0)
     assert np.linalg.norm(preds[0] - preds[1]) <= 1e-3 * np.linalg.norm(preds[1])
+
+
+def test_seeded_training_is_reproducible():
+    """The backward pass adds its partial sums in a fixed order (no floating-
+    point atomics), so two trainings from the same seed on the same pairs give
+    the same weights bit for bit, and the learned guess the same sweep count."""
+    from ttcode_gb300 import guess
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(40, 64, 32, seed=2, delt=100.0)
+    blobs, sweeps = [], []
+    for _ in range(2):
+        f = start_run(sh)
+        guess.init(f, seed=1, capacity=4)
+        assert guess.capture_pairs(f, sh, guess.random_cases(4, seed=10)) == 4
+        for e in range(3):
+            guess.train(f, epochs=1, lr=5e-4, seed=e)
+        blobs.append(guess.save_weights(f))
+        case = guess.random_cases(1, seed=99)[0]
+        sweeps.append(guess.sweeps_with(f, sh, case, "learned")[0])
+        f.close()
+    assert blobs[0] == blobs[1]
+    assert sweeps[0] == sweeps[1]

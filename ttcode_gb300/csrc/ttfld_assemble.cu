@@ -165,170 +165,244 @@ static int qdens(ttfld_ctx* c) {
   return 0;
 }
 
-// FLIM pprphy.f:362-565 (IFLIMTYP 1 and 2, irad=3).  skip_kappa /
-// skip_qdens: KAPPA / QDENS already ran on the same T and rho in this step,
-// so their outputs would be recomputed bit for bit (:396-402).
-static int flim(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
-  if (energy_iter <= 1) {  // :396-402
+// ---- FLIM, DIFF, CALCULATEFLUX and FLUX_BC, one face at a time ---------
+// Each reference loop nest becomes a device function of one face with the
+// reference's operand order, so that a single kernel can form FLIM, DIFF
+// and the fluxes of a face together (bit for bit the values of the separate
+// loops).
+
+// FLIM's x loop body, pprphy.f:414-448 (IFLIMTYP 2).
+__device__ __forceinline__ double flimx_calc(const Dev& d, int i, int j, int k) {
+  const double sg = d.sigval;
+  double gradx = (HA(ER, i, j, k) - HA(ER, i - 1, j, k)) / G(dxb, i);
+  double grady = (G(ddx1, i) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
+                  G(ddx0, i) * (HA(ER, i - 1, j + 1, k) - HA(ER, i - 1, j - 1, k))) /
+                 (G(geoxga, i) * G(geozg, k) * (G(xyb, j + 1) - G(xyb, j - 1)));
+  double gradz = (G(ddx1, i) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
+                  G(ddx0, i) * (HA(ER, i - 1, j, k + 1) - HA(ER, i - 1, j, k - 1))) /
+                 (G(geoxha, i) * (G(xzb, k + 1) - G(xzb, k - 1)));
+  double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + 1.0e-50;
+  double rrx = 2.0 * grad /
+               (HA(RHQX, i, j, k) *
+                (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)) *
+                (HA(ER, i, j, k) + HA(ER, i - 1, j, k)));
+  return (2.0 + rrx) / (6.0 + 3.0 * rrx + rrx * rrx);
+}
+
+// FLIM's y loop body, pprphy.f:462-484.
+__device__ __forceinline__ double flimy_calc(const Dev& d, int i, int j, int k) {
+  const double sg = d.sigval;
+  double gradx = (G(ddy1, j) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
+                  G(ddy0, j) * (HA(ER, i + 1, j - 1, k) - HA(ER, i - 1, j - 1, k))) /
+                 (G(xxb, i + 1) - G(xxb, i - 1));
+  double grady = (HA(ER, i, j, k) - HA(ER, i, j - 1, k)) / (G(geoxg, i) * G(geozg, k) * G(dyb, j));
+  double gradz = (G(ddy1, j) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
+                  G(ddy0, j) * (HA(ER, i, j - 1, k + 1) - HA(ER, i, j - 1, k - 1))) /
+                 ((G(xzb, k + 1) - G(xzb, k - 1)) * G(geoxh, i));
+  double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + 1.0e-50;
+  double rry = 2.0 * grad /
+               (HA(RHQY, i, j, k) *
+                (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)) *
+                (HA(ER, i, j, k) + HA(ER, i, j - 1, k)));
+  return (2.0 + rry) / (6.0 + 3.0 * rry + rry * rry);
+}
+
+// FLIM's z loop body, pprphy.f:493-515.
+__device__ __forceinline__ double flimz_calc(const Dev& d, int i, int j, int k) {
+  const double sg = d.sigval;
+  double gradx = (G(ddz1, k) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
+                  G(ddz0, k) * (HA(ER, i + 1, j, k - 1) - HA(ER, i - 1, j, k - 1))) /
+                 (G(xxb, i + 1) - G(xxb, i - 1));
+  double grady = (G(ddz1, k) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
+                  G(ddz0, k) * (HA(ER, i, j + 1, k - 1) - HA(ER, i, j - 1, k - 1))) /
+                 ((G(xyb, j + 1) - G(xyb, j - 1)) * G(geoxg, i) * G(geozga, k));
+  double gradz = (HA(ER, i, j, k) - HA(ER, i, j, k - 1)) / (G(geoxh, i) * G(dzb, k));
+  double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + 1.0e-50;
+  double rrz = 2.0 * grad /
+               (HA(RHQZ, i, j, k) *
+                (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)) *
+                (HA(ER, i, j, k) + HA(ER, i, j, k - 1)));
+  return (2.0 + rrz) / (6.0 + 3.0 * rrz + rrz * rrz);
+}
+
+// FLIMX(i,j,k) as FLIM leaves it: formed for i <= UPPERBND-1 (:414-448),
+// the value of UPPERBND-1 above (:449-454; re-formed here from the same
+// inputs, so the same bits).  With UPPERBND <= 1 the face is neither formed
+// nor copied and the array keeps its value.
+__device__ __forceinline__ double flimx_at(const Dev& d, int i, int j, int k) {
+  if (d.iflimtyp == 1) return 1.0 / 3.0;
+  const int ub = PA(UB, j, k);
+  if (i <= ub - 1) return flimx_calc(d, i, j, k);
+  if (ub >= 2 && ub <= d.nx + 1) return flimx_calc(d, ub - 1, j, k);
+  return FA(FLIMX, i, j, k);
+}
+
+// The y and z loops form the faces up to the last x loop's xmax_index,
+// UPPERBND(NY,NZ)-1 (:464, :495); the copies of :485-489 and :516-520 then
+// give every face from UPPERBND(j,k) up the value of UPPERBND(j,k)-1.
+__device__ __forceinline__ double flimy_loop(const Dev& d, int i, int j, int k) {
+  return i <= PA(UB, d.ny, d.nz) - 1 ? flimy_calc(d, i, j, k) : FA(FLIMY, i, j, k);
+}
+__device__ __forceinline__ double flimy_at(const Dev& d, int i, int j, int k) {
+  if (d.iflimtyp == 1) return 1.0 / 3.0;
+  const int ub = PA(UB, j, k);
+  if (ub >= 2 && ub <= d.nx + 1 && i >= ub) return flimy_loop(d, ub - 1, j, k);
+  return flimy_loop(d, i, j, k);
+}
+__device__ __forceinline__ double flimz_loop(const Dev& d, int i, int j, int k) {
+  return i <= PA(UB, d.ny, d.nz) - 1 ? flimz_calc(d, i, j, k) : FA(FLIMZ, i, j, k);
+}
+__device__ __forceinline__ double flimz_at(const Dev& d, int i, int j, int k) {
+  if (d.iflimtyp == 1) return 1.0 / 3.0;
+  const int ub = PA(UB, j, k);
+  if (ub >= 2 && ub <= d.nx + 1 && i >= ub) return flimz_loop(d, ub - 1, j, k);
+  return flimz_loop(d, i, j, k);
+}
+
+// DIFF pprad.f:74-156, one face of each direction (with the ieta = 5 floor).
+__device__ __forceinline__ double difrx_of(const Dev& d, int i, int j, int k, double fl) {
+  const double sg = d.sigval;
+  double v = TT_FD * fl /
+             (G(dxb, i) * HA(RHQX, i, j, k) *
+              (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)));
+  if (d.ieta == 5) {
+    double mn = HA(RHQX, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                (G(dxb, i) * 4.0 * TT_ARAD * p3(G(ddx1, i) * HA(T, i, j, k) + G(ddx0, i) * HA(T, i - 1, j, k)) *
+                 d.pr_num);
+    v = fmax(v, mn);
+  }
+  return v;
+}
+__device__ __forceinline__ double difry_of(const Dev& d, int i, int j, int k, double fl) {
+  const double sg = d.sigval;
+  double v = TT_FD * fl /
+             (G(dyb, j) * G(geoxg, i) * G(geozg, k) * HA(RHQY, i, j, k) *
+              (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)));
+  if (d.ieta == 5) {
+    double mn = HA(RHQY, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                (G(dyb, j) * G(geoxg, i) * G(geozg, k) * 4.0 * TT_ARAD *
+                 p3(G(ddy1, j) * HA(T, i, j, k) + G(ddy0, j) * HA(T, i, j - 1, k)) * d.pr_num);
+    v = fmax(v, mn);
+  }
+  return v;
+}
+__device__ __forceinline__ double difrz_of(const Dev& d, int i, int j, int k, double fl) {
+  const double sg = d.sigval;
+  double v = TT_FD * fl /
+             (G(dzb, k) * G(geoxh, i) * HA(RHQZ, i, j, k) *
+              (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)));
+  if (d.ieta == 5) {
+    double mn = HA(RHQZ, i, j, k) * HA(CV, i, j, k) * d.xnue /
+                (G(dzb, k) * G(geoxh, i) * 4.0 * TT_ARAD *
+                 p3(G(ddz1, k) * HA(T, i, j, k) + G(ddz0, k) * HA(T, i, j, k - 1)) * d.pr_num);
+    v = fmax(v, mn);
+  }
+  return v;
+}
+
+// FLUX_X(i,j,k) as CALCULATEFLUX (ppenergy.f:880-920) and FLUX_BC (:922-982)
+// leave it, for i = 1..NX+1, j = 1..NY, k = 1..NZ: the diffusive flux, the
+// top value c E_R(UPPERBND-1)/2 from UPPERBND up, Fbottom on the first face.
+__device__ __forceinline__ double fluxx_final(const Dev& d, int i, int j, int k, double difr) {
+  double f = -difr * (HA(ER, i, j, k) - HA(ER, i - 1, j, k));
+  const int ub = PA(UB, j, k);
+  if (i >= ub && ub >= 1) f = TT_FD * HA(ER, ub - 1, j, k) / 2.0;
+  if (i == 1) f = d.fbottom;
+  return f;
+}
+
+// FLIM (MODE 0), FLIM + DIFF (1), or FLIM + DIFF + CALCULATEFLUX + FLUX_BC
+// (2) in one pass over the faces (1:NX+1,1:NY+1,1:NZ+1); each thread forms
+// the x, y and z faces that share its index.  KAPPA and QDENS, which FLIM
+// calls for energy_iter <= 1 (pprphy.f:396-402), run first unless they
+// already ran on the same T and rho in this step (skip_kappa / skip_qdens).
+template <int MODE>
+static int faces(ttfld_ctx* c, int energy_iter, bool skip_kappa, bool skip_qdens) {
+  if (energy_iter <= 1) {
     int rc;
     if (!skip_kappa && (rc = kappa(c))) return rc;
     if (!skip_qdens && (rc = qdens(c))) return rc;
   }
   Dev d = c->d;
-  const double sg = d.sigval;
-  if (d.iflimtyp == 1) {
-    launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
-      size_t q = fidx(d, i, j, k);
-      d.FLIMX[q] = 1.0 / 3.0; d.FLIMY[q] = 1.0 / 3.0; d.FLIMZ[q] = 1.0 / 3.0;
-    });
-    TT_CHECK_LAUNCH();
-    return 0;
-  }
-  const double xdmin = 1.0e-50;
-  // x-direction :414-448, i = 1..UPPERBND(j,k)-1
-  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
-    if (i > PA(UB, j, k) - 1) return;
-    double gradx = (HA(ER, i, j, k) - HA(ER, i - 1, j, k)) / G(dxb, i);
-    double grady = (G(ddx1, i) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
-                    G(ddx0, i) * (HA(ER, i - 1, j + 1, k) - HA(ER, i - 1, j - 1, k))) /
-                   (G(geoxga, i) * G(geozg, k) * (G(xyb, j + 1) - G(xyb, j - 1)));
-    double gradz = (G(ddx1, i) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
-                    G(ddx0, i) * (HA(ER, i - 1, j, k + 1) - HA(ER, i - 1, j, k - 1))) /
-                   (G(geoxha, i) * (G(xzb, k + 1) - G(xzb, k - 1)));
-    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
-    double rrx = 2.0 * grad /
-                 (HA(RHQX, i, j, k) *
-                  (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)) *
-                  (HA(ER, i, j, k) + HA(ER, i - 1, j, k)));
-    FA(FLIMX, i, j, k) = (2.0 + rrx) / (6.0 + 3.0 * rrx + rrx * rrx);
-  });
-  TT_CHECK_LAUNCH();
-  // :449-454
-  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
-    int ub = PA(UB, j, k);
-    if (ub < 2 || ub > d.nx + 1) return;  // UPPERBND outside the grid: no copy
-    if (i >= ub) FA(FLIMX, i, j, k) = FA(FLIMX, ub - 1, j, k);
-  });
-  TT_CHECK_LAUNCH();
-  // y and z loops reuse the last x-loop xmax_index (pprphy.f:464, 495)
-  // y-direction :462-484
-  launch_box(c->stream, box(1, d.nx, 1, d.ny + 1, 1, d.nz), [=] __device__(int i, int j, int k) {
-    int xmax_index = PA(UB, d.ny, d.nz) - 1;
-    if (i > xmax_index) return;
-    double gradx = (G(ddy1, j) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
-                    G(ddy0, j) * (HA(ER, i + 1, j - 1, k) - HA(ER, i - 1, j - 1, k))) /
-                   (G(xxb, i + 1) - G(xxb, i - 1));
-    double grady = (HA(ER, i, j, k) - HA(ER, i, j - 1, k)) / (G(geoxg, i) * G(geozg, k) * G(dyb, j));
-    double gradz = (G(ddy1, j) * (HA(ER, i, j, k + 1) - HA(ER, i, j, k - 1)) +
-                    G(ddy0, j) * (HA(ER, i, j - 1, k + 1) - HA(ER, i, j - 1, k - 1))) /
-                   ((G(xzb, k + 1) - G(xzb, k - 1)) * G(geoxh, i));
-    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
-    double rry = 2.0 * grad /
-                 (HA(RHQY, i, j, k) *
-                  (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)) *
-                  (HA(ER, i, j, k) + HA(ER, i, j - 1, k)));
-    FA(FLIMY, i, j, k) = (2.0 + rry) / (6.0 + 3.0 * rry + rry * rry);
-  });
-  TT_CHECK_LAUNCH();
-  // z-direction :493-515
-  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
-    int xmax_index = PA(UB, d.ny, d.nz) - 1;
-    if (i > xmax_index) return;
-    double gradx = (G(ddz1, k) * (HA(ER, i + 1, j, k) - HA(ER, i - 1, j, k)) +
-                    G(ddz0, k) * (HA(ER, i + 1, j, k - 1) - HA(ER, i - 1, j, k - 1))) /
-                   (G(xxb, i + 1) - G(xxb, i - 1));
-    double grady = (G(ddz1, k) * (HA(ER, i, j + 1, k) - HA(ER, i, j - 1, k)) +
-                    G(ddz0, k) * (HA(ER, i, j + 1, k - 1) - HA(ER, i, j - 1, k - 1))) /
-                   ((G(xyb, j + 1) - G(xyb, j - 1)) * G(geoxg, i) * G(geozga, k));
-    double gradz = (HA(ER, i, j, k) - HA(ER, i, j, k - 1)) / (G(geoxh, i) * G(dzb, k));
-    double grad = sqrt(gradx * gradx + grady * grady + gradz * gradz) + xdmin;
-    double rrz = 2.0 * grad /
-                 (HA(RHQZ, i, j, k) *
-                  (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)) *
-                  (HA(ER, i, j, k) + HA(ER, i, j, k - 1)));
-    FA(FLIMZ, i, j, k) = (2.0 + rrz) / (6.0 + 3.0 * rrz + rrz * rrz);
-  });
-  TT_CHECK_LAUNCH();
-  // :485-489 and :516-520 (the copies read only i = UPPERBND-1 values)
-  launch_box(c->stream, box(1, d.nx, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
-    int ub = PA(UB, j, k);
-    if (ub < 2 || ub > d.nx + 1 || i < ub) return;
-    if (k <= d.nz) FA(FLIMY, i, j, k) = FA(FLIMY, ub - 1, j, k);
-    if (j <= d.ny) FA(FLIMZ, i, j, k) = FA(FLIMZ, ub - 1, j, k);
-  });
-  TT_CHECK_LAUNCH();
-  return 0;
-}
-
-// DIFF pprad.f:74-156
-static int diff(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
-  int rc = flim(c, energy_iter, skip_kappa, skip_qdens);
-  if (rc) return rc;
-  Dev d = c->d;
-  const double sg = d.sigval;
   launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
     if (j <= d.ny && k <= d.nz) {
-      double v = TT_FD * FA(FLIMX, i, j, k) /
-                 (G(dxb, i) * HA(RHQX, i, j, k) *
-                  (G(ddx1, i) * (HA(XKAPR, i, j, k) + sg) + G(ddx0, i) * (HA(XKAPR, i - 1, j, k) + sg)));
-      if (d.ieta == 5) {
-        double mn = HA(RHQX, i, j, k) * HA(CV, i, j, k) * d.xnue /
-                    (G(dxb, i) * 4.0 * TT_ARAD *
-                     p3(G(ddx1, i) * HA(T, i, j, k) + G(ddx0, i) * HA(T, i - 1, j, k)) * d.pr_num);
-        v = fmax(v, mn);
+      const double fl = flimx_at(d, i, j, k);
+      FA(FLIMX, i, j, k) = fl;
+      if (MODE >= 1) {
+        const double dr = difrx_of(d, i, j, k, fl);
+        FA(DIFRX, i, j, k) = dr;
+        if (MODE == 2) FA(FLUXX, i, j, k) = fluxx_final(d, i, j, k, dr);
       }
-      FA(DIFRX, i, j, k) = v;
     }
     if (i <= d.nx && k <= d.nz) {
-      double v = TT_FD * FA(FLIMY, i, j, k) /
-                 (G(dyb, j) * G(geoxg, i) * G(geozg, k) * HA(RHQY, i, j, k) *
-                  (G(ddy1, j) * (HA(XKAPR, i, j, k) + sg) + G(ddy0, j) * (HA(XKAPR, i, j - 1, k) + sg)));
-      if (d.ieta == 5) {
-        double mn = HA(RHQY, i, j, k) * HA(CV, i, j, k) * d.xnue /
-                    (G(dyb, j) * G(geoxg, i) * G(geozg, k) * 4.0 * TT_ARAD *
-                     p3(G(ddy1, j) * HA(T, i, j, k) + G(ddy0, j) * HA(T, i, j - 1, k)) * d.pr_num);
-        v = fmax(v, mn);
+      const double fl = flimy_at(d, i, j, k);
+      FA(FLIMY, i, j, k) = fl;
+      if (MODE >= 1) {
+        const double dr = difry_of(d, i, j, k, fl);
+        FA(DIFRY, i, j, k) = dr;
+        if (MODE == 2) {
+          double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j - 1, k));
+          if (j <= d.ny) {  // FLUX_BC's loop covers j = 1..NY (:940-970)
+            const int ub = PA(UB, j, k);
+            if (i >= ub && ub >= 1) f = 0.0;
+          }
+          FA(FLUXY, i, j, k) = f;
+        }
       }
-      FA(DIFRY, i, j, k) = v;
     }
     if (i <= d.nx && j <= d.ny) {
-      double v = TT_FD * FA(FLIMZ, i, j, k) /
-                 (G(dzb, k) * G(geoxh, i) * HA(RHQZ, i, j, k) *
-                  (G(ddz1, k) * (HA(XKAPR, i, j, k) + sg) + G(ddz0, k) * (HA(XKAPR, i, j, k - 1) + sg)));
-      if (d.ieta == 5) {
-        double mn = HA(RHQZ, i, j, k) * HA(CV, i, j, k) * d.xnue /
-                    (G(dzb, k) * G(geoxh, i) * 4.0 * TT_ARAD *
-                     p3(G(ddz1, k) * HA(T, i, j, k) + G(ddz0, k) * HA(T, i, j, k - 1)) * d.pr_num);
-        v = fmax(v, mn);
+      const double fl = flimz_at(d, i, j, k);
+      FA(FLIMZ, i, j, k) = fl;
+      if (MODE >= 1) {
+        const double dr = difrz_of(d, i, j, k, fl);
+        FA(DIFRZ, i, j, k) = dr;
+        if (MODE == 2) {
+          double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j, k - 1));
+          if (k <= d.nz) {
+            const int ub = PA(UB, j, k);
+            if (i >= ub && ub >= 1) f = 0.0;
+          }
+          FA(FLUXZ, i, j, k) = f;
+        }
       }
-      FA(DIFRZ, i, j, k) = v;
     }
   });
   TT_CHECK_LAUNCH();
   return 0;
 }
 
-// CALCULATEFLUX ppenergy.f:880-920 followed by FLUX_BC ppenergy.f:922-982.
+static int diff(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
+  return faces<1>(c, energy_iter, skip_kappa, skip_qdens);
+}
 static int calculateflux(ttfld_ctx* c, int energy_iter, bool skip_kappa = false, bool skip_qdens = false) {
-  int rc = diff(c, energy_iter, skip_kappa, skip_qdens);
-  if (rc) return rc;
+  return faces<2>(c, energy_iter, skip_kappa, skip_qdens);
+}
+
+// The CALCULATEFLUX + FLUX_BC of COUPLED_ENERGY_EQS's set-up (ppenergy.f:
+// 74-75) as far as the step reads it: its only reader is the upper boundary
+// loop (:80-105), which takes FLUX_X at i >= UPPERBND(j,k), clamped into the
+// array for ghost j, k, i = NX+2; the call at :253-255 forms every face again
+// before anything else reads them.  Those faces are formed here from the
+// same inputs (after KAPPA and QDENS, which that FLIM call runs): from
+// UPPERBND up FLUX_BC's c E_R(UPPERBND-1)/2, below it (only reachable from a
+// ghost column whose UPPERBND differs from its clamped neighbour's) the full
+// FLIM, DIFF and flux of the face.
+int asm_top_fluxes(ttfld_ctx* c, bool kappa_done) {
+  int rc;
+  if (!kappa_done && (rc = kappa(c))) return rc;
+  if ((rc = qdens(c))) return rc;
   Dev d = c->d;
-  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
-    if (j <= d.ny && k <= d.nz)
-      FA(FLUXX, i, j, k) = -FA(DIFRX, i, j, k) * (HA(ER, i, j, k) - HA(ER, i - 1, j, k));
-    if (i <= d.nx && k <= d.nz)
-      FA(FLUXY, i, j, k) = -FA(DIFRY, i, j, k) * (HA(ER, i, j, k) - HA(ER, i, j - 1, k));
-    if (i <= d.nx && j <= d.ny)
-      FA(FLUXZ, i, j, k) = -FA(DIFRZ, i, j, k) * (HA(ER, i, j, k) - HA(ER, i, j, k - 1));
-  });
-  TT_CHECK_LAUNCH();
-  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
-    int ub = PA(UB, j, k);
-    if (i >= ub && ub >= 1) {
-      FA(FLUXX, i, j, k) = TT_FD * HA(ER, ub - 1, j, k) / 2.0;
-      if (i != d.nx + 1) { FA(FLUXY, i, j, k) = 0.0; FA(FLUXZ, i, j, k) = 0.0; }
-    }
-    if (i == 1) FA(FLUXX, 1, j, k) = d.fbottom;
+  launch_box(c->stream, box(1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    const int ub = PA(UB, j, k);
+    if (i < ub || ub < 1) return;
+    const int ic = i > d.nx + 1 ? d.nx + 1 : i;
+    const int jc = j < 1 ? 1 : (j > d.ny ? d.ny : j);
+    const int kc = k < 1 ? 1 : (k > d.nz ? d.nz : k);
+    const int ubc = PA(UB, jc, kc);
+    double f;
+    if (ic >= ubc && ubc >= 1) f = ic == 1 ? d.fbottom : TT_FD * HA(ER, ubc - 1, jc, kc) / 2.0;
+    else f = fluxx_final(d, ic, jc, kc, difrx_of(d, ic, jc, kc, flimx_at(d, ic, jc, kc)));
+    FA(FLUXX, ic, jc, kc) = f;   // threads that meet on one face write the same value
   });
   TT_CHECK_LAUNCH();
   return 0;
@@ -338,35 +412,68 @@ static int calculateflux(ttfld_ctx* c, int energy_iter, bool skip_kappa = false,
 static int fill_evalues(ttfld_ctx* c, double theta) {
   Dev d = c->d;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
-    size_t q = cidx(d, i, j, k);
-    double e1 = -G(surxa, i + 1) * FA(DIFRX, i + 1, j, k) / (G(surxb, i) * G(dxa, i));
-    double e2 = -G(surxa, i) * FA(DIFRX, i, j, k) / (G(surxb, i) * G(dxa, i));
-    double e3 = -FA(DIFRY, i, j + 1, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
-    double e4 = -FA(DIFRY, i, j, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
-    double e5 = -FA(DIFRZ, i, j, k + 1) * G(surza, k + 1) / (G(xxb, i) * G(surzb, k) * G(dza, k));
-    double e6 = -FA(DIFRZ, i, j, k) * G(surza, k) / (G(xxb, i) * G(surzb, k) * G(dza, k));
-    double eta = d.ETA[q];
-    d.E1[q] = e1; d.E2[q] = e2; d.E3[q] = e3; d.E4[q] = e4; d.E5[q] = e5; d.E6[q] = e6;
-    d.E7[q] = 1.0 + (1.0 - eta) * d.delt * HA(RH, i, j, k) * HA(XKAPP, i, j, k) * TT_FD;
-    d.E8[q] = (eta * (1.0 - theta) - 1.0) * d.delt;
-    d.E16[q] = e1 + e2 + e3 + e4 + e5 + e6;
+    const size_t q = cidx(d, i, j, k);
+    store_evalues(d, q, evalues_cell(d, i, j, k, theta, d.ETA[q]));
   });
   TT_CHECK_LAUNCH();
   return 0;
 }
 
-// CALCULATEDIVF_WITHF ppenergy.f:825-878, NCOSYS=2 (:853-867).
-static int divf_withf(ttfld_ctx* c, double* out, double theta, bool fill = true) {
+// CALCULATEDIVF_WITHF ppenergy.f:825-878, NCOSYS=2 (:853-867).  Its six
+// factors are quotients of grid metrics alone, so they are formed once per
+// context (the same operations on the same operands, so the same bits) and
+// the divergence of a cell costs six products and five sums:
+//   ax1(i) = surxa(i+1)/(surxb(i) dxa(i)),  ax0(i) = surxa(i)/(surxb(i) dxa(i)),
+//   ay(i,j,k) = 1/(xxb(i) surzb(k) dya(j)),
+//   az1(i,k) = surza(k+1)/(xxb(i) surzb(k) dza(k)),  az0(i,k) = surza(k)/(...).
+DivfTab divf_tab(ttfld_ctx* c) {
   Dev d = c->d;
+  const size_t nx = d.nx, nxz = (size_t)d.nx * d.nz;
+  DivfTab t;
+  t.ax1 = c->divf_tab;
+  t.ax0 = t.ax1 + nx;
+  t.az1 = t.ax0 + nx;
+  t.az0 = t.az1 + nxz;
+  t.ay = t.az0 + nxz;
+  return t;
+}
+
+static int ensure_divf_tab(ttfld_ctx* c) {
+  if (c->divf_tab) return 0;
+  Dev d = c->d;
+  const size_t n = 2 * (size_t)d.nx + 2 * (size_t)d.nx * d.nz + ncell(d);
+  TT_CHECK(cudaMalloc((void**)&c->divf_tab, n * sizeof(double)));
+  const DivfTab t = divf_tab(c);
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     double xb = G(xxb, i), szb = G(surzb, k);
-    double v = ((G(surxa, i + 1) / (G(surxb, i) * G(dxa, i))) * FA(FLUXX, i + 1, j, k) -
-                (G(surxa, i) / (G(surxb, i) * G(dxa, i))) * FA(FLUXX, i, j, k)) +
-               ((1.0 / (xb * szb * G(dya, j))) * FA(FLUXY, i, j + 1, k) -
-                (1.0 / (xb * szb * G(dya, j))) * FA(FLUXY, i, j, k)) +
-               ((G(surza, k + 1) / (xb * szb * G(dza, k))) * FA(FLUXZ, i, j, k + 1) -
-                (G(surza, k) / (xb * szb * G(dza, k))) * FA(FLUXZ, i, j, k));
-    out[cidx(d, i, j, k)] = v;
+    if (j == 1 && k == 1) {
+      t.ax1[i - 1] = G(surxa, i + 1) / (G(surxb, i) * G(dxa, i));
+      t.ax0[i - 1] = G(surxa, i) / (G(surxb, i) * G(dxa, i));
+    }
+    if (j == 1) {
+      t.az1[(i - 1) + (size_t)d.nx * (k - 1)] = G(surza, k + 1) / (xb * szb * G(dza, k));
+      t.az0[(i - 1) + (size_t)d.nx * (k - 1)] = G(surza, k) / (xb * szb * G(dza, k));
+    }
+    t.ay[cidx(d, i, j, k)] = 1.0 / (xb * szb * G(dya, j));
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+void asm_free(ttfld_ctx* c) {
+  if (c->divf_tab) cudaFree(c->divf_tab);
+  c->divf_tab = nullptr;
+}
+
+int asm_prepare(ttfld_ctx* c) { return ensure_divf_tab(c); }
+
+static int divf_withf(ttfld_ctx* c, double* out, double theta, bool fill = true) {
+  int rc = ensure_divf_tab(c);
+  if (rc) return rc;
+  Dev d = c->d;
+  const DivfTab t = divf_tab(c);
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    out[cidx(d, i, j, k)] = divf_cell(d, t, i, j, k);
   });
   TT_CHECK_LAUNCH();
   return fill ? fill_evalues(c, theta) : 0;
@@ -394,15 +501,14 @@ static int stellarinput_heating(ttfld_ctx* c) {
     }
   });
   TT_CHECK_LAUNCH();
+  // STELLAR_DTAU and STELLARINPUT of the same cell in one pass
   launch_box(c->stream, box(1, d.nx + 1, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
     int is = i < 2 ? 2 : (i > d.nx ? d.nx : i);  // dtaus(1)=dtaus(2), dtaus(NX+1)=dtaus(NX)
-    HA(DTAUS, i, j, k) = (HA(STAU, is - 1, j, k) - HA(STAU, is + 1, j, k)) / 2.0;
-  });
-  TT_CHECK_LAUNCH();
-  launch_box(c->stream, box(1, d.nx, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    const double dtaus = (HA(STAU, is - 1, j, k) - HA(STAU, is + 1, j, k)) / 2.0;
+    HA(DTAUS, i, j, k) = dtaus;
+    if (i > d.nx) return;
     double tinc = PA(TINC, j, k), mu = PA(MU, j, k);
-    HA(SI, i, j, k) = TT_SBCONST * (p4(tinc) / mu) * (exp(-HA(STAU, i, j, k) / mu)) * HA(DTAUS, i, j, k) /
-                      G(dxb, i);
+    HA(SI, i, j, k) = TT_SBCONST * (p4(tinc) / mu) * (exp(-HA(STAU, i, j, k) / mu)) * dtaus / G(dxb, i);
   });
   TT_CHECK_LAUNCH();
   return 0;

@@ -186,7 +186,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   c->opts.solver = TTFLD_SOLVER_SOR64_EXACT;
   c->opts.guess = TTFLD_GUESS_ZERO;
   c->opts.tol = 1e-10;
-  c->opts.inner_digits = 5;
+  c->opts.inner_digits = 4;
   c->opts.fallback_rule = 3;
   c->prev_scale = 0.9;
   Dev& d = c->d;
@@ -278,6 +278,7 @@ int ttfld_destroy(ttfld_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   unet_free(c);
+  asm_free(c);
   mix_free(c);
   krylov_free(c);
   if (c->opac) cudaFree(c->opac);
@@ -315,7 +316,7 @@ int ttfld_set_solver(ttfld_ctx* c, const ttfld_solve_opts* o) {
   if (o->fallback_rule < 0 || o->fallback_rule > 3) return TTFLD_E_ARGS;
   if (o->sweep_form < 0 || o->sweep_form > 2) return TTFLD_E_ARGS;
   c->opts = *o;
-  if (c->opts.inner_digits <= 0) c->opts.inner_digits = 5;
+  if (c->opts.inner_digits <= 0) c->opts.inner_digits = 4;
   if (c->opts.inner_digits > 12) c->opts.inner_digits = 12;
   return TTFLD_OK;
 }

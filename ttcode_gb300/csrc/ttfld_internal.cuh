@@ -270,6 +270,7 @@ struct ttfld_ctx {
   void* krylov;             // PCG workspace (allocated on first use)
   void* opac;               // opacity table of kappa_model 2 (device), with its sizes
   int opac_nt, opac_nrh;
+  double* divf_tab;         // metric quotients of CALCULATEDIVF_WITHF (allocated on first use)
   double last_solve_ms;
 };
 
@@ -295,6 +296,65 @@ int halo_shift(ttfld_ctx* c, double* a);
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);
 int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1);
 int unet_guess(ttfld_ctx* c, double* x_out, double* resid_l1);
+void asm_free(ttfld_ctx* c);
+
+// The metric quotients of CALCULATEDIVF_WITHF (ppenergy.f:853-867), formed
+// once per context: ax1/ax0 per i, az1/az0 per (i,k), ay per cell.
+struct DivfTab {
+  double *ax1, *ax0, *az1, *az0, *ay;
+};
+DivfTab divf_tab(ttfld_ctx* c);
+
+// FILL_EVALUES ppenergy.f:984-1030 for one cell, given its eta.
+struct EvalRow {
+  double e1, e2, e3, e4, e5, e6, e7, e8, e16;
+};
+__device__ __forceinline__ EvalRow evalues_cell(const Dev& d, int i, int j, int k, double theta, double eta) {
+  EvalRow r;
+  r.e1 = -G(surxa, i + 1) * FA(DIFRX, i + 1, j, k) / (G(surxb, i) * G(dxa, i));
+  r.e2 = -G(surxa, i) * FA(DIFRX, i, j, k) / (G(surxb, i) * G(dxa, i));
+  r.e3 = -FA(DIFRY, i, j + 1, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
+  r.e4 = -FA(DIFRY, i, j, k) / (G(xxb, i) * G(surzb, k) * G(dya, j));
+  r.e5 = -FA(DIFRZ, i, j, k + 1) * G(surza, k + 1) / (G(xxb, i) * G(surzb, k) * G(dza, k));
+  r.e6 = -FA(DIFRZ, i, j, k) * G(surza, k) / (G(xxb, i) * G(surzb, k) * G(dza, k));
+  r.e7 = 1.0 + (1.0 - eta) * d.delt * HA(RH, i, j, k) * HA(XKAPP, i, j, k) * TT_FD;
+  r.e8 = (eta * (1.0 - theta) - 1.0) * d.delt;
+  r.e16 = r.e1 + r.e2 + r.e3 + r.e4 + r.e5 + r.e6;
+  return r;
+}
+__device__ __forceinline__ void store_evalues(const Dev& d, size_t q, const EvalRow& r) {
+  d.E1[q] = r.e1; d.E2[q] = r.e2; d.E3[q] = r.e3; d.E4[q] = r.e4; d.E5[q] = r.e5; d.E6[q] = r.e6;
+  d.E7[q] = r.e7; d.E8[q] = r.e8; d.E16[q] = r.e16;
+}
+
+// FILL_SOR_MATRIX ppsor.f:189-277 for one cell from its EVAL values, with
+// B_VECTOR_BOUNDARIES (ppsor.f:280-329): returns true for the identity rows
+// whose right-hand side is zero.
+__device__ __forceinline__ bool sor_row(const Dev& d, int i, int j, int k, size_t q, const EvalRow& r) {
+  double e8 = r.e8;
+  double a = r.e7 + e8 * r.e16;
+  double b = -e8 * r.e2, cc = -e8 * r.e1, dd = -e8 * r.e4;
+  double e = -e8 * r.e3, f = -e8 * r.e6, g = -e8 * r.e5;
+  int ub = PA(UB, j, k);
+  bool ident = (i >= ub) || (i == d.nx) || (k == 1) || (k == d.nz);
+  if (ident) { a = 1.0; b = 0.0; cc = 0.0; dd = 0.0; e = 0.0; f = 0.0; g = 0.0; }
+  if (i == ub - 1) cc = 0.0;
+  if (i == d.nx - 1) cc = 0.0;
+  if (k == 2) f = 0.0;
+  if (k == d.nz - 1) g = 0.0;
+  d.SA[q] = a; d.SB[q] = b; d.SC[q] = cc; d.SD[q] = dd; d.SE[q] = e; d.SF[q] = f; d.SG[q] = g;
+  return ident;
+}
+
+// The divergence of the fluxes of cell (i,j,k), in the reference's operand
+// order with its metric quotients read from the table.
+__device__ __forceinline__ double divf_cell(const Dev& d, const DivfTab& t, int i, int j, int k) {
+  const size_t ik = (size_t)(i - 1) + (size_t)d.nx * (k - 1);
+  const double ay = t.ay[cidx(d, i, j, k)];
+  return ((t.ax1[i - 1] * FA(FLUXX, i + 1, j, k) - t.ax0[i - 1] * FA(FLUXX, i, j, k)) +
+          (ay * FA(FLUXY, i, j + 1, k) - ay * FA(FLUXY, i, j, k))) +
+         (t.az1[ik] * FA(FLUXZ, i, j, k + 1) - t.az0[ik] * FA(FLUXZ, i, j, k));
+}
 int unet_capture(ttfld_ctx* c);
 void unet_free(ttfld_ctx* c);
 }  // namespace ttfld

@@ -723,7 +723,8 @@ static int poll(ttfld_ctx* c) {
 
 // Defect correction: anchor r = b - A x in FP64, run FP32 sweeps on
 // A e = r until the in-sweep norm of x + e has dropped by 10^-inner_digits
-// (default 1e-5, well inside FP32 precision) relative to the anchor or
+// (default 1e-4, inside FP32's reach even on the stiff shells) relative to
+// the anchor or
 // reached tol, x += e, repeat;
 // stop when the FP64 ||b - A x||_1 / ||b||_1 <= tol.
 //

@@ -21,20 +21,11 @@ namespace ttfld {
 int fill_sor_matrix(ttfld_ctx* c, bool zero_rhs) {
   Dev d = c->d;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
-    size_t q = cidx(d, i, j, k);
-    double e8 = d.E8[q];
-    double a = d.E7[q] + e8 * d.E16[q];
-    double b = -e8 * d.E2[q], cc = -e8 * d.E1[q], dd = -e8 * d.E4[q];
-    double e = -e8 * d.E3[q], f = -e8 * d.E6[q], g = -e8 * d.E5[q];
-    int ub = PA(UB, j, k);
-    bool ident = (i >= ub) || (i == d.nx) || (k == 1) || (k == d.nz);
-    if (ident) { a = 1.0; b = 0.0; cc = 0.0; dd = 0.0; e = 0.0; f = 0.0; g = 0.0; }
-    if (i == ub - 1) cc = 0.0;
-    if (i == d.nx - 1) cc = 0.0;
-    if (k == 2) f = 0.0;
-    if (k == d.nz - 1) g = 0.0;
-    d.SA[q] = a; d.SB[q] = b; d.SC[q] = cc; d.SD[q] = dd; d.SE[q] = e; d.SF[q] = f; d.SG[q] = g;
-    if (ident && zero_rhs) d.RHS[q] = 0.0;
+    const size_t q = cidx(d, i, j, k);
+    EvalRow r;
+    r.e1 = d.E1[q]; r.e2 = d.E2[q]; r.e3 = d.E3[q]; r.e4 = d.E4[q]; r.e5 = d.E5[q]; r.e6 = d.E6[q];
+    r.e7 = d.E7[q]; r.e8 = d.E8[q]; r.e16 = d.E16[q];
+    if (sor_row(d, i, j, k, q, r) && zero_rhs) d.RHS[q] = 0.0;
   });
   TT_CHECK_LAUNCH();
   return 0;

@@ -14,6 +14,8 @@ int asm_fill_evalues(ttfld_ctx* c, double theta);
 int asm_divf(ttfld_ctx* c, double* out, double theta, bool fill = true);
 int asm_stellar(ttfld_ctx* c);
 int asm_bounds(ttfld_ctx* c);
+int asm_top_fluxes(ttfld_ctx* c, bool kappa_done);
+int asm_prepare(ttfld_ctx* c);
 int solve_delta_er(ttfld_ctx* c, ttfld_solve_stats* st);
 
 // Q/E_R upper boundary, ppenergy.f:80-105 and :678-702.  FLUX_X is declared
@@ -81,11 +83,20 @@ static int z_bc(ttfld_ctx* c) {
   return 0;
 }
 
-// Per-cell FQ, FR, Jacobian, eta and RHS_ER, ppenergy.f:287-345.
-static int jacobian(ttfld_ctx* c, double theta) {
+// One pass over the cells for an outer iteration's linear system:
+// CALCULATEDIVF_WITHF's divergence (ppenergy.f:285, from the metric-quotient
+// table; in the first iteration the fluxes are those DIVF_OLD was formed
+// from, so DIVF is DIVF_OLD), the per-cell FQ, FR, Jacobian, eta and RHS_ER
+// (:287-345), FILL_EVALUES (:348), and FILL_SOR_MATRIX with
+// B_VECTOR_BOUNDARIES (ppsor.f:24-26).  Each cell reads only its own cell
+// values and its faces, so fusing the loops keeps every value bit for bit.
+static int rows(ttfld_ctx* c, double theta, bool divf_is_old) {
   Dev d = c->d;
+  const DivfTab t = divf_tab(c);
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
     size_t h = hidx(d, i, j, k), q = cidx(d, i, j, k);
+    const double divf = divf_is_old ? d.DIVF_OLD[q] : divf_cell(d, t, i, j, k);
+    d.DIVF[q] = divf;
     double qq = d.Q[h], rh = d.RH[h], cv = d.CV[h], er = d.ER[h], kp = d.XKAPP[h];
     double qr = qq / (rh * cv);
     double bb = TT_ARAD * p4(qr);
@@ -94,20 +105,23 @@ static int jacobian(ttfld_ctx* c, double theta) {
     if (d.f_incident > 1) {
       double si = d.SI[h];
       double heat = si / (rh * d.XKAPA[h]);
-      fq = qq - d.Q_OLD[h] + d.delt * ((1 - theta) * (d.DIVF_OLD[q] - d.DIVF[q]) + (rh * kp * TT_FD * (bb - er)) - si);
+      fq = qq - d.Q_OLD[h] + d.delt * ((1 - theta) * (d.DIVF_OLD[q] - divf) + (rh * kp * TT_FD * (bb - er)) - si);
       dfq = 1.0 + (d.delt / cv) * (kp * 4.0 * TT_ARAD * TT_FD * p3(qr) + (TT_FD * (bb - er) * d.DXKAPP[h]) -
                                    heat * d.DXKAPA[h]);
     } else {
-      fq = qq - d.Q_OLD[h] + d.delt * ((1 - theta) * (d.DIVF_OLD[q] - d.DIVF[q]) + rh * kp * TT_FD * (bb - er));
+      fq = qq - d.Q_OLD[h] + d.delt * ((1 - theta) * (d.DIVF_OLD[q] - divf) + rh * kp * TT_FD * (bb - er));
       dfq = 1.0 + (d.delt / cv) * (kp * 4.0 * TT_ARAD * TT_FD * p3(qr) + TT_FD * (bb - er) * d.DXKAPP[h]);
     }
-    double fr = er - d.ER_OLD[h] + d.delt * (d.DIVF[q] - rh * kp * TT_FD * (bb - er));
+    double fr = er - d.ER_OLD[h] + d.delt * (divf - rh * kp * TT_FD * (bb - er));
     d.FQ[q] = fq; d.FR[q] = fr; d.DFQ[q] = dfq; d.DFR[q] = dfr;
     double eta;
     if (dfq != 0.0) eta = -dfr / dfq;
     else { eta = 0.0; d.stp->dfq_zero = 1; }
     d.ETA[q] = eta;
-    d.RHS[q] = -fr - eta * fq;
+    const EvalRow e = evalues_cell(d, i, j, k, theta, eta);
+    store_evalues(d, q, e);
+    const bool ident = sor_row(d, i, j, k, q, e);
+    d.RHS[q] = ident ? 0.0 : -fr - eta * fq;
   });
   TT_CHECK_LAUNCH();
   return 0;
@@ -205,7 +219,10 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
     if ((rc = asm_kappa(c)) || (rc = asm_stellar(c))) return rc;
     kappa_done = true;
   }
-  if ((rc = asm_calculateflux(c, 0, kappa_done, false))) return rc;     // :74-75
+  if ((rc = asm_prepare(c))) return rc;
+  // :74-75: only the top faces' fluxes are read (by :80-105) before :253-255
+  // forms every face again
+  if ((rc = asm_top_fluxes(c, kappa_done))) return rc;
   if ((rc = upper_bc(c)) || (rc = left_bc(c)) || (rc = z_bc(c))) return rc;
   if ((rc = halo_shift(c, d.ER))) return rc;                            // :230-245
   TT_CHECK(cudaMemcpyAsync(d.Q_OLD, d.Q, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
@@ -223,14 +240,12 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
     // shift just done repeats the one of :230-245, and FLIM at energy_iter
     // 0 and 1 takes the same branch (:396-402) -- so they are not formed again.
     if (energy_iter > 1 && (rc = asm_calculateflux(c, energy_iter))) return rc;
-    if ((rc = asm_divf(c, d.DIVF, theta, false))) return rc;
-    if ((rc = jacobian(c, theta))) return rc;                           // :287-345
-    if ((rc = asm_fill_evalues(c, theta))) return rc;                   // :348
+    if ((rc = rows(c, theta, energy_iter == 1))) return rc;             // :285-348, ppsor.f:24-26
     if (c->params.adjust_sor && energy_iter == 1 && (c->params.iii % 10000 == 0 || c->params.iii == 1)) {
       if ((rc = ttfld_adjust_sor_param(c, nullptr))) return rc;         // :372-374
       d = c->d;
+      if ((rc = fill_sor_matrix(c))) return rc;
     }
-    if ((rc = fill_sor_matrix(c))) return rc;                           // ppsor.f:24-26
     ttfld_solve_stats ss{};
     rc = solve_delta_er(c, &ss);                                        // :375
     if (rc < 0) return rc;

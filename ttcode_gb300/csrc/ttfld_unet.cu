@@ -549,15 +549,18 @@ static int conv_fwd(cudaStream_t s, const ConvArgs& a) {
 }
 
 // ---- weight gradient ------------------------------------------------------
-// dW[tap][co][ci] += sum_v dZ[v][co] * X[v shifted by tap][ci]: per warp one
+// dW[tap][co][ci] = sum_v dZ[v][co] * X[v shifted by tap][ci]: per warp one
 // tap, 16 output channels (A = dZ^T, 16 x 16 voxels) and all input channels
 // (B = shifted X, 16 voxels x 8 channels per n-block), over a chunk of voxels.
+// Each warp stores its chunk's sums (no atomics); a second pass adds the
+// chunks in chunk order, so a training run is reproducible bit for bit.
+constexpr long long kWgradWarps = 9728;  // about one wave of warps (152 SMs x 64)
 struct WgradArgs {
   const bf16* dz;
   int dz_cs, dz_co, cout;
   const bf16* x;
   int x_cs, x_co, cin;  // cin % 8 == 0 (the padded input width)
-  float* dw;            // [27][cout][cin]
+  float* part;          // [chunk][27][cout][cin] per-chunk sums
   int X, Y, Z;
   long long chunk;      // voxels per warp (multiple of 16)
 };
@@ -617,29 +620,41 @@ __global__ void __launch_bounds__(256) conv3_wgrad_kernel(WgradArgs a) {
       mma_bf16(acc[nb], a0, a1, a2, a3, pack2(x0, x1), pack2(x2, x3));
     }
   }
-  // C: (row = co r / r+8, col = ci nb*8+cq, +1)
-  float* dwt = a.dw + (size_t)tap * a.cout * a.cin;
+  // C: (row = co r / r+8, col = ci nb*8+cq, +1), into this chunk's slice
+  float* dwt = a.part + ((size_t)ck * 27 + tap) * a.cout * a.cin;
 #pragma unroll
   for (int nb = 0; nb < NB; ++nb) {
     const int ci = nb * 8 + cq;
-    atomicAdd(dwt + (size_t)(ct * 16 + r) * a.cin + ci, acc[nb][0]);
-    atomicAdd(dwt + (size_t)(ct * 16 + r) * a.cin + ci + 1, acc[nb][1]);
-    atomicAdd(dwt + (size_t)(ct * 16 + r + 8) * a.cin + ci, acc[nb][2]);
-    atomicAdd(dwt + (size_t)(ct * 16 + r + 8) * a.cin + ci + 1, acc[nb][3]);
+    *reinterpret_cast<float2*>(dwt + (size_t)(ct * 16 + r) * a.cin + ci) = make_float2(acc[nb][0], acc[nb][1]);
+    *reinterpret_cast<float2*>(dwt + (size_t)(ct * 16 + r + 8) * a.cin + ci) = make_float2(acc[nb][2], acc[nb][3]);
   }
 }
 
-static int conv_wgrad(cudaStream_t s, WgradArgs a) {
+// out[c] = sum over b = 0..nb-1 of part[b * C + c], added in b order
+// (accumulate: out[c] += that sum).
+template <class T>
+__global__ void sum_parts_kernel(const T* part, int nb, long long C, T* out, int accumulate) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < C; c += (long long)gridDim.x * blockDim.x) {
+    T s = 0;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)b * C + c];
+    out[c] = accumulate ? out[c] + s : s;
+  }
+}
+
+// Weight gradient of one layer into dw [27][cout][cin] (written).
+static int conv_wgrad(cudaStream_t s, WgradArgs a, float* dw) {
   if (a.cout % 16 || a.cin % 8) return TTFLD_E_ARGS;
   const long long V = (long long)a.X * a.Y * a.Z;
-  // about one full wave of warps (152 SMs x 64 warps), each reducing a long
-  // run of voxels before its atomics, so the atomics stay few
+  // at most one full wave of warps, each summing a long run of voxels
   const long long tiles = 27LL * (a.cout / 16);
-  long long chunk = (V * tiles + 9727) / 9728;
+  long long nch = kWgradWarps / tiles;
+  if (nch < 1) nch = 1;
+  long long chunk = (V + nch - 1) / nch;
   chunk = (chunk + 15) / 16 * 16;
   if (chunk < 16) chunk = 16;
   a.chunk = chunk;
-  const long long warps = 27LL * (a.cout / 16) * ((V + chunk - 1) / chunk);
+  nch = (V + chunk - 1) / chunk;   // <= kWgradWarps / tiles: the partials fit max_wpart()
+  const long long warps = tiles * nch;
   const int blocks = (int)((warps * 32 + 255) / 256);
   switch (a.cin / 8) {
     case 2: conv3_wgrad_kernel<2><<<blocks, 256, 0, s>>>(a); break;
@@ -650,7 +665,9 @@ static int conv_wgrad(cudaStream_t s, WgradArgs a) {
     case 16: conv3_wgrad_kernel<16><<<blocks, 256, 0, s>>>(a); break;
     default: return TTFLD_E_UNSUPPORTED;
   }
-  count_launches(1);
+  const long long C = 27LL * a.cout * a.cin;
+  sum_parts_kernel<float><<<grid_for(C), 256, 0, s>>>(a.part, (int)nch, C, dw, 0);
+  count_launches(2);
   TT_CHECK_LAUNCH();
   return 0;
 }
@@ -668,8 +685,9 @@ __global__ void act_bwd_kernel(bf16* dy, int dy_cs, int dy_co, const bf16* y, in
   }
 }
 
-// bias gradient: db[c] += sum_v dZ[v][c]
-__global__ void bias_grad_kernel(const bf16* dz, int cs, int co, int C, long long V, float* db) {
+// bias gradient, per block: part[block][c] = sum over the block's voxels of
+// dZ[v][c] (the blocks' sums are added in block order afterwards)
+__global__ void bias_grad_kernel(const bf16* dz, int cs, int co, int C, long long V, float* part) {
   __shared__ float sh[64 * 8];
   const int c = threadIdx.x % C, lanes = blockDim.x / C, l = threadIdx.x / C;
   float acc = 0.f;
@@ -681,7 +699,7 @@ __global__ void bias_grad_kernel(const bf16* dz, int cs, int co, int C, long lon
   if (threadIdx.x < C) {
     float t = 0.f;
     for (int q = 0; q < lanes; ++q) t += sh[q * C + threadIdx.x];
-    atomicAdd(db + threadIdx.x, t);
+    part[(size_t)blockIdx.x * C + threadIdx.x] = t;
   }
 }
 
@@ -777,19 +795,22 @@ __global__ void head_fwd_kernel(const bf16* a13, const float* w, float* pred, lo
 }
 
 __global__ void loss_kernel(const float* pred, const float* target, const unsigned char* mask, long long V, double inv_n,
-                            float* gpred, double* loss) {
+                            float* gpred, double* part) {
+  __shared__ double sh[32];
   double acc = 0.0;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
     const float d = mask[v] ? pred[v] - target[v] : 0.f;
     acc += (double)d * d;
     gpred[v] = (float)(2.0 * inv_n) * d;
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc * inv_n);
+  const double b = block_sum(acc * inv_n, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
 }
 
-// d(a13)[v][c] = gpred[v] * w[c]; dw[c] += sum gpred * a13; db += sum gpred
-__global__ void head_bwd_kernel(const float* gpred, const bf16* a13, const float* w, bf16* ga13, float* gw, long long V) {
+// d(a13)[v][c] = gpred[v] * w[c]; per block: part[block][c] = sum gpred * a13,
+// part[block][16] = sum gpred (added in block order afterwards)
+__global__ void head_bwd_kernel(const float* gpred, const bf16* a13, const float* w, bf16* ga13, float* part, long long V) {
+  __shared__ float sh[17][32];
   float acc[17];
   for (int c = 0; c < 17; ++c) acc[c] = 0.f;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
@@ -801,10 +822,17 @@ __global__ void head_bwd_kernel(const float* gpred, const bf16* a13, const float
     }
     acc[16] += g;
   }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   for (int c = 0; c < 17; ++c) {
     float s = acc[c];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(gw + c, s);
+    if (lane == 0) sh[c][wp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 17) {
+    float t = 0.f;
+    for (int q = 0; q < nw; ++q) t += sh[threadIdx.x][q];
+    part[(size_t)blockIdx.x * 17 + threadIdx.x] = t;
   }
 }
 
@@ -1133,7 +1161,19 @@ int forward(ttfld_ctx* c) {
 
 // Backward of one conv layer: dY (in place -> dZ), weight/bias gradients,
 // and (when gx != null) the input gradient, written or accumulated.
-int conv_backward(ttfld_ctx* c, float* gpad, int l, bf16* gy, int gy_cs, int gy_co, const bf16* y, int y_cs, int y_co,
+// Gradient workspace of one training call: the padded weight gradient of a
+// layer, the per-chunk weight-gradient sums, and the per-block sums of the
+// bias, head and loss reductions (each added in a fixed order).
+constexpr int kMaxGradBlocks = 4096;  // >= any grid_for() grid
+struct GradWork {
+  float* gpad;   // max_wpad()
+  float* wpart;  // max_wpart()
+  float* bpart;  // kMaxGradBlocks x 64
+  float* hpart;  // kMaxGradBlocks x 17
+  double* lpart; // kMaxGradBlocks
+};
+
+int conv_backward(ttfld_ctx* c, GradWork* gw, int l, bf16* gy, int gy_cs, int gy_co, const bf16* y, int y_cs, int y_co,
                   const bf16* x, int x_cs, int x_co, bf16* gx, int gx_cs, int gx_co, int accum, int lev) {
   Net* n = net_of(c);
   const LayerSpec& s = kLayers[l];
@@ -1141,12 +1181,13 @@ int conv_backward(ttfld_ctx* c, float* gpad, int l, bf16* gy, int gy_cs, int gy_
   const long long V = L(lev).vox();
   int rc;
   act_bwd_kernel<<<GRID(V * s.cout), 256, 0, st>>>(gy, gy_cs, gy_co, y, y_cs, y_co, s.cout, V);
-  bias_grad_kernel<<<GRID(V / 8 + 1), 512, 0, st>>>(gy, gy_cs, gy_co, s.cout, V, n->g + n->boff[l]);
-  count_launches(2);
-  TT_CHECK(cudaMemsetAsync(gpad, 0, (size_t)27 * s.cout * s.cin_pad * 4, st));
-  WgradArgs wa{gy, gy_cs, gy_co, s.cout, x, x_cs, x_co, s.cin_pad, gpad, L(lev).X, L(lev).Y, L(lev).Z, 0};
-  if ((rc = conv_wgrad(st, wa))) return rc;
-  wgrad_fold_kernel<<<GRID(27LL * s.cout * s.cin), 256, 0, st>>>(gpad, s.cin, s.cin_pad, s.cout, n->g + n->woff[l]);
+  const int bblocks = GRID(V / 8 + 1);
+  bias_grad_kernel<<<bblocks, 512, 0, st>>>(gy, gy_cs, gy_co, s.cout, V, gw->bpart);
+  sum_parts_kernel<float><<<1, 64, 0, st>>>(gw->bpart, bblocks, s.cout, n->g + n->boff[l], 1);
+  count_launches(3);
+  WgradArgs wa{gy, gy_cs, gy_co, s.cout, x, x_cs, x_co, s.cin_pad, gw->wpart, L(lev).X, L(lev).Y, L(lev).Z, 0};
+  if ((rc = conv_wgrad(st, wa, gw->gpad))) return rc;
+  wgrad_fold_kernel<<<GRID(27LL * s.cout * s.cin), 256, 0, st>>>(gw->gpad, s.cin, s.cin_pad, s.cout, n->g + n->woff[l]);
   count_launches(1);
   if (gx) {
     ConvArgs a;
@@ -1163,7 +1204,7 @@ int conv_backward(ttfld_ctx* c, float* gpad, int l, bf16* gy, int gy_cs, int gy_
 }
 
 // Loss against n->target/mask and the gradients of every parameter (n->g).
-int backward(ttfld_ctx* c, float* gpad, double* loss_out) {
+int backward(ttfld_ctx* c, GradWork* gw, double* loss_out) {
   Net* n = net_of(c);
   cudaStream_t s = c->stream;
   const long long V0 = L(0).vox(), VF = n->full.vox();
@@ -1179,12 +1220,15 @@ int backward(ttfld_ctx* c, float* gpad, double* loss_out) {
     for (unsigned char m : hm) nmask += m;
   }
   const double inv_n = 1.0 / (double)(nmask > 0 ? nmask : 1);
-  loss_kernel<<<GRID(VF), 256, 0, s>>>(n->pred, n->target, n->mask, VF, inv_n, n->gpred, n->loss_acc);
+  const int lblocks = GRID(VF), hblocks = GRID(V0);
+  loss_kernel<<<lblocks, 256, 0, s>>>(n->pred, n->target, n->mask, VF, inv_n, n->gpred, gw->lpart);
+  sum_parts_kernel<double><<<1, 32, 0, s>>>(gw->lpart, lblocks, 1, n->loss_acc, 0);
   pred_down_kernel<<<GRID(V0), 256, 0, s>>>(n->gpred, n->full, n->gpred_half, L(0));
-  head_bwd_kernel<<<GRID(V0), 256, 0, s>>>(n->gpred_half, n->a13, n->p + n->hoff, n->g_a13, n->g + n->hoff, V0);
-  count_launches(3);
+  head_bwd_kernel<<<hblocks, 256, 0, s>>>(n->gpred_half, n->a13, n->p + n->hoff, n->g_a13, gw->hpart, V0);
+  sum_parts_kernel<float><<<1, 32, 0, s>>>(gw->hpart, hblocks, 17, n->g + n->hoff, 1);
+  count_launches(5);
 #define BWD(l, gy, gcs, gco, y, ycs, yco, x, xcs, xco, gx, gxcs, gxco, acc, lev)                                  \
-  if ((rc = conv_backward(c, gpad, l, gy, gcs, gco, y, ycs, yco, x, xcs, xco, gx, gxcs, gxco, acc, lev))) return rc;
+  if ((rc = conv_backward(c, gw, l, gy, gcs, gco, y, ycs, yco, x, xcs, xco, gx, gxcs, gxco, acc, lev))) return rc;
   BWD(13, n->g_a13, 16, 0, n->a13, 16, 0, n->a12, 16, 0, n->g_a12, 16, 0, 0, 0);
   BWD(12, n->g_a12, 16, 0, n->a12, 16, 0, n->cat0, 48, 0, n->g_cat0, 48, 0, 0, 0);
   up_bwd_kernel<<<GRID(L(1).vox() * 32), 256, 0, s>>>(n->g_cat0, 48, 0, L(0), n->g_a11, 32, L(1), 32);
@@ -1218,6 +1262,17 @@ int backward(ttfld_ctx* c, float* gpad, double* loss_out) {
   return 0;
 }
 
+// Largest per-chunk weight-gradient sums of a layer: at most kWgradWarps / tiles
+// chunks of [27][cout][cin_pad], i.e. kWgradWarps x 16 x cin_pad floats.
+size_t max_wpart() {
+  size_t m = 0;
+  for (int l = 0; l < kNumConv; ++l) {
+    size_t v = (size_t)kWgradWarps * 16 * kLayers[l].cin_pad;
+    if (v > m) m = v;
+  }
+  return m;
+}
+
 // Largest [27][cout][cin_pad] of the layers (the padded weight-gradient buffer).
 size_t max_wpad(const Net* n) {
   size_t m = 0;
@@ -1226,6 +1281,21 @@ size_t max_wpad(const Net* n) {
     if (v > m) m = v;
   }
   return m;
+}
+
+// One allocation for the gradient workspace (freed with cudaFree(gw->gpad)).
+int alloc_gradwork(const Net* n, GradWork* gw) {
+  const size_t a = align256(max_wpad(n) * 4), b = align256(max_wpart() * 4);
+  const size_t c = align256((size_t)kMaxGradBlocks * 64 * 4), d = align256((size_t)kMaxGradBlocks * 17 * 4);
+  const size_t e = align256((size_t)kMaxGradBlocks * 8);
+  char* p = nullptr;
+  TT_CHECK(cudaMalloc((void**)&p, a + b + c + d + e));
+  gw->gpad = (float*)p;
+  gw->wpart = (float*)(p + a);
+  gw->bpart = (float*)(p + a + b);
+  gw->hpart = (float*)(p + a + b + c);
+  gw->lpart = (double*)(p + a + b + c + d);
+  return 0;
 }
 
 // Features of the current state averaged over the 2x2x2 cells of each
@@ -1388,8 +1458,9 @@ int ttfld_guess_train(ttfld_ctx* c, int epochs, double lr, uint64_t seed, double
   if (!n || !n->ready) return TTFLD_E_NOMODEL;
   if (n->count < 1) return TTFLD_E_ARGS;
   const long long V0 = L(0).vox(), VF = n->full.vox();
-  float* gpad = nullptr;
-  TT_CHECK(cudaMalloc((void**)&gpad, max_wpad(n) * 4));
+  GradWork gw;
+  int rc0 = alloc_gradwork(n, &gw);
+  if (rc0) return rc0;
   std::vector<int> order(n->count);
   uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 1;
   double tot = 0.0;
@@ -1416,7 +1487,7 @@ int ttfld_guess_train(ttfld_ctx* c, int epochs, double lr, uint64_t seed, double
         target[v] = __bfloat162float(tg[v]);
       });
       double loss = 0.0;
-      if ((rc = prep_weights(c)) || (rc = forward(c)) || (rc = backward(c, gpad, &loss))) break;
+      if ((rc = prep_weights(c)) || (rc = forward(c)) || (rc = backward(c, &gw, &loss))) break;
       n->step += 1;
       const float b1 = 0.9f, b2 = 0.999f;
       const float c1 = 1.f - powf(b1, (float)n->step), c2 = 1.f - powf(b2, (float)n->step);
@@ -1429,7 +1500,7 @@ int ttfld_guess_train(ttfld_ctx* c, int epochs, double lr, uint64_t seed, double
     }
   }
   cudaStreamSynchronize(c->stream);
-  cudaFree(gpad);
+  cudaFree(gw.gpad);
   if (rc) return rc;
   if (mean_loss) *mean_loss = cnt ? tot / cnt : 0.0;
   c->have_model = 1;
@@ -1449,13 +1520,13 @@ int ttfld_guess_gradients(ttfld_ctx* c, const float* feat, const float* target, 
   if (rc) return rc;
   TT_CHECK(cudaMemcpy(n->target, target, (size_t)VF * 4, cudaMemcpyHostToDevice));
   TT_CHECK(cudaMemcpy(n->mask, mask, (size_t)VF, cudaMemcpyHostToDevice));
-  float* gpad = nullptr;
-  TT_CHECK(cudaMalloc((void**)&gpad, max_wpad(n) * 4));
+  GradWork gw;
+  if ((rc = alloc_gradwork(n, &gw))) return rc;
   rc = prep_weights(c);
   if (!rc) rc = forward(c);
-  if (!rc) rc = backward(c, gpad, loss);
+  if (!rc) rc = backward(c, &gw, loss);
   cudaStreamSynchronize(c->stream);
-  cudaFree(gpad);
+  cudaFree(gw.gpad);
   if (rc) return rc;
   if (grads) TT_CHECK(cudaMemcpy(grads, n->g, n->nparams * 4, cudaMemcpyDeviceToHost));
   return 0;
