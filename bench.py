@@ -273,12 +273,23 @@ def run_profile_step(args):
 
 
 def run_profile_sweeps(args):
-    """For the ncu capture of the dominant kernel: the shell256 system, then
-    inside cudaProfilerStart/Stop one launch of 8 FP32 sweeps (the warm-up of
-    ttfld_time_sweeps) and one of 16 (in-sweep norm every 8th)."""
+    """For the ncu capture of the dominant kernel: the shell256 system (or a
+    shell of --profile-dims NX,NY,NZ, e.g. 160,256,128 for a working set
+    beyond L2), then inside cudaProfilerStart/Stop one launch of 8 FP32
+    sweeps (the warm-up of ttfld_time_sweeps) and one of 16 (in-sweep norm
+    every 8th)."""
     import torch
     torch.cuda.set_device(0)
-    sh, f, _ = build_system(0, train=False)
+    if args.profile_dims:
+        from ttcode_gb300.fld import start_run
+        from ttcode_gb300.synthetic import make_shell
+        nx, ny, nz = (int(v) for v in args.profile_dims.split(","))
+        sh = make_shell(nx, ny, nz, seed=1, delt=100.0)
+        sh.params["epsmat"] = 1e-10
+        f = start_run(sh)
+        first_system(f)
+    else:
+        sh, f, _ = build_system(0, train=False)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
     ms = f.time_sweeps("mixed", 16)
@@ -646,6 +657,7 @@ def main():
                     help="only build the system and run one mixed and one exact FP64 solve")
     ap.add_argument("--profile-sweeps", action="store_true",
                     help="only build the system and run 8 + 16 FP32 sweeps")
+    ap.add_argument("--profile-dims", default="", help="NX,NY,NZ of the --profile-sweeps shell (default shell256)")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run three implicit steps, the third inside cudaProfilerStart/Stop")
     ap.add_argument("--profile-pcg", action="store_true",

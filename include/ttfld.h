@@ -118,6 +118,8 @@ typedef struct {
                        /* 1 = prescribed: XKAP* are uploaded, KAPPA no-op  */
                        /* 2 = a (T, rho) table, BurrowsOPC's interpolation
                               (ttfld_set_opacity_table)                    */
+                       /* 3 = Freedman's (T, P) table, FreedmanOPC's
+                              interpolation (ttfld_set_freedman_table)     */
 } ttfld_params;
 
 /* How SOLVE_WITH_SOR's linear system is solved on the device. */
@@ -250,12 +252,18 @@ int ttfld_bounds(ttfld_ctx* ctx);
 /* KAPPA, pprphy.f:1-360, and SUBSIG, pprphy.f:567-583, by kappa_model:
  * 0 the synthetic analytic opacity on the extents of the IKAPTYP 20:25
  * branch (pprphy.f:321-351); 1 nothing (XKAP* are the caller's); 2 that
- * branch with BurrowsOPC on the table of ttfld_set_opacity_table
- * (TTFLD_E_OPACITY where the reference stops). */
+ * branch with BurrowsOPC on the table of ttfld_set_opacity_table (and,
+ * after ttfld_set_wave_table, the per-bin opacities xkapW); 3 the IKAPTYP
+ * 4:5 branch (pprphy.f:88-110, MODTYP 2) with FreedmanOPC on the table of
+ * ttfld_set_freedman_table and PRESSG's ideal-gas pressure (TTFLD_E_OPACITY
+ * where the reference stops). */
 int ttfld_kappa(ttfld_ctx* ctx);
 /* CALCMUSTAR ppsub.f:156-179 and CALC_TINCIDENT pprad.f:296-405 are
  * evaluated by the caller and uploaded as MU_STAR / TINCIDENT. */
-/* STELLARINPUT_HEATING, pprad.f:408-516 (grey branch, :490-502). */
+/* STELLARINPUT_HEATING, pprad.f:408-516: the grey branch (:490-502), or
+ * after ttfld_set_wave_table the wavelength-binned branch of IKAPTYP 20-24
+ * (:433-448, WAVELENGTH_CALCSTELLARTAU :519-547 and
+ * WAVELENGTH_STELLAR_DTAU :549-568) on KAPPA's per-bin opacities. */
 int ttfld_stellarinput_heating(ttfld_ctx* ctx);
 /* DIFF, pprad.f:74-156, including FLIM pprphy.f:362-565; energy_iter <= 1
  * also re-evaluates KAPPA, SUBSIG and QDENS (pprphy.f:396-402). */
@@ -367,6 +375,38 @@ typedef struct {
   const double* log_abs;
 } ttfld_opacity_table;
 int ttfld_set_opacity_table(ttfld_ctx* ctx, const ttfld_opacity_table* table);
+
+/* The per-wavelength-bin part of the same Burrows table for IKAPTYP 20-24:
+ * log10 BurrowsXKAP_waveopac on the kappa_model 2 table's nodes (nt x nrh x
+ * nbins, T fastest, bin slowest; pprphy.f:1138-1151), the star's flux per
+ * bin BSTAR_BIN (READBURROWSOPCTABLE's BSTAR_WAVEBINS file,
+ * pprphy.f:1525-1539), RSTAR in solar radii (ipp) and the orbit's semi-major
+ * axis semi in cm (pp.f:205).  Needs ttfld_set_opacity_table first; the
+ * per-bin opacities and optical depths take 2 x nbins halo arrays on the
+ * device.  nbins = 0 drops the table (grey heating again).  Host memory,
+ * copied. */
+typedef struct {
+  int32_t nbins;
+  const double* log_waveopac;  /* (nt, nrh, nbins) */
+  const double* bstar_bin;     /* (nbins) */
+  double rstar;                /* RSTAR, solar radii */
+  double semi;                 /* semi-major axis, cm */
+} ttfld_wave_table;
+int ttfld_set_wave_table(ttfld_ctx* ctx, const ttfld_wave_table* table);
+
+/* FreedmanOPC's table for kappa_model 3 (pprphy.f:800-942; read by
+ * READFREEDMANOPCTABLE, pprphy.f:944-1002, from files not in the
+ * reference's tree): log10 Rosseland, Planck and absorption means on the
+ * 42 FreedmanTVAL x 18 FreedmanPVAL nodes (ppmod.f:690-700; T index
+ * fastest), and the gas's mu_gas for PRESSG's ideal-gas pressure
+ * PG = Rgas T RH / mu_gas (ppphy.f:17-20).  Host memory, copied. */
+typedef struct {
+  const double* log_ross;  /* (42, 18) */
+  const double* log_plnk;
+  const double* log_abs;
+  double mu_gas;
+} ttfld_freedman_table;
+int ttfld_set_freedman_table(ttfld_ctx* ctx, const ttfld_freedman_table* table);
 
 /* ---- measurement (no reference counterpart) --------------------------- */
 /* Runs n back-to-back sweeps of a solver's sweep kernels on the current

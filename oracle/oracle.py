@@ -67,6 +67,8 @@ def _load():
         lib.ttor_sor_sweeps.argtypes = [vp, ctypes.c_int]
         lib.ttor_sor_sweeps_mt.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         lib.ttor_solve_with_sor_mt.argtypes = [vp, ctypes.c_int]
+        lib.ttor_set_freedman_table.argtypes = [vp, vp, vp, vp, ctypes.c_double]
+        lib.ttor_set_wave_table.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_double]
         lib.ttor_coupled_energy_eqs.argtypes = [vp, ctypes.c_int]
         lib.ttor_raddif.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         lib.ttor_set_opacity_table.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [vp] * 5

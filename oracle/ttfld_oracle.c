@@ -27,6 +27,7 @@
 #define ARAD_C ((double)7.56596e-15f)
 #define SBCONST_C ((double)5.6705e-5f)
 #define RGAS_C ((double)8.315e7f)
+#define RSOL_C ((double)6.9598e10f)
 
 struct ttor_state {
   int nx, ny, nz;
@@ -38,6 +39,17 @@ struct ttor_state {
   /* opacity table (BurrowsOPC's arrays), used by KAPPA when opac_nt > 0 */
   int opac_nt, opac_nrh;
   double *opac_lt, *opac_lrh, *opac_ross, *opac_plnk, *opac_abs;
+  /* per-wavelength-bin opacities of the same table (BurrowsXKAP_waveopac),
+   * the star's flux per bin (BSTAR_BIN) and RSTAR, semi: with wave_nb > 0
+   * KAPPA also forms XKAPW and STELLARINPUT_HEATING takes the binned branch
+   * of IKAPTYP 20-24 */
+  int wave_nb;
+  double *wave_opac, *wave_bstar, *XKAPW, *STAU_W;
+  double wave_rstar, wave_semi;
+  /* FreedmanXKAP_ross/plnk/abs (42 x 18, T fastest) and mu_gas: with
+   * freed_set KAPPA takes the IKAPTYP 4:5 branch */
+  int freed_set;
+  double freed_ross[42 * 18], freed_plnk[42 * 18], freed_abs[42 * 18], freed_mu;
   /* results */
   int sor_iter, energy_iter, status, sor_total, solves;
   double global_rnorm, global_rhsnorm, global_deltaq, global_deltaer;
@@ -85,6 +97,9 @@ static size_t nhalo(const ttor_state* s) {
   return (size_t)(s->nx + 4) * (s->ny + 4) * (s->nz + 4);
 }
 static size_t ncell(const ttor_state* s) { return (size_t)s->nx * s->ny * s->nz; }
+static size_t hidx(const ttor_state* s, int i, int j, int k) {
+  return (size_t)(i + 1) + (size_t)NXH * ((size_t)(j + 1) + (size_t)NYH * (size_t)(k + 1));
+}
 static size_t nface(const ttor_state* s) {
   return (size_t)(s->nx + 1) * (s->ny + 1) * (s->nz + 1);
 }
@@ -173,6 +188,7 @@ void ttor_destroy(ttor_state* s) {
   for (size_t f = 0; f < NFIELDS; ++f) free(*(double**)((char*)s + FIELDS[f].off));
   free(s->UPPERBND);
   free(s->opac_lt); free(s->opac_lrh); free(s->opac_ross); free(s->opac_plnk); free(s->opac_abs);
+  free(s->wave_opac); free(s->wave_bstar); free(s->XKAPW); free(s->STAU_W);
   free(s);
 }
 
@@ -456,8 +472,158 @@ int ttor_set_opacity_table(ttor_state* s, int nt, int nrh, const double* lt, con
   return 0;
 }
 
+/* BurrowsOPC's per-bin opacities (pprphy.f:1138-1151) at the bracketing of
+ * (T, rho) burrows_opc uses: 10**(bilinear of log BurrowsXKAP_waveopac). */
+static int burrows_wave(const ttor_state* s, double t, double rh, double* kw) {
+  double rh1 = log10(rh), tm1 = log10(t);
+  if (tm1 < (double)1.69896f) tm1 = (double)1.69897f;
+  if (tm1 > (double)3.69889f) tm1 = (double)3.69888f;
+  if (rh1 < (double)-11.9996f) rh1 = (double)-11.9995f;
+  if (rh1 > (double)-1.99993f) rh1 = (double)-1.99994f;
+  const int nt = s->opac_nt, nr = s->opac_nrh;
+  int K;
+  for (K = 1; K <= nt; ++K)
+    if (s->opac_lt[K - 1] > tm1) break;
+  if (K == nt + 1 || K == 1) return 2;
+  const int it = K, it1 = K - 1;
+  double ws1 = s->opac_lt[it1 - 1] - tm1;
+  double ws = s->opac_lt[it1 - 1] - s->opac_lt[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  for (K = 1; K <= nr; ++K)
+    if (s->opac_lrh[K - 1] > rh1) break;
+  if (K == nr + 1 || K == 1) return 2;
+  const int iw = K, iw1 = K - 1;
+  double ws2 = rh1 - s->opac_lrh[iw1 - 1];
+  double ws3 = s->opac_lrh[iw - 1] - s->opac_lrh[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+  const size_t nn = (size_t)nt * nr;
+#define TW(p, q, l) s->wave_opac[(size_t)((p) - 1) + (size_t)nt * (size_t)((q) - 1) + nn * (size_t)(l)]
+  for (int l = 0; l < s->wave_nb; ++l) {
+    const double w4 = ws2 * (ws1 * TW(it, iw, l) + ws * TW(it1, iw, l));
+    const double w5 = ws3 * (ws1 * TW(it, iw1, l) + ws * TW(it1, iw1, l));
+    kw[l] = pow(10.0, w4 + w5);
+  }
+#undef TW
+  return 0;
+}
+
+int ttor_set_wave_table(ttor_state* s, int nb, const double* waveopac, const double* bstar, double rstar,
+                        double semi) {
+  if (nb < 1 || s->opac_nt < 2 || !waveopac || !bstar || !(semi > 0.0)) return -1;
+  free(s->wave_opac); free(s->wave_bstar); free(s->XKAPW); free(s->STAU_W);
+  const size_t nn = (size_t)s->opac_nt * s->opac_nrh * nb;
+  s->wave_opac = (double*)malloc(nn * sizeof(double));
+  s->wave_bstar = (double*)malloc(nb * sizeof(double));
+  s->XKAPW = (double*)calloc(nhalo(s) * nb, sizeof(double));
+  s->STAU_W = (double*)calloc(nhalo(s) * nb, sizeof(double));
+  if (!s->wave_opac || !s->wave_bstar || !s->XKAPW || !s->STAU_W) return -2;
+  memcpy(s->wave_opac, waveopac, nn * sizeof(double));
+  memcpy(s->wave_bstar, bstar, nb * sizeof(double));
+  s->wave_nb = nb;
+  s->wave_rstar = rstar;
+  s->wave_semi = semi;
+  return 0;
+}
+
+/* The node values of FreedmanTVAL / FreedmanPVAL (ppmod.f:690-700; P in mbar). */
+static const double FREED_T[42] = {
+    75.0, 100.0, 110.0, 120.0, 130.0, 140.0, 150.0, 160.0, 170.0, 180.0, 190.0, 200.0, 210.0, 220.0,
+    230.0, 240.0, 250.0, 275.0, 300.0, 400.0, 500.0, 575.0, 650.0, 725.0, 800.0, 900.0, 1000.0, 1100.0,
+    1200.0, 1300.0, 1400.0, 1500.0, 1600.0, 1700.0, 1800.0, 1900.0, 2000.0, 2300.0, 2600.0, 3000.0,
+    3500.0, 4000.0};
+static const double FREED_P[18] = {0.001, 0.003, 0.01, 0.03, 0.1, 0.3, 1.0, 3.0, 10.0,
+                                   30.0, 100.0, 300.0, 1000.0, 3000.0, 10000.0, 30000.0, 100000.0, 300000.0};
+
+/* FreedmanOPC pprphy.f:800-942 at (T, P_gas in dyn/cm^2): P in mbar, the
+ * clamps of :830-833, the first node above T and above P, weights linear
+ * in T and P (WS3 = 1. - WS2 with a REAL*4 1., exactly 1), 10** of the
+ * bilinear log means, the T-derivative stand-ins of :895-899.  Returns 0,
+ * or 1 T <= 0, 2 above / 3 below the nodes, 4 a non-positive opacity. */
+static int freedman_opc(const ttor_state* s, double t, double pg, double* kp, double* kr, double* ka, double* dkp,
+                        double* dka) {
+  if (t <= 0.0) return 1;
+  double pg1 = pg * (0.001);
+  double tm1 = t;
+  if (tm1 < 75.0) tm1 = 75.001;
+  if (tm1 > 4000.0) tm1 = 3999.9;
+  if (pg1 < 0.001) pg1 = 0.001001;
+  if (pg1 > 300000.0) pg1 = 299999.9;
+  int K;
+  for (K = 1; K <= 42; ++K)
+    if (FREED_T[K - 1] > tm1) break;
+  if (K == 43) return 2;
+  const int it = K, it1 = K - 1;
+  if (it1 == 0) return 3;
+  double ws1 = FREED_T[it1 - 1] - tm1;
+  double ws = FREED_T[it1 - 1] - FREED_T[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  for (K = 1; K <= 18; ++K)
+    if (FREED_P[K - 1] > pg1) break;
+  if (K == 19) return 2;
+  const int iw = K, iw1 = K - 1;
+  if (iw1 == 0) return 3;
+  double ws2 = pg1 - FREED_P[iw1 - 1];
+  double ws3 = FREED_P[iw - 1] - FREED_P[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+#define TF(a, p, q) a[(size_t)((p) - 1) + (size_t)42 * (size_t)((q) - 1)]
+  const double* tabs[3] = {s->freed_ross, s->freed_plnk, s->freed_abs};
+  double out[3];
+  for (int m = 0; m < 3; ++m) {
+    const double* a = tabs[m];
+    const double w4 = ws2 * (ws1 * TF(a, it, iw) + ws * TF(a, it1, iw));
+    const double w5 = ws3 * (ws1 * TF(a, it, iw1) + ws * TF(a, it1, iw1));
+    out[m] = pow(10.0, w4 + w5);
+  }
+  *kr = out[0]; *kp = out[1]; *ka = out[2];
+  *dkp = ((pow(10.0, TF(s->freed_plnk, it, iw))) - (pow(10.0, TF(s->freed_plnk, it1, iw)))) /
+         (FREED_T[it - 1] - FREED_T[it1 - 1]);
+  *dka = ((pow(10.0, TF(s->freed_abs, it, iw))) - (pow(10.0, TF(s->freed_abs, it1, iw)))) /
+         (FREED_T[it - 1] - FREED_T[it1 - 1]);
+#undef TF
+  if (*kr <= 0.0 || *kp <= 0.0 || *ka <= 0.0) return 4;
+  return 0;
+}
+
+int ttor_set_freedman_table(ttor_state* s, const double* ross, const double* plnk, const double* absk,
+                            double mu_gas) {
+  if (!ross || !plnk || !absk || !(mu_gas > 0.0)) return -1;
+  memcpy(s->freed_ross, ross, sizeof(s->freed_ross));
+  memcpy(s->freed_plnk, plnk, sizeof(s->freed_plnk));
+  memcpy(s->freed_abs, absk, sizeof(s->freed_abs));
+  s->freed_mu = mu_gas;
+  s->freed_set = 1;
+  return 0;
+}
+
 int ttor_kappa(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
+  if (s->freed_set) {   /* the IKAPTYP 4:5 branch, MODTYP 2, pprphy.f:88-110 */
+    for (int k = -1; k <= nz + 2; ++k)
+      for (int j = -1; j <= ny + 2; ++j) {
+        int ub = P(UPPERBND, j, k);
+        if (ub < -1 || ub > nx + 2) return -2;
+        for (int i = -1; i <= ub; ++i) {
+          /* PRESSG, ideal gas (ppphy.f:17-20): PG = Rgas*T*RH/mu_gas */
+          const double pg = RGAS_C * H(T, i, j, k) * H(RH, i, j, k) / s->freed_mu;
+          double kp, kr, ka, dkp, dka;
+          if (freedman_opc(s, H(T, i, j, k), pg, &kp, &kr, &ka, &dkp, &dka)) return -10;
+          H(XKAPP, i, j, k) = kp; H(XKAPR, i, j, k) = kr; H(XKAPA, i, j, k) = ka;
+          H(DXKAPP_DT, i, j, k) = dkp; H(DXKAPA_DT, i, j, k) = dka;
+        }
+        for (int i = ub + 1; i <= nx + 2; ++i) {
+          H(XKAPR, i, j, k) = H(XKAPR, ub, j, k);
+          H(XKAPP, i, j, k) = H(XKAPP, ub, j, k);
+          H(XKAPA, i, j, k) = H(XKAPA, ub, j, k);
+          H(DXKAPP_DT, i, j, k) = H(DXKAPP_DT, ub, j, k);
+          H(DXKAPA_DT, i, j, k) = H(DXKAPA_DT, ub, j, k);
+        }
+      }
+    return 0;
+  }
   if (s->opac_nt > 0) {   /* the IKAPTYP 20:25 branch with BurrowsOPC, pprphy.f:321-351 */
     for (int k = -1; k <= nz + 2; ++k)
       for (int j = -1; j <= ny + 2; ++j) {
@@ -468,6 +634,11 @@ int ttor_kappa(ttor_state* s) {
           if (burrows_opc(s, H(T, i, j, k), H(RH, i, j, k), &kp, &kr, &ka, &dkp, &dka)) return -10;
           H(XKAPP, i, j, k) = kp; H(XKAPR, i, j, k) = kr; H(XKAPA, i, j, k) = ka;
           H(DXKAPP_DT, i, j, k) = dkp; H(DXKAPA_DT, i, j, k) = dka;
+          if (s->wave_nb > 0) {
+            double kw[64];
+            if (s->wave_nb > 64 || burrows_wave(s, H(T, i, j, k), H(RH, i, j, k), kw)) return -10;
+            for (int l = 0; l < s->wave_nb; ++l) s->XKAPW[hidx(s, i, j, k) + nhalo(s) * (size_t)l] = kw[l];
+          }
         }
         for (int i = ub; i <= nx + 2; ++i) {
           H(XKAPR, i, j, k) = H(XKAPR, ub - 1, j, k);
@@ -475,6 +646,8 @@ int ttor_kappa(ttor_state* s) {
           H(XKAPA, i, j, k) = H(XKAPA, ub - 1, j, k);
           H(DXKAPP_DT, i, j, k) = H(DXKAPP_DT, ub - 1, j, k);
           H(DXKAPA_DT, i, j, k) = H(DXKAPA_DT, ub - 1, j, k);
+          for (int l = 0; l < s->wave_nb; ++l)
+            s->XKAPW[hidx(s, i, j, k) + nhalo(s) * (size_t)l] = s->XKAPW[hidx(s, ub - 1, j, k) + nhalo(s) * (size_t)l];
         }
       }
     return 0;
@@ -731,12 +904,56 @@ int ttor_calculatedivf_withf(ttor_state* s, int which, double theta) {
  * (1:NX, -1:NY+2, -1:NZ+2) (ppmod.f:341); the reference loop runs i to
  * NX+2 and its last two writes land in the next column, which the loop
  * then overwrites, so only i = 1..NX is kept here. */
+/* The wavelength-binned branch of STELLARINPUT_HEATING for IKAPTYP 20-24
+ * (pprad.f:433-448): WAVELENGTH_CALCSTELLARTAU (pprad.f:519-547: per bin,
+ * the optical depth summed from UPPERBND inward, zero elsewhere),
+ * WAVELENGTH_STELLAR_DTAU (:549-568: central differences for i = 2..NX,
+ * dtaus(1) = dtaus(2), dtaus(NX+1) = 0), then the bins summed in order,
+ * times (RSTAR*RSOL/semi)**2 / dxb(i).  STELLARINPUT is formed for
+ * i = 1..NX, its declared extent. */
+static int stellar_binned(ttor_state* s) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz, nb = s->wave_nb;
+  const size_t nh = nhalo(s);
+  double dr = G1(xxb, 2) - G1(xxb, 1);
+  for (size_t q = 0; q < nh * (size_t)nb; ++q) s->STAU_W[q] = 0.0;
+  for (int k = -1; k <= nz + 2; ++k)
+    for (int j = -1; j <= ny + 2; ++j) {
+      double tot[64];
+      for (int l = 0; l < nb; ++l) tot[l] = 0.0;
+      int ub = P(UPPERBND, j, k);
+      if (ub > nx + 1) ub = nx + 1;
+      for (int i = ub; i >= 1; --i)
+        for (int l = 0; l < nb; ++l) {
+          tot[l] = tot[l] + (s->XKAPW[hidx(s, i, j, k) + nh * (size_t)l] * H(RH, i, j, k) * dr);
+          s->STAU_W[hidx(s, i, j, k) + nh * (size_t)l] = tot[l];
+        }
+    }
+  const double f = s->wave_rstar * RSOL_C / s->wave_semi;
+  const double geo = f * f;
+  for (int k = -1; k <= nz + 2; ++k)
+    for (int j = -1; j <= ny + 2; ++j) {
+      const double mu = P(MU_STAR, j, k);
+      for (int i = 1; i <= nx; ++i) {
+        const int is = i < 2 ? 2 : i;   /* dtaus(1) = dtaus(2); i <= NX here */
+        double si = 0.0;
+        for (int l = 0; l < nb; ++l) {
+          const double* tw = s->STAU_W + nh * (size_t)l;
+          const double dtaus = (tw[hidx(s, is - 1, j, k)] - tw[hidx(s, is + 1, j, k)]) / 2.0;
+          si = si + s->wave_bstar[l] * (exp(-tw[hidx(s, i, j, k)] / mu)) * dtaus;
+        }
+        H(STELLARINPUT, i, j, k) = si * geo / G1(dxb, i);
+      }
+    }
+  return 0;
+}
+
 int ttor_stellarinput_heating(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
   if (s->f_incident == 0) {
     for (size_t q = 0; q < nhalo(s); ++q) s->STELLARINPUT[q] = 0.0;
     return 0;
   }
+  if (s->wave_nb > 0) return stellar_binned(s);
   double dr = G1(xxb, 2) - G1(xxb, 1);
   for (int k = -1; k <= nz + 2; ++k)
     for (int j = -1; j <= ny + 2; ++j) {

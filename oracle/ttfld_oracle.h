@@ -89,6 +89,16 @@ int ttor_sor_sweeps(ttor_state* s, int nsweeps);
  * decomposition on the host cores, for the CPU baseline). */
 int ttor_sor_sweeps_mt(ttor_state* s, int nsweeps, int nthreads);
 int ttor_solve_with_sor_mt(ttor_state* s, int nthreads);
+/* FreedmanXKAP_ross/plnk/abs (42 x 18 log10 means, T index fastest) and
+ * mu_gas: KAPPA then takes the IKAPTYP 4:5 branch (FreedmanOPC). */
+int ttor_set_freedman_table(ttor_state* s, const double* ross, const double* plnk, const double* absk,
+                            double mu_gas);
+/* After ttor_set_opacity_table: the per-bin log10 opacities (nt x nrh x nb,
+ * T fastest, bin slowest), BSTAR_BIN (nb), RSTAR (solar radii) and semi
+ * (cm): KAPPA also forms the per-bin opacities and STELLARINPUT_HEATING
+ * takes the wavelength-binned branch of IKAPTYP 20-24. */
+int ttor_set_wave_table(ttor_state* s, int nb, const double* waveopac, const double* bstar, double rstar,
+                        double semi);
 int ttor_adjust_sor_param(ttor_state* s);
 int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds);
 /* DIFFUSION (ppdif.f) of the field "SCALAR" with constant xnue/Pr. */

@@ -396,3 +396,66 @@ def test_burrows_kappa_branch_9_14():
     t.ikaptyp = 21
     with pytest.raises(O.OpacityFileError):
         O.burrows_kappa(t, T, RH, ub)
+
+
+# ---- FreedmanOPC and the binned stellar heating in the oracle --------------
+def _oracle_freedman(sh, tab, mu=2.3):
+    o = oracle_from_shell(sh, start=False)
+    keep = [np.asfortranarray(a) for a in (tab.ross, tab.plnk, tab.absk)]
+    assert __import__("oracle")._load().ttor_set_freedman_table(o.h, *[a.ctypes.data for a in keep], mu) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    o.set("iii", 1)
+    return o
+
+
+def test_oracle_freedman_kappa_matches_host():
+    """The oracle's KAPPA IKAPTYP 4:5 branch (C FreedmanOPC, PRESSG's ideal-gas
+    pressure) against the host restatement on the same shell and table."""
+    sh = make_shell(16, 12, 10, seed=3, delt=100.0)
+    tab = O.analytic_freedman_table()
+    o = _oracle_freedman(sh, tab)
+    want = O.freedman_kappa(tab, o.f("T"), o.f("RH"), o.f("UPPERBND"), 2.3)
+    for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT"):
+        assert rel_l2(o.f(n), want[n]) <= 1e-14, n
+
+
+def _oracle_table(sh, f_incident, bins=None, bstar=None, rstar=1.0, semi=7.0e11):
+    """The oracle on a kappa_model 2 table of the analytic model, with an
+    optional per-bin part (log opacities (nt, nrh, nb) and BSTAR)."""
+    from ttcode_gb300.synthetic import analytic_opacity_table
+    lt, lr, kr, kp, ka = analytic_opacity_table(1e-2)
+    L = __import__("oracle")._load()
+    o = oracle_from_shell(sh, start=False)
+    o.set("f_incident", f_incident)
+    keep = [np.ascontiguousarray(lt), np.ascontiguousarray(lr)] + [np.asfortranarray(a) for a in (kr, kp, ka)]
+    assert L.ttor_set_opacity_table(o.h, lt.size, lr.size, *[a.ctypes.data for a in keep]) == 0
+    if bins is not None:
+        w = np.asfortranarray(bins)
+        b = np.ascontiguousarray(bstar, dtype=np.float64)
+        assert L.ttor_set_wave_table(o.h, b.size, w.ctypes.data, b.ctypes.data, rstar, semi) == 0
+    o.set("iii", 0)
+    assert o.call("bounds") == 0 and o.call("kappa") == 0
+    o.set("iii", 1)
+    assert o.call("stellarinput_heating") == 0
+    return o, ka
+
+
+def test_binned_heating_reduces_to_grey():
+    """With one bin whose opacity is the absorption mean, constant incident
+    temperature and mu = 1 (F_INCIDENT 4), the binned STELLARINPUT is the
+    grey one times BSTAR (RSTAR RSOL / semi)^2 / (SBCONST T_irr^4); three
+    bins of that opacity add their BSTAR (linearity in the bins)."""
+    sh = make_shell(20, 12, 10, seed=4, delt=100.0)
+    from ttcode_gb300.synthetic import mu_star_tincident
+    mu, tinc = mu_star_tincident(sh.grid, sh.params["tirr"], 4)
+    sh.fields["MU_STAR"], sh.fields["TINCIDENT"] = mu, tinc
+    og, ka = _oracle_table(sh, 4)
+    grey = og.f("STELLARINPUT")[2:22].copy()
+    rstar, semi, b = 1.155, 6.8e11, 3.0e9
+    ob, _ = _oracle_table(sh, 4, ka[:, :, None], [b], rstar, semi)
+    f = rstar * float(np.float32(6.9598e10)) / semi
+    ratio = b * (f * f) / (float(np.float32(5.6705e-5)) * sh.params["tirr"] ** 4)
+    assert rel_l2(ob.f("STELLARINPUT")[2:22], grey * ratio) <= 1e-14
+    o3, _ = _oracle_table(sh, 4, np.repeat(ka[:, :, None], 3, axis=2), [b, 2 * b, 0.5 * b], rstar, semi)
+    assert rel_l2(o3.f("STELLARINPUT")[2:22], 3.5 * ob.f("STELLARINPUT")[2:22]) <= 1e-14

@@ -69,6 +69,16 @@ class OpacityTable(ctypes.Structure):
                 ("log_abs", ctypes.c_void_p)]
 
 
+class WaveTable(ctypes.Structure):
+    _fields_ = [("nbins", ctypes.c_int32), ("log_waveopac", ctypes.c_void_p), ("bstar_bin", ctypes.c_void_p),
+                ("rstar", ctypes.c_double), ("semi", ctypes.c_double)]
+
+
+class FreedmanTableC(ctypes.Structure):
+    _fields_ = [("log_ross", ctypes.c_void_p), ("log_plnk", ctypes.c_void_p), ("log_abs", ctypes.c_void_p),
+                ("mu_gas", ctypes.c_double)]
+
+
 class Energy(ctypes.Structure):
     _fields_ = [(n, c_double) for n in ("volume", "e_rad", "e_gas", "heating", "flux_bottom", "flux_top",
                                         "flux_theta")]
@@ -116,7 +126,8 @@ EXPORTS = ("ttfld_abi_version", "ttfld_status_string", "ttfld_create", "ttfld_de
            "ttfld_guess_dataset", "ttfld_guess_capture_next", "ttfld_guess_dataset_count",
            "ttfld_guess_train", "ttfld_guess_gradients", "ttfld_guess_predict",
            "ttfld_guess_num_params", "ttfld_begin_step", "ttfld_guess_set_conv", "ttfld_energy_sums",
-           "ttfld_solve_with_hypre", "ttfld_raddif", "ttfld_set_opacity_table")
+           "ttfld_solve_with_hypre", "ttfld_raddif", "ttfld_set_opacity_table", "ttfld_set_wave_table",
+           "ttfld_set_freedman_table")
 
 _lib = None
 
@@ -166,6 +177,8 @@ def lib():
     L.ttfld_solve_with_hypre.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolveStats)]
     L.ttfld_raddif.argtypes = [vp, ctypes.POINTER(RaddifParams), ctypes.POINTER(SolveStats)]
     L.ttfld_set_opacity_table.argtypes = [vp, ctypes.POINTER(OpacityTable)]
+    L.ttfld_set_wave_table.argtypes = [vp, ctypes.POINTER(WaveTable)]
+    L.ttfld_set_freedman_table.argtypes = [vp, ctypes.POINTER(FreedmanTableC)]
     L.ttfld_sor_sweeps.argtypes = [vp, ctypes.c_int, P_double, P_double]
     L.ttfld_true_residual.argtypes = [vp, P_double, P_double]
     L.ttfld_adjust_sor_param.argtypes = [vp, P_double]

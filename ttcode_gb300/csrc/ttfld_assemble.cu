@@ -104,9 +104,144 @@ __device__ __forceinline__ int burrows_opc(const OpacTab& tb, double t, double r
   return 0;
 }
 
+// BurrowsOPC's per-bin opacities (pprphy.f:1138-1151): 10** of the bilinear
+// form of log BurrowsXKAP_waveopac at burrows_opc's bracketing of (T, rho),
+// for the nb bins, into out[l * stride].  Returns 0, or 2/3 off the table.
+__device__ __forceinline__ int burrows_wave(const OpacTab& tb, const double* wop, int nb, double t, double rh,
+                                           double* out, size_t stride) {
+  double rh1 = log10(rh), tm1 = log10(t);
+  if (tm1 < (double)1.69896f) tm1 = (double)1.69897f;
+  if (tm1 > (double)3.69889f) tm1 = (double)3.69888f;
+  if (rh1 < (double)-11.9996f) rh1 = (double)-11.9995f;
+  if (rh1 > (double)-1.99993f) rh1 = (double)-1.99994f;
+  int it = 1;
+  while (it <= tb.nt && !(tb.lt[it - 1] > tm1)) ++it;
+  if (it == tb.nt + 1) return 2;
+  if (it == 1) return 3;
+  const int it1 = it - 1;
+  double ws1 = tb.lt[it1 - 1] - tm1;
+  double ws = tb.lt[it1 - 1] - tb.lt[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  int iw = 1;
+  while (iw <= tb.nrh && !(tb.lrh[iw - 1] > rh1)) ++iw;
+  if (iw == tb.nrh + 1) return 2;
+  if (iw == 1) return 3;
+  const int iw1 = iw - 1;
+  double ws2 = rh1 - tb.lrh[iw1 - 1];
+  double ws3 = tb.lrh[iw - 1] - tb.lrh[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+  const size_t nn = (size_t)tb.nt * tb.nrh;
+  const size_t n00 = (size_t)(it - 1) + (size_t)tb.nt * (iw - 1), n10 = (size_t)(it - 1) + (size_t)tb.nt * (iw1 - 1);
+  const size_t n11 = (size_t)(it1 - 1) + (size_t)tb.nt * (iw1 - 1), n01 = (size_t)(it1 - 1) + (size_t)tb.nt * (iw - 1);
+  for (int l = 0; l < nb; ++l) {
+    const double* a = wop + nn * l;
+    const double w4 = ws2 * (ws1 * a[n00] + ws * a[n01]);
+    const double w5 = ws3 * (ws1 * a[n10] + ws * a[n11]);
+    out[stride * l] = pow(10.0, w4 + w5);
+  }
+  return 0;
+}
+
+// FreedmanTVAL and FreedmanPVAL (ppmod.f:690-700; P in mbar).
+__device__ const double kFreedT[42] = {
+    75.0, 100.0, 110.0, 120.0, 130.0, 140.0, 150.0, 160.0, 170.0, 180.0, 190.0, 200.0, 210.0, 220.0,
+    230.0, 240.0, 250.0, 275.0, 300.0, 400.0, 500.0, 575.0, 650.0, 725.0, 800.0, 900.0, 1000.0, 1100.0,
+    1200.0, 1300.0, 1400.0, 1500.0, 1600.0, 1700.0, 1800.0, 1900.0, 2000.0, 2300.0, 2600.0, 3000.0,
+    3500.0, 4000.0};
+__device__ const double kFreedP[18] = {0.001, 0.003, 0.01, 0.03, 0.1, 0.3, 1.0, 3.0, 10.0,
+                                       30.0, 100.0, 300.0, 1000.0, 3000.0, 10000.0, 30000.0, 100000.0, 300000.0};
+
+// FreedmanOPC pprphy.f:800-942 at (T, P_gas in dyn/cm^2): P in mbar, the
+// clamps of :830-833, the first node above T and above P, weights linear in
+// T and P, 10** of the bilinear log means, the T-derivative stand-ins of
+// :895-899.  tab holds ross, plnk, abs (42 x 18 each, T fastest).  Returns
+// 0, or 1 T <= 0, 2 above / 3 below the nodes, 4 a non-positive opacity.
+__device__ __forceinline__ int freedman_opc(const double* tab, double t, double pg, double& kp, double& kr,
+                                            double& ka, double& dkp, double& dka) {
+  if (t <= 0.0) return 1;
+  double pg1 = pg * (0.001);
+  double tm1 = t;
+  if (tm1 < 75.0) tm1 = 75.001;
+  if (tm1 > 4000.0) tm1 = 3999.9;
+  if (pg1 < 0.001) pg1 = 0.001001;
+  if (pg1 > 300000.0) pg1 = 299999.9;
+  int it = 1;
+  while (it <= 42 && !(kFreedT[it - 1] > tm1)) ++it;
+  if (it == 43) return 2;
+  if (it == 1) return 3;
+  const int it1 = it - 1;
+  double ws1 = kFreedT[it1 - 1] - tm1;
+  double ws = kFreedT[it1 - 1] - kFreedT[it - 1];
+  ws1 = ws1 / ws;
+  ws = 1.0 - ws1;
+  int iw = 1;
+  while (iw <= 18 && !(kFreedP[iw - 1] > pg1)) ++iw;
+  if (iw == 19) return 2;
+  if (iw == 1) return 3;
+  const int iw1 = iw - 1;
+  double ws2 = pg1 - kFreedP[iw1 - 1];
+  double ws3 = kFreedP[iw - 1] - kFreedP[iw1 - 1];
+  ws2 = ws2 / ws3;
+  ws3 = 1.0 - ws2;
+  const size_t n00 = (size_t)(it - 1) + 42 * (size_t)(iw - 1), n10 = (size_t)(it - 1) + 42 * (size_t)(iw1 - 1);
+  const size_t n11 = (size_t)(it1 - 1) + 42 * (size_t)(iw1 - 1), n01 = (size_t)(it1 - 1) + 42 * (size_t)(iw - 1);
+  const double* ross = tab;
+  const double* plnk = tab + 42 * 18;
+  const double* absk = tab + 2 * 42 * 18;
+  auto interp = [&](const double* a) {
+    const double w4 = ws2 * (ws1 * a[n00] + ws * a[n01]);
+    const double w5 = ws3 * (ws1 * a[n10] + ws * a[n11]);
+    return pow(10.0, w4 + w5);
+  };
+  kr = interp(ross);
+  kp = interp(plnk);
+  ka = interp(absk);
+  const double dt = kFreedT[it - 1] - kFreedT[it1 - 1];
+  dkp = ((pow(10.0, plnk[n00])) - (pow(10.0, plnk[n01]))) / dt;
+  dka = ((pow(10.0, absk[n00])) - (pow(10.0, absk[n01]))) / dt;
+  if (kr <= 0.0 || kp <= 0.0 || ka <= 0.0) return 4;
+  return 0;
+}
+
 static int kappa(ttfld_ctx* c) {
   Dev d = c->d;
   if (d.kappa_model == 1) return 0;  // prescribed opacities: KAPPA is the caller's
+  if (d.kappa_model == 3) {
+    if (!c->freed) {
+      fprintf(stderr, "ttfld: kappa_model 3 without a Freedman table (ttfld_set_freedman_table)\n");
+      return TTFLD_E_OPACITY;
+    }
+    // the IKAPTYP 4:5 branch, MODTYP 2 (pprphy.f:88-110): FreedmanOPC for
+    // i = -1..UPPERBND on PRESSG's PG = Rgas T RH / mu_gas, the values of
+    // UPPERBND above it (each of those cells evaluates UPPERBND itself)
+    int* err = (int*)c->freed;
+    const double* tab = c->freed + 1;
+    const double mu = c->freed_mu;
+    TT_CHECK(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+      const int ub = PA(UB, j, k);
+      if (ub < -1 || ub > d.nx + 2) { atomicExch(err, 5); return; }
+      const size_t s = hidx(d, i <= ub ? i : ub, j, k), q = hidx(d, i, j, k);
+      const double pg = TT_RGAS * d.T[s] * d.RH[s] / mu;
+      double kp, kr, ka, dkp, dka;
+      const int e = freedman_opc(tab, d.T[s], pg, kp, kr, ka, dkp, dka);
+      if (e) atomicExch(err, e);
+      d.XKAPR[q] = kr; d.XKAPP[q] = kp; d.XKAPA[q] = ka;
+      d.DXKAPP[q] = dkp; d.DXKAPA[q] = dka;
+    });
+    TT_CHECK_LAUNCH();
+    int e = 0;
+    TT_CHECK(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TT_CHECK(cudaStreamSynchronize(c->stream));
+    if (e) {
+      fprintf(stderr, "ttfld: KAPPA from the Freedman table stopped (reason %d: 1 T<=0, 2 above, 3 below the "
+                      "nodes, 4 non-positive opacity, 5 UPPERBND outside the grid)\n", e);
+      return TTFLD_E_OPACITY;
+    }
+    return 0;
+  }
   if (d.kappa_model == 2) {
     if (!c->opac) {
       fprintf(stderr, "ttfld: kappa_model 2 without an opacity table (ttfld_set_opacity_table)\n");
@@ -114,6 +249,11 @@ static int kappa(ttfld_ctx* c) {
     }
     const OpacTab tb = opac_tab(c);
     TT_CHECK(cudaMemsetAsync(tb.err, 0, sizeof(int), c->stream));
+    // with a wave table, also the per-bin opacities xkapW (pprphy.f:331-341)
+    const int nb = c->wave ? c->wave_nb : 0;
+    const double* wop = c->wave;
+    double* xkapw = c->xkapw;
+    const size_t nh = nhalo(d);
     // cells from UPPERBND up take the values of UPPERBND-1 (pprphy.f:336-348)
     launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
       int ub = PA(UB, j, k);
@@ -121,7 +261,8 @@ static int kappa(ttfld_ctx* c) {
       size_t s = hidx(d, i < ub ? i : ub - 1, j, k);
       size_t q = hidx(d, i, j, k);
       double kp, kr, ka, dkp, dka;
-      const int e = burrows_opc(tb, d.T[s], d.RH[s], kp, kr, ka, dkp, dka);
+      int e = burrows_opc(tb, d.T[s], d.RH[s], kp, kr, ka, dkp, dka);
+      if (nb > 0 && !e) e = burrows_wave(tb, wop, nb, d.T[s], d.RH[s], xkapw + q, nh);
       if (e) atomicExch(tb.err, e);
       d.XKAPR[q] = kr; d.XKAPP[q] = kp; d.XKAPA[q] = ka;
       d.DXKAPP[q] = dkp; d.DXKAPA[q] = dka;
@@ -312,10 +453,11 @@ __device__ __forceinline__ double fluxx_final(const Dev& d, int i, int j, int k,
 }
 
 // FLIM (MODE 0), FLIM + DIFF (1), or FLIM + DIFF + CALCULATEFLUX + FLUX_BC
-// (2) in one pass over the faces (1:NX+1,1:NY+1,1:NZ+1); each thread forms
-// the x, y and z faces that share its index.  KAPPA and QDENS, which FLIM
-// calls for energy_iter <= 1 (pprphy.f:396-402), run first unless they
-// already ran on the same T and rho in this step (skip_kappa / skip_qdens).
+// (2): one pass per direction over its faces, each face formed whole
+// (limiter, diffusion coefficient, flux) by one thread.  KAPPA and QDENS,
+// which FLIM calls for energy_iter <= 1 (pprphy.f:396-402), run first unless
+// they already ran on the same T and rho in this step (skip_kappa /
+// skip_qdens).
 template <int MODE>
 static int faces(ttfld_ctx* c, int energy_iter, bool skip_kappa, bool skip_qdens) {
   if (energy_iter <= 1) {
@@ -324,46 +466,46 @@ static int faces(ttfld_ctx* c, int energy_iter, bool skip_kappa, bool skip_qdens
     if (!skip_qdens && (rc = qdens(c))) return rc;
   }
   Dev d = c->d;
-  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny + 1, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
-    if (j <= d.ny && k <= d.nz) {
-      const double fl = flimx_at(d, i, j, k);
-      FA(FLIMX, i, j, k) = fl;
-      if (MODE >= 1) {
-        const double dr = difrx_of(d, i, j, k, fl);
-        FA(DIFRX, i, j, k) = dr;
-        if (MODE == 2) FA(FLUXX, i, j, k) = fluxx_final(d, i, j, k, dr);
+  launch_box(c->stream, box(1, d.nx + 1, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    const double fl = flimx_at(d, i, j, k);
+    FA(FLIMX, i, j, k) = fl;
+    if (MODE >= 1) {
+      const double dr = difrx_of(d, i, j, k, fl);
+      FA(DIFRX, i, j, k) = dr;
+      if (MODE == 2) FA(FLUXX, i, j, k) = fluxx_final(d, i, j, k, dr);
+    }
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(1, d.nx, 1, d.ny + 1, 1, d.nz), [=] __device__(int i, int j, int k) {
+    const double fl = flimy_at(d, i, j, k);
+    FA(FLIMY, i, j, k) = fl;
+    if (MODE >= 1) {
+      const double dr = difry_of(d, i, j, k, fl);
+      FA(DIFRY, i, j, k) = dr;
+      if (MODE == 2) {
+        double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j - 1, k));
+        if (j <= d.ny) {  // FLUX_BC's loop covers j = 1..NY (:940-970)
+          const int ub = PA(UB, j, k);
+          if (i >= ub && ub >= 1) f = 0.0;
+        }
+        FA(FLUXY, i, j, k) = f;
       }
     }
-    if (i <= d.nx && k <= d.nz) {
-      const double fl = flimy_at(d, i, j, k);
-      FA(FLIMY, i, j, k) = fl;
-      if (MODE >= 1) {
-        const double dr = difry_of(d, i, j, k, fl);
-        FA(DIFRY, i, j, k) = dr;
-        if (MODE == 2) {
-          double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j - 1, k));
-          if (j <= d.ny) {  // FLUX_BC's loop covers j = 1..NY (:940-970)
-            const int ub = PA(UB, j, k);
-            if (i >= ub && ub >= 1) f = 0.0;
-          }
-          FA(FLUXY, i, j, k) = f;
+  });
+  TT_CHECK_LAUNCH();
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz + 1), [=] __device__(int i, int j, int k) {
+    const double fl = flimz_at(d, i, j, k);
+    FA(FLIMZ, i, j, k) = fl;
+    if (MODE >= 1) {
+      const double dr = difrz_of(d, i, j, k, fl);
+      FA(DIFRZ, i, j, k) = dr;
+      if (MODE == 2) {
+        double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j, k - 1));
+        if (k <= d.nz) {
+          const int ub = PA(UB, j, k);
+          if (i >= ub && ub >= 1) f = 0.0;
         }
-      }
-    }
-    if (i <= d.nx && j <= d.ny) {
-      const double fl = flimz_at(d, i, j, k);
-      FA(FLIMZ, i, j, k) = fl;
-      if (MODE >= 1) {
-        const double dr = difrz_of(d, i, j, k, fl);
-        FA(DIFRZ, i, j, k) = dr;
-        if (MODE == 2) {
-          double f = -dr * (HA(ER, i, j, k) - HA(ER, i, j, k - 1));
-          if (k <= d.nz) {
-            const int ub = PA(UB, j, k);
-            if (i >= ub && ub >= 1) f = 0.0;
-          }
-          FA(FLUXZ, i, j, k) = f;
-        }
+        FA(FLUXZ, i, j, k) = f;
       }
     }
   });
@@ -482,11 +624,64 @@ static int divf_withf(ttfld_ctx* c, double* out, double theta, bool fill = true)
 // CALCSTELLARTAU pprad.f:191-221, STELLAR_DTAU :223-242 and the grey
 // STELLARINPUT of STELLARINPUT_HEATING :490-502.  STELLARINPUT is declared
 // (1:NX,-1:NY+2,-1:NZ+2) (ppmod.f:341); only i = 1..NX is formed.
+// The wavelength-binned branch of STELLARINPUT_HEATING for IKAPTYP 20-24
+// (pprad.f:433-448): WAVELENGTH_CALCSTELLARTAU (pprad.f:519-547, per bin the
+// optical depth summed from UPPERBND inward, zero elsewhere; one thread per
+// column and bin), then per cell WAVELENGTH_STELLAR_DTAU's central
+// differences (:549-568, dtaus(1) = dtaus(2)) and the bins summed in order,
+// times (RSTAR*RSOL/semi)**2 / dxb(i), for i = 1..NX.
+static int stellar_binned(ttfld_ctx* c) {
+  Dev d = c->d;
+  const int nb = c->wave_nb;
+  const size_t nh = nhalo(d);
+  double* tau = c->stauw;
+  const double* xkapw = c->xkapw;
+  const double* bstar = c->wave + (size_t)c->opac_nt * c->opac_nrh * nb;
+  TT_CHECK(cudaMemsetAsync(tau, 0, nh * nb * sizeof(double), c->stream));
+  launch_box(c->stream, box(0, nb - 1, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int l, int j, int k) {
+    const double dr = G(xxb, 2) - G(xxb, 1);
+    int ub = PA(UB, j, k);
+    if (ub > d.nx + 1) ub = d.nx + 1;
+    const double* kw = xkapw + nh * l;
+    double* tw = tau + nh * l;
+    double tot = 0.0;
+    for (int i = ub; i >= 1; --i) {
+      const size_t q = hidx(d, i, j, k);
+      tot = tot + (kw[q] * d.RH[q] * dr);
+      tw[q] = tot;
+    }
+  });
+  TT_CHECK_LAUNCH();
+  const double f = c->wave_rstar * TT_RSOL / c->wave_semi;
+  const double geo = f * f;
+  launch_box(c->stream, box(1, d.nx, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int i, int j, int k) {
+    const double mu = PA(MU, j, k);
+    const int is = i < 2 ? 2 : i;
+    const size_t q = hidx(d, i, j, k), qm = hidx(d, is - 1, j, k), qp = hidx(d, is + 1, j, k);
+    double si = 0.0;
+    for (int l = 0; l < nb; ++l) {
+      const double* tw = tau + nh * l;
+      const double dtaus = (tw[qm] - tw[qp]) / 2.0;
+      si = si + bstar[l] * (exp(-tw[q] / mu)) * dtaus;
+    }
+    d.SI[q] = si * geo / G(dxb, i);
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
 static int stellarinput_heating(ttfld_ctx* c) {
   Dev d = c->d;
   if (d.f_incident == 0) {
     TT_CHECK(cudaMemsetAsync(d.SI, 0, nhalo(d) * 8, c->stream));
     return 0;
+  }
+  if (c->wave && c->wave_nb > 0) {
+    if (d.kappa_model != 2) {
+      fprintf(stderr, "ttfld: the binned stellar heating needs kappa_model 2 (its per-bin opacities)\n");
+      return TTFLD_E_UNSUPPORTED;
+    }
+    return stellar_binned(c);
   }
   launch_box(c->stream, box(0, 0, -1, d.ny + 2, -1, d.nz + 2), [=] __device__(int, int j, int k) {
     double dr = G(xxb, 2) - G(xxb, 1);
@@ -671,6 +866,41 @@ int ttfld_set_opacity_table(ttfld_ctx* c, const ttfld_opacity_table* t) {
   TT_CHECK(cudaMemcpy(p, t->log_plnk, nn * sizeof(double), cudaMemcpyHostToDevice));
   p += nn;
   TT_CHECK(cudaMemcpy(p, t->log_abs, nn * sizeof(double), cudaMemcpyHostToDevice));
+  return TTFLD_OK;
+}
+
+int ttfld_set_wave_table(ttfld_ctx* c, const ttfld_wave_table* t) {
+  if (!c || !t || t->nbins < 0) return TTFLD_E_ARGS;
+  TT_CHECK(cudaSetDevice(c->device));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  if (c->wave) { cudaFree(c->wave); c->wave = nullptr; }
+  if (c->xkapw) { cudaFree(c->xkapw); c->xkapw = nullptr; c->stauw = nullptr; }
+  c->wave_nb = 0;
+  if (t->nbins == 0) return TTFLD_OK;
+  if (!c->opac || !t->log_waveopac || !t->bstar_bin || !(t->semi > 0.0)) return TTFLD_E_ARGS;
+  const size_t nn = (size_t)c->opac_nt * c->opac_nrh * t->nbins;
+  TT_CHECK(cudaMalloc((void**)&c->wave, (nn + t->nbins) * sizeof(double)));
+  TT_CHECK(cudaMemcpy(c->wave, t->log_waveopac, nn * sizeof(double), cudaMemcpyHostToDevice));
+  TT_CHECK(cudaMemcpy(c->wave + nn, t->bstar_bin, t->nbins * sizeof(double), cudaMemcpyHostToDevice));
+  const size_t nh = nhalo(c->d);
+  TT_CHECK(cudaMalloc((void**)&c->xkapw, 2 * nh * t->nbins * sizeof(double)));
+  TT_CHECK(cudaMemset(c->xkapw, 0, 2 * nh * t->nbins * sizeof(double)));
+  c->stauw = c->xkapw + nh * t->nbins;
+  c->wave_nb = t->nbins;
+  c->wave_rstar = t->rstar;
+  c->wave_semi = t->semi;
+  return TTFLD_OK;
+}
+
+int ttfld_set_freedman_table(ttfld_ctx* c, const ttfld_freedman_table* t) {
+  if (!c || !t || !t->log_ross || !t->log_plnk || !t->log_abs || !(t->mu_gas > 0.0)) return TTFLD_E_ARGS;
+  TT_CHECK(cudaSetDevice(c->device));
+  TT_CHECK(cudaStreamSynchronize(c->stream));
+  if (!c->freed) TT_CHECK(cudaMalloc((void**)&c->freed, (1 + 3 * 42 * 18) * sizeof(double)));
+  TT_CHECK(cudaMemcpy(c->freed + 1, t->log_ross, 42 * 18 * sizeof(double), cudaMemcpyHostToDevice));
+  TT_CHECK(cudaMemcpy(c->freed + 1 + 42 * 18, t->log_plnk, 42 * 18 * sizeof(double), cudaMemcpyHostToDevice));
+  TT_CHECK(cudaMemcpy(c->freed + 1 + 2 * 42 * 18, t->log_abs, 42 * 18 * sizeof(double), cudaMemcpyHostToDevice));
+  c->freed_mu = t->mu_gas;
   return TTFLD_OK;
 }
 

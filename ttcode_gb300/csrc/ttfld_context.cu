@@ -139,7 +139,7 @@ int validate_params(const ttfld_params* p) {
   if (p->f_incident < 0 || p->f_incident > 5) return TTFLD_E_UNSUPPORTED;
   if (p->isigtyp != 0 && p->isigtyp != 1) return TTFLD_E_UNSUPPORTED;
   if (p->ibdrad != 4 && p->ibdrad != 7 && p->ibdrad != 9) return TTFLD_E_UNSUPPORTED;
-  if (p->kappa_model < 0 || p->kappa_model > 2) return TTFLD_E_UNSUPPORTED;
+  if (p->kappa_model < 0 || p->kappa_model > 3) return TTFLD_E_UNSUPPORTED;
   return 0;
 }
 
@@ -282,6 +282,9 @@ int ttfld_destroy(ttfld_ctx* c) {
   mix_free(c);
   krylov_free(c);
   if (c->opac) cudaFree(c->opac);
+  if (c->freed) cudaFree(c->freed);
+  if (c->wave) cudaFree(c->wave);
+  if (c->xkapw) cudaFree(c->xkapw);
   if (c->prev_x) cudaFree(c->prev_x);
   if (c->guess_tmp) cudaFree(c->guess_tmp);
   if (c->slab) cudaFree(c->slab);

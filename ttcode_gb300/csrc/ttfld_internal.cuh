@@ -14,6 +14,8 @@
 #define TT_FD ((double)2.99792458e10f)
 #define TT_ARAD ((double)7.56596e-15f)
 #define TT_SBCONST ((double)5.6705e-5f)
+#define TT_RGAS ((double)8.315e7f)
+#define TT_RSOL ((double)6.9598e10f)
 
 namespace ttfld {
 
@@ -271,6 +273,13 @@ struct ttfld_ctx {
   void* opac;               // opacity table of kappa_model 2 (device), with its sizes
   int opac_nt, opac_nrh;
   double* divf_tab;         // metric quotients of CALCULATEDIVF_WITHF (allocated on first use)
+  double* freed;            // Freedman table of kappa_model 3: ross, plnk, abs (42 x 18 each)
+  double freed_mu;
+  double* wave;             // per-bin opacities (nt x nrh x nbins), then BSTAR_BIN (nbins)
+  int wave_nb;
+  double wave_rstar, wave_semi;
+  double* xkapw;            // per-bin opacities (halo x nbins)
+  double* stauw;            // per-bin stellar optical depth (halo x nbins)
   double last_solve_ms;
 };
 

@@ -181,6 +181,29 @@ class FLD:
         t = _ffi.OpacityTable(nt, nrh, *[a.ctypes.data for a in keep])
         check("ttfld_set_opacity_table", self.L.ttfld_set_opacity_table(self.h, ctypes.byref(t)))
 
+    def set_wave_table(self, log_waveopac, bstar_bin, rstar: float, semi: float):
+        """The per-bin part of the kappa_model 2 table for IKAPTYP 20-24 (KAPPA's
+        per-bin opacities and the binned STELLARINPUT_HEATING): log10
+        BurrowsXKAP_waveopac, shape (nt, nrh, nbins); BSTAR_BIN (nbins); RSTAR
+        (solar radii) and the semi-major axis (cm).  nbins = 0 (an empty
+        bstar_bin) goes back to the grey heating."""
+        bs = np.ascontiguousarray(bstar_bin, dtype=np.float64)
+        w = np.asfortranarray(log_waveopac, dtype=np.float64)
+        if bs.size and w.shape[2] != bs.size:
+            raise ValueError("log_waveopac must be (nt, nrh, nbins) with nbins = len(bstar_bin)")
+        self._wave_keep = (w, bs)
+        t = _ffi.WaveTable(bs.size, w.ctypes.data, bs.ctypes.data, float(rstar), float(semi))
+        check("ttfld_set_wave_table", self.L.ttfld_set_wave_table(self.h, ctypes.byref(t)))
+
+    def set_freedman_table(self, log_ross, log_plnk, log_abs, mu_gas: float):
+        """FreedmanOPC's table for kappa_model 3 (the IKAPTYP 4:5 branch):
+        log10 means on the 42 x 18 (T, P) nodes, and mu_gas."""
+        keep = [np.asfortranarray(a, dtype=np.float64) for a in (log_ross, log_plnk, log_abs)]
+        if any(a.shape != (42, 18) for a in keep):
+            raise ValueError("Freedman means must be (42, 18): FreedmanTVAL x FreedmanPVAL")
+        t = _ffi.FreedmanTableC(*[a.ctypes.data for a in keep], float(mu_gas))
+        check("ttfld_set_freedman_table", self.L.ttfld_set_freedman_table(self.h, ctypes.byref(t)))
+
     def set_burrows_table(self, table):
         """A table of ``opacity.read_burrows_table`` for KAPPA's IKAPTYP 20:25
         branch (pprphy.f:321-351; ``kappa_model`` 2): its nodes and its
@@ -247,6 +270,9 @@ def start_run(shell, device: int = 0, opacity_table=None) -> FLD:
     f = FLD(shell.grid, shell.params, device)
     if opacity_table is not None:
         f.set_burrows_table(opacity_table)
+        t = opacity_table
+        if t.ikaptyp in (20, 21, 22, 23, 24) and t.bstar_bin is not None and t.semi:
+            f.set_wave_table(t.waveopac, t.bstar_bin, t.rstar, t.semi)
     f.load_shell(shell)
     f.set_params(iii=0)
     f.bounds()

@@ -21,6 +21,8 @@ from __future__ import annotations
 
 import os
 
+import numpy as np
+
 from .fortio import ListDirected, integer, real
 from .grid import Grid, gitter
 
@@ -222,10 +224,23 @@ def bottom_gradients(ipp: dict, tinit_bottom: float, rhinit_bottom: float, table
     return None, None
 
 
+def semi_major_axis(ipp: dict) -> float:
+    """The orbit's semi-major axis in cm, pp.f:205-206:
+    (GRAV*MSOL*(mstar1+mstar2)*((Porb*DAY)**2)/(4*PI*PI))**(1/3), with
+    the single-precision constants of ppmod.f:1074-1092."""
+    import math
+    grav, msol, day = float(np.float32(6.672e-8)), float(np.float32(1.989e33)), float(np.float32(8.64e4))
+    pd = ipp["porb"] * day
+    x = grav * msol * (ipp["mstar1"] + ipp["mstar2"]) * (pd * pd) / (4.0 * math.pi * math.pi)
+    return math.pow(x, 1.0 / 3.0)
+
+
 def open_run_directory(directory: str, poles_off: bool = False, **overrides):
     """A ttcode run directory as the set-up reads it: ``ipp`` (readinitfile),
     the restart file ``AKTTD`` (or ``AKTTD_ASCII``, READRESTART) on GITTER's
-    grid, and for IKAPTYP 20-25 the Burrows tables (READBURROWSOPCTABLE).
+    grid, and for IKAPTYP 20-25 the Burrows tables (READBURROWSOPCTABLE;
+    for 20-24 with the BSTAR bins, RSTAR and the semi-major axis the binned
+    stellar heating needs).
     Returns (shell, table, ipp, restart): ``fld.start_run(shell,
     opacity_table=table)`` starts a context from them (for IKAPTYP 4-5 and
     9-14 the caller uploads ``opacity.freedman_kappa`` /
@@ -243,5 +258,6 @@ def open_run_directory(directory: str, poles_off: bool = False, **overrides):
     if params["kappa_model"] == 2:
         table = opacity.read_opacity_tables(directory, ipp["planet_num"], ipp["ikaptyp"], ipp["gamma_opc"],
                                             ipp["mu_gas"])
+        table.rstar, table.semi = ipp["rstar"], semi_major_axis(ipp)
     shell = akttd.shell_of_restart(rst, grid_of_ipp(ipp), params)
     return shell, table, ipp, rst

@@ -162,6 +162,8 @@ class BurrowsTable:
     local_bb: np.ndarray
     bin_tstar: float | None = None
     bstar_bin: np.ndarray | None = None
+    rstar: float | None = None      # RSTAR (solar radii) and the orbit's semi-major axis (cm) of the
+    semi: float | None = None       # run, for the binned stellar heating of IKAPTYP 20-24
     log_t: np.ndarray = field(default_factory=lambda: BURROWS_LOG_T.copy())
     log_rho: np.ndarray = field(default_factory=lambda: BURROWS_LOG_RHO.copy())
 
@@ -599,3 +601,18 @@ def write_burrows_table(path, ikaptyp: int, t_absorption: float, plnk, ross, abs
                 if nval > 5 + WAVE_BINS:
                     row += list(localwave[it, ir, :]) + list(local_bb[it, ir, :])
                 fh.write(" ".join(f"{float(v):.17g}" for v in row) + "\n")
+
+
+def analytic_freedman_table(kap0: float = 1e-2, mu_gas: float = 2.3, dplnk: float = 0.1,
+                            dabs: float = -0.1) -> FreedmanTable:
+    """A table in FreedmanOPC's layout for tests (the reference's table files
+    are not in its tree): on the FreedmanTVAL x FreedmanPVAL nodes, log10 of
+    the analytic kappa = kap0 sqrt(rho) (T/1000)^1.5 with the ideal-gas
+    density rho = P mu_gas / (Rgas T) (P in dyn/cm^2) as the Rosseland
+    mean, offset by dplnk and dabs decades for the Planck and absorption
+    means."""
+    T, P = np.meshgrid(FREEDMAN_T, FREEDMAN_P * 1000.0, indexing="ij")
+    rho = P * mu_gas / (RGAS * T)
+    lk = math.log10(kap0) + 0.5 * np.log10(rho) + 1.5 * np.log10(T / 1000.0)
+    return FreedmanTable(4, 6117.0, np.asfortranarray(lk + dplnk), np.asfortranarray(lk),
+                         np.asfortranarray(lk + dabs))
