@@ -18,10 +18,12 @@ Beside the headline line's timed region, the same run reports
     guess, then the previous step's solution, FP32/FP64) and for the plain
     FP64 SOR (exact rounding and scaled), with the error of each against the
     exact FP64 SOR at EPSMAT = 1e-12 over those steps;
-  * "shell512": the 160 x 512 x 256 shell (dt = 300 s, opacity contrast 1e4):
-    30 implicit steps by the product path and by the plain scaled FP64 SOR,
-    their per-step ratio, errors after 3 steps against the FP64 SOR at
-    1e-12, and the FP32 sweep's roofline at a size beyond L2;
+  * "shell512" / "stiff512": the 160 x 512 x 256 shells (dt = 300 s,
+    opacity contrast 1e4; dt = 1000 s, contrast 1e6): 30 / 10 implicit
+    steps by the product path and by the plain scaled FP64 SOR, their
+    per-step ratio, the learned guess's fallback rate, errors after 3 steps
+    against the FP64 SOR at 1e-12, and the FP32 sweep's roofline at a size
+    beyond L2;
   * "cpu_baseline": complete solves of the bench system by the C oracle (the
     reference loop and stopping rule) on all host cores, and on one core.
 
@@ -466,7 +468,9 @@ def run_gpu(args):
     if rank == 0 and ws == 1:
         line["step"] = step_block(sh, args.steps, blob)
         if not args.no_shell512 and args.steps512 > 0:
-            line["shell512"] = shell512_block(args.steps512, peak, peak_kind)
+            line["shell512"] = big_block("shell512", args.steps512, peak, peak_kind)
+        if not args.no_shell512 and args.stiff_steps > 0:
+            line["stiff512"] = big_block("stiff512", args.stiff_steps, peak, peak_kind)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -503,22 +507,31 @@ def step_block(sh, nsteps, blob):
             "speedup_vs_fp64_exact": v["fp64_exact"]["ms_per_step"] / prod}
 
 
-def shell512_block(nsteps, peak, peak_kind):
-    """The 160 x 512 x 256 shell (dt 300 s, opacity contrast 1e4): nsteps
-    implicit steps by the product path (a network trained on 8 first solves
-    of other irradiations and dt in [150, 600] s of the same shell) and by
-    the plain scaled FP64 SOR from zero, errors after 3 steps against the
-    scaled FP64 SOR at EPSMAT = 1e-12, and the FP32 sweep's CUDA-event
-    roofline on the shell's first system (a working set beyond L2)."""
+BIG_SHELLS = {
+    "shell512": ("160x512x256 (r x phi x theta), 20971520 cells, dt=300 s, opacity contrast 1e4", (150.0, 600.0)),
+    "stiff512": ("160x512x256 (r x phi x theta), 20971520 cells, dt=1000 s, opacity contrast 1e6", (500.0, 2000.0)),
+}
+
+
+def big_block(name, nsteps, peak, peak_kind):
+    """A 160 x 512 x 256 shell (shell512: dt 300 s, opacity contrast 1e4;
+    stiff512: dt 1000 s, contrast 1e6): nsteps implicit steps by the product
+    path (a network trained on 8 first solves of other irradiations and time
+    steps of the same shell; its guess kept only if it beats zero, the
+    fallbacks counted) and by the plain scaled FP64 SOR from zero, errors
+    after 3 steps against the scaled FP64 SOR at EPSMAT = 1e-12, and the
+    FP32 sweep's CUDA-event roofline on the shell's first system (a working
+    set beyond L2)."""
     import torch
     from ttcode_gb300 import runs
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import shell
-    sh = shell("shell512", seed=1)
+    desc, dt_range = BIG_SHELLS[name]
+    sh = shell(name, seed=1)
     sh.params["epsmat"] = 1e-10
     sh.params["itmax"] = 200000
     t0 = time.perf_counter()
-    blob, info = runs.train_guess(sh, 8, 12, 5e-4, (150.0, 600.0))
+    blob, info = runs.train_guess(sh, 8, 12, 5e-4, dt_range)
     snap_at = min(3, nsteps)
     _, ref_snap = runs.run_variant(sh, "fp64_fast", snap_at, snap_at, epsmat=1e-12)
     v = _variants(sh, ("mixed_learned", "fp64_fast"), nsteps, snap_at, ref_snap, blob)
@@ -526,14 +539,23 @@ def shell512_block(nsteps, peak, peak_kind):
     first_system(f)
     nx, ny, nz = sh.dims
     ms = f.time_sweeps("mixed", 50)
+    # SOLVE_WITH_HYPRE on the same EVAL arrays with the reference's settings
+    # (tol 1e-6, 50 iterations): the first call chooses the preconditioner's
+    # sweep count, the second reuses it
+    hyp = []
+    for _ in range(2):
+        h = f.solve_with_hypre()
+        hyp.append({"status": h.status, "iterations": h.sor_iter, "gs_sweeps": h.gs_sweeps, "ms": h.solve_ms,
+                    "ratio": h.rnorm / h.rhsnorm if h.rhsnorm > 0 else None})
     f.close()
     torch.cuda.synchronize()
     achieved = BYTES_FP32_SWEEP * nx * ny * nz / (ms * 1e-3) / 1e9
-    return {"workload": "shell512: 160x512x256 (r x phi x theta), 20971520 cells, dt=300 s, opacity contrast 1e4, "
-                        "seed 1; consecutive implicit steps from the set-up state, tol 1e-10",
+    return {"workload": f"{name}: {desc}, seed 1; consecutive implicit steps from the set-up state, tol 1e-10",
             "steps": nsteps, "training": info,
             "reference": f"scaled FP64 SOR at EPSMAT 1e-12 over the first {snap_at} steps",
             **v, "speedup_per_step_vs_fp64_fast": v["fp64_fast"]["ms_per_step"] / v["mixed_learned"]["ms_per_step"],
+            "fallback_rate": v["mixed_learned"]["fallbacks"] / max(1, nsteps),
+            "solve_with_hypre": {"first": hyp[0], "second": hyp[1]},
             "roofline": {"kernel": "sweeps32_persistent (one full sweep)", "ms_per_sweep": ms,
                          "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * nx * ny * nz, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind},
@@ -652,7 +674,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--steps512", type=int, default=30, help="implicit steps of the 160x512x256 block")
-    ap.add_argument("--no-shell512", action="store_true", help="skip the 160x512x256 block")
+    ap.add_argument("--stiff-steps", type=int, default=10,
+                    help="implicit steps of the 160x512x256 dt=1000 s, contrast 1e6 block")
+    ap.add_argument("--no-shell512", action="store_true", help="skip the 160x512x256 blocks")
     ap.add_argument("--profile-solve", action="store_true",
                     help="only build the system and run one mixed and one exact FP64 solve")
     ap.add_argument("--profile-sweeps", action="store_true",

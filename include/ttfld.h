@@ -198,7 +198,8 @@ typedef struct {
                               guess (network inference, fallback test)    */
   int32_t stalls;          /* FP32 inner runs ended at their rounding floor
                               and re-anchored in FP64 (mixed, PCG)        */
-  int32_t reserved;
+  int32_t gs_sweeps;       /* SOLVE_WITH_HYPRE: symmetric line Gauss-Seidel
+                              sweeps per preconditioner application       */
 } ttfld_solve_stats;
 
 typedef struct {
@@ -289,8 +290,11 @@ int ttfld_solve_system(ttfld_ctx* ctx, ttfld_solve_stats* stats);
  * ||Sigma W (b-Ax)||_2 / ||Sigma W b||_2 <= tol on the symmetrised system,
  * or maxit iterations (then status 1).  tol <= 0 and maxit <= 0 select the
  * reference's 1e-6 and 50 (pphypre.f:45-55).  hypre's SMG preconditioner is
- * replaced by one symmetric red-black Gauss-Seidel sweep over the radial
- * lines (each line solved exactly).  stats may be NULL. */
+ * replaced by m symmetric red-black Gauss-Seidel sweeps over the radial
+ * lines (each line solved exactly): m starts at 1 and, when a solve reaches
+ * maxit before tol, the solve is run again from x = 1 with a larger m
+ * (predicted from the rate it showed); the context keeps m for its next
+ * solves (stats->gs_sweeps).  stats may be NULL. */
 int ttfld_solve_with_hypre(ttfld_ctx* ctx, double tol, int maxit,
                            ttfld_solve_stats* stats);
 /* The IRAD=1 radiation step, RADDIF (pprad.f:1-38): ER = arad T^4, DIFFEL

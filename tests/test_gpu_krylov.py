@@ -116,3 +116,27 @@ def test_hypre_iteration_limit_reports_status(small):
     o, f, x_ref = _hypre_case(small)
     st = f.solve_with_hypre(tol=1e-14, maxit=3)
     assert st.status == 1 and st.sor_iter == 3
+
+
+def test_hypre_strengthens_its_preconditioner_to_meet_the_cap():
+    """On a 160x256x128 shell (opacity contrast 1e4, dt 300 s) one symmetric
+    line Gauss-Seidel sweep per preconditioner application needs more than
+    20 PCG iterations for tol 1e-6; with a cap of 20 SOLVE_WITH_HYPRE runs
+    the solve again with more sweeps and ends with status 0 within the cap,
+    its answer within 1e-4 of the same system's 1e-12 solution, and the
+    context keeps the sweep count for its next solve."""
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(160, 256, 128, seed=1, delt=300.0, contrast=1e4)
+    f = start_run(sh)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)                  # leaves the EVAL arrays of a real step
+    st_ref = f.solve_with_hypre(tol=1e-12, maxit=5000)
+    assert st_ref.status == 0 and st_ref.gs_sweeps == 1
+    ref = f.download("DELTA_ER")[2:-2, 2:-2, 2:-2]
+    st = f.solve_with_hypre(tol=1e-6, maxit=20)
+    assert st.status == 0 and st.sor_iter <= 20 and st.gs_sweeps > 1, (st.status, st.sor_iter, st.gs_sweeps)
+    assert rel_l2(f.download("DELTA_ER")[2:-2, 2:-2, 2:-2], ref) <= 1e-4
+    st2 = f.solve_with_hypre(tol=1e-6, maxit=20)
+    assert st2.status == 0 and st2.gs_sweeps == st.gs_sweeps and st2.sor_iter <= 20
+    f.close()

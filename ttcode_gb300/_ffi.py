@@ -54,7 +54,7 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("sor_iter", c_int32), ("corrections", c_int32), ("fallback", c_int32),
                 ("status", c_int32), ("rnorm", c_double), ("rhsnorm", c_double),
                 ("true_resid_l1", c_double), ("guess_resid_l1", c_double), ("solve_ms", c_double),
-                ("guess_ms", c_double), ("stalls", c_int32), ("reserved", c_int32)]
+                ("guess_ms", c_double), ("stalls", c_int32), ("gs_sweeps", c_int32)]
 
 
 class RaddifParams(ctypes.Structure):

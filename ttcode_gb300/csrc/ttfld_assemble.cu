@@ -373,31 +373,28 @@ __device__ __forceinline__ double flimz_calc(const Dev& d, int i, int j, int k) 
 __device__ __forceinline__ double flimx_at(const Dev& d, int i, int j, int k) {
   if (d.iflimtyp == 1) return 1.0 / 3.0;
   const int ub = PA(UB, j, k);
-  if (i <= ub - 1) return flimx_calc(d, i, j, k);
-  if (ub >= 2 && ub <= d.nx + 1) return flimx_calc(d, ub - 1, j, k);
-  return FA(FLIMX, i, j, k);
+  if (i > ub - 1 && !(ub >= 2 && ub <= d.nx + 1)) return FA(FLIMX, i, j, k);
+  return flimx_calc(d, i <= ub - 1 ? i : ub - 1, j, k);   // one inlined copy of the face
 }
 
 // The y and z loops form the faces up to the last x loop's xmax_index,
 // UPPERBND(NY,NZ)-1 (:464, :495); the copies of :485-489 and :516-520 then
 // give every face from UPPERBND(j,k) up the value of UPPERBND(j,k)-1.
-__device__ __forceinline__ double flimy_loop(const Dev& d, int i, int j, int k) {
-  return i <= PA(UB, d.ny, d.nz) - 1 ? flimy_calc(d, i, j, k) : FA(FLIMY, i, j, k);
+// The face whose value face (i,j,k) ends with: itself, or UPPERBND-1 from
+// UPPERBND up (one inlined copy of the face computation).
+__device__ __forceinline__ int flim_source(const Dev& d, int i, int j, int k) {
+  const int ub = PA(UB, j, k);
+  return (ub >= 2 && ub <= d.nx + 1 && i >= ub) ? ub - 1 : i;
 }
 __device__ __forceinline__ double flimy_at(const Dev& d, int i, int j, int k) {
   if (d.iflimtyp == 1) return 1.0 / 3.0;
-  const int ub = PA(UB, j, k);
-  if (ub >= 2 && ub <= d.nx + 1 && i >= ub) return flimy_loop(d, ub - 1, j, k);
-  return flimy_loop(d, i, j, k);
-}
-__device__ __forceinline__ double flimz_loop(const Dev& d, int i, int j, int k) {
-  return i <= PA(UB, d.ny, d.nz) - 1 ? flimz_calc(d, i, j, k) : FA(FLIMZ, i, j, k);
+  const int is = flim_source(d, i, j, k);
+  return is <= PA(UB, d.ny, d.nz) - 1 ? flimy_calc(d, is, j, k) : FA(FLIMY, is, j, k);
 }
 __device__ __forceinline__ double flimz_at(const Dev& d, int i, int j, int k) {
   if (d.iflimtyp == 1) return 1.0 / 3.0;
-  const int ub = PA(UB, j, k);
-  if (ub >= 2 && ub <= d.nx + 1 && i >= ub) return flimz_loop(d, ub - 1, j, k);
-  return flimz_loop(d, i, j, k);
+  const int is = flim_source(d, i, j, k);
+  return is <= PA(UB, d.ny, d.nz) - 1 ? flimz_calc(d, is, j, k) : FA(FLIMZ, is, j, k);
 }
 
 // DIFF pprad.f:74-156, one face of each direction (with the ieta = 5 floor).

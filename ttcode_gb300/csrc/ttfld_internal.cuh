@@ -273,6 +273,7 @@ struct ttfld_ctx {
   void* opac;               // opacity table of kappa_model 2 (device), with its sizes
   int opac_nt, opac_nrh;
   double* divf_tab;         // metric quotients of CALCULATEDIVF_WITHF (allocated on first use)
+  int hypre_gs;             // SOLVE_WITH_HYPRE's symmetric line Gauss-Seidel sweeps (0: not yet chosen)
   double* freed;            // Freedman table of kappa_model 3: ross, plnk, abs (42 x 18 each)
   double freed_mu;
   double* wave;             // per-bin opacities (nt x nrh x nbins), then BSTAR_BIN (nbins)

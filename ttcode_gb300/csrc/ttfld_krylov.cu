@@ -54,6 +54,7 @@ namespace {
 constexpr int kPcgThreads = 256;   // one block per SM; 248 registers for the batched passes
 constexpr int kPcgStall = 25;      // iterations without a new minimum of r.z end an inner run
 constexpr double kInnerReduce = 1e-4;  // relative reduction of sqrt(r.z) asked of one inner run
+constexpr int kMaxGsSweeps = 32;       // symmetric line Gauss-Seidel sweeps per preconditioner application
 
 struct Kry {
   int nx, ny, nz;
@@ -508,14 +509,16 @@ __device__ __forceinline__ float op_one(const Kry& k, const float* po, float* pn
 }
 
 // z = M^-1 r for the preconditioner M, with UPDATE first r -= alpha s.
-// SGS: one symmetric red-black line Gauss-Seidel sweep (red lines, black
-// lines against the new red z, red lines against the black z; two more grid
-// barriers); otherwise the radial line solve of every column (block
-// Jacobi).  acc gains this thread's share of r.z.  False if a barrier gave
-// up.
+// SGS: `sweeps` symmetric red-black line Gauss-Seidel sweeps from z = 0
+// (red lines, then black lines against the new red z, red against the new
+// black, ...: 2 sweeps + 1 colour passes, a grid barrier between passes; two
+// symmetric sweeps in a row share their middle red pass), a symmetric
+// preconditioner; otherwise the radial line solve of every column (block
+// Jacobi).  acc gains this thread's share of r.z (from each colour's last
+// pass).  False if a barrier gave up.
 template <bool UPDATE, bool SGS>
 __device__ __forceinline__ bool precondition(const Kry& k, SolverDev* sol, unsigned int nb, long long col0,
-                                             long long colstride, float alpha, float& acc) {
+                                             long long colstride, float alpha, float& acc, int sweeps) {
   if (!SGS) {
     for (long long c = col0; c < k.ncol; c += colstride) acc += line_pass<UPDATE>(k, c, alpha);
     return true;
@@ -523,9 +526,16 @@ __device__ __forceinline__ bool precondition(const Kry& k, SolverDev* sol, unsig
   const long long half = k.ncol >> 1;
   for (long long m = col0; m < half; m += colstride) (void)line_pass<UPDATE>(k, col_of(m, 0, k.ny), alpha);
   if (!grid_sync(sol, nb)) return false;
-  for (long long m = col0; m < half; m += colstride) acc += line_gs<UPDATE>(k, col_of(m, 1, k.ny), alpha);
-  if (!grid_sync(sol, nb)) return false;
-  for (long long m = col0; m < half; m += colstride) acc += line_gs<false>(k, col_of(m, 0, k.ny), 0.f);
+  float ab = 0.f;  // r.z of the black lines' first pass (their last with one sweep)
+  for (long long m = col0; m < half; m += colstride) ab += line_gs<UPDATE>(k, col_of(m, 1, k.ny), alpha);
+  if (sweeps == 1) acc += ab;
+#pragma unroll 1
+  for (int p = 2; p <= 2 * sweeps; ++p) {
+    if (!grid_sync(sol, nb)) return false;
+    float ap = 0.f;
+    for (long long m = col0; m < half; m += colstride) ap += line_gs<false>(k, col_of(m, p & 1, k.ny), 0.f);
+    if (p >= 2 * sweeps - 1) acc += ap;  // the last pass of its colour
+  }
   return true;
 }
 
@@ -542,7 +552,7 @@ __device__ __forceinline__ bool precondition(const Kry& k, SolverDev* sol, unsig
 // (sol->scratch[2]).
 template <bool SGS>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, SolverDev* sol, double* partials,
-                                                                   int maxit, double stop_ratio) {
+                                                                   int maxit, double stop_ratio, int sweeps) {
   __shared__ double sh[32];
   __shared__ double bc[3];
   const unsigned int nb = gridDim.x;
@@ -560,7 +570,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   // terms) are FP32 -- GB300's FP64 pipe is narrow -- and widened to FP64
   // for the block and grid sums.
   float acc = 0.f;
-  if (!precondition<false, SGS>(k, sol, nb, col0, colstride, 0.f, acc)) return;
+  if (!precondition<false, SGS>(k, sol, nb, col0, colstride, 0.f, acc, sweeps)) return;
   {
     const double v = block_sum((double)acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -617,7 +627,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     const float alpha = (float)(gamma / ps);
     // line phase: r -= alpha s, z = M^-1 r, r.z
     acc = 0.f;
-    if (!precondition<true, SGS>(k, sol, nb, col0, colstride, alpha, acc)) return;
+    if (!precondition<true, SGS>(k, sol, nb, col0, colstride, alpha, acc, sweeps)) return;
     {
       const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -716,7 +726,8 @@ int pcg_blocks(long long ncells) {
 }
 
 // One inner run; returns its iterations in *its.
-int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, bool sgs, int* its) {
+// gs: 0 block-Jacobi radial lines, m >= 1 m symmetric line Gauss-Seidel sweeps.
+int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int gs, int* its) {
   const int nb = pcg_blocks(w->k.n);
   if (nb <= 0) {
     fprintf(stderr, "ttfld: the PCG solver needs cooperative launch\n");
@@ -729,8 +740,9 @@ int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, bool sg
   Kry k = w->k;
   SolverDev* sol = c->sol;
   double* partials = c->partials;
-  void* args[] = {&k, &sol, &partials, &maxit, &stop_ratio};
-  const void* kern = sgs ? (const void*)pcg32_persistent<true> : (const void*)pcg32_persistent<false>;
+  int sweeps = gs > 0 ? gs : 1;
+  void* args[] = {&k, &sol, &partials, &maxit, &stop_ratio, &sweeps};
+  const void* kern = gs > 0 ? (const void*)pcg32_persistent<true> : (const void*)pcg32_persistent<false>;
   TT_CHECK(cudaLaunchCooperativeKernel(kern, dim3(nb), dim3(kPcgThreads), args, 0, c->stream));
   count_launches(1);
   int rc = poll_sol(c);
@@ -770,7 +782,7 @@ int prepare(ttfld_ctx* c, KryWork* w, bool hypre) {
 // tol (the hypre system's PCG rule on the symmetric form).  budget bounds
 // the PCG iterations.  With guess_test, the initial iterate is kept only if
 // its preconditioned residual norm r.z is below that of the zero iterate.
-int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, long long budget, bool l2, bool sgs,
+int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, long long budget, bool l2, int gs,
              int guess_test, int* fallback, ttfld_solve_stats* st) {
   KryWork* w = kry_work(c);
   if (!w) return TTFLD_E_CUDA;
@@ -785,7 +797,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
   }
   if (guess_test) {
     int its = 0;
-    if ((rc = launch_inner(c, w, 0, 0.0, sgs, &its))) return rc;
+    if ((rc = launch_inner(c, w, 0, 0.0, gs, &its))) return rc;
     const double g_guess = c->host_sol->scratch[2];
     // the zero iterate: r = b
     double* zero_x = c->guess_tmp;
@@ -794,7 +806,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
       zero_x = c->guess_tmp;
     }
     TT_CHECK(cudaMemsetAsync(zero_x, 0, nhalo(c->d) * 8, c->stream));
-    if ((rc = anchor(c, w, zero_x, b, hypre, l2, false)) || (rc = launch_inner(c, w, 0, 0.0, sgs, &its))) return rc;
+    if ((rc = anchor(c, w, zero_x, b, hypre, l2, false)) || (rc = launch_inner(c, w, 0, 0.0, gs, &its))) return rc;
     const double g_zero = c->host_sol->scratch[2];
     if (!(g_guess < g_zero)) {
       TT_CHECK(cudaMemsetAsync(x, 0, nhalo(c->d) * 8, c->stream));
@@ -826,7 +838,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
     if (target < kInnerReduce) target = kInnerReduce;
     long long left = budget - total;
     int its = 0;
-    if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, sgs, &its))) return rc;
+    if ((rc = launch_inner(c, w, (int)(left < 1000000 ? left : 1000000), target, gs, &its))) return rc;
     total += its;
     ++anchors;
     if (c->host_sol->stalled) ++stalls;
@@ -856,7 +868,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
 
 int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
-  return pcg_core(c, x, b, false, c->opts.tol, budget, false, false, guess_test, fallback, st);
+  return pcg_core(c, x, b, false, c->opts.tol, budget, false, 0, guess_test, fallback, st);
 }
 
 void krylov_free(ttfld_ctx* c) {
@@ -882,13 +894,35 @@ int ttfld_solve_with_hypre(ttfld_ctx* c, double tol, int maxit, ttfld_solve_stat
   int rc = fill_sor_matrix(c, false);  // the 7-point rows; b is taken from RHS_ER as it is
   if (rc) return rc;
   Dev d = c->d;
-  // x = 1 in the interior (pphypre.f:136); the halo is left as it is, as
-  // SOLVE_WITH_HYPRE only writes delta_ER(1:NX,1:NY,1:NZ) (pphypre.f:84-92)
   double* x = d.DELTA_ER;
-  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) { x[hidx(d, i, j, k)] = 1.0; });
-  TT_CHECK_LAUNCH();
+  // hypre's PCG is preconditioned by a multigrid cycle, which keeps its
+  // iteration count nearly independent of the grid; the line Gauss-Seidel
+  // preconditioner here needs more iterations on finer (phi, theta) grids.
+  // Its strength is the number m of symmetric sweeps per application: a
+  // solve that reaches the iteration cap before tol is run again from
+  // x = 1 with m raised from the rate that solve showed (iterations scale
+  // about as m^-1/2), and the context keeps m for its later solves.
+  int m = c->hypre_gs > 0 ? c->hypre_gs : 1;
   TT_CHECK(cudaEventRecord(c->ev0, c->stream));
-  rc = pcg_core(c, x, d.RHS, true, tol, maxit, true, true, 0, nullptr, st);
+  for (;;) {
+    // x = 1 in the interior (pphypre.f:136); the halo is left as it is, as
+    // SOLVE_WITH_HYPRE only writes delta_ER(1:NX,1:NY,1:NZ) (pphypre.f:84-92)
+    launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) { x[hidx(d, i, j, k)] = 1.0; });
+    TT_CHECK_LAUNCH();
+    rc = pcg_core(c, x, d.RHS, true, tol, maxit, true, m, 0, nullptr, st);
+    if (rc != TTFLD_MAXITER || m >= kMaxGsSweeps) break;
+    const double ratio = st->rhsnorm > 0.0 ? st->rnorm / st->rhsnorm : 1.0;
+    double grow = 4.0;
+    if (ratio > 0.0 && ratio < 1.0) {
+      const double need = maxit * log(tol) / log(ratio);  // iterations at this m, at this rate
+      const double f = need / (0.8 * maxit);
+      grow = f * f;
+    }
+    int m2 = (int)ceil(m * (grow < 2.0 ? 2.0 : grow));
+    m = m2 < kMaxGsSweeps ? m2 : kMaxGsSweeps;
+  }
+  c->hypre_gs = m;
+  st->gs_sweeps = m;
   TT_CHECK(cudaEventRecord(c->ev1, c->stream));
   TT_CHECK(cudaEventSynchronize(c->ev1));
   float ms = 0.f;
