@@ -23,6 +23,7 @@
 // Backward-data is the same kernel on flipped, transposed weights; the weight
 // gradient is a GEMM over voxels (A = gradient^T, B = shifted input) reduced
 // with FP32 atomics (so training is not bitwise reproducible; inference is).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdlib.h>
@@ -320,20 +321,31 @@ static int launch_conv_smem(cudaStream_t s, const ConvArgs& a) {
 }
 
 // ---- tcgen05 form for the large levels ------------------------------------
-// The same convolution on the 5th-generation tensor cores: a CTA computes
-// M = 128 output voxels (8 along x times 16 along y, one z-plane) times
-// N = cout (16 or 32) as 27 * cin/16 tcgen05.mma (kind::f16, BF16 x BF16 ->
-// FP32) accumulating in tensor memory, issued by one thread and completed on
-// an mbarrier; four warps read the accumulators back (tcgen05.ld) for the
+// The same convolution on the 5th-generation tensor cores.  An output tile
+// is M = 128 voxels (8 along x times 16 along y, one z-plane) times N = cout
+// (16 or 32): 27 * cin/16 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32)
+// accumulate it in tensor memory, issued by one thread and completed on an
+// mbarrier; four warps read the accumulators back (tcgen05.ld) for the
 // epilogue.  Operands sit in shared memory without swizzle in the canonical
 // K-major core-matrix layout (8 rows x 16 bytes): the input tile with its
-// halo (10 x 18 x 3 voxels) is stored channel-group-major, [cin/8][voxel]
-// of 16 bytes, so that for any tap the 8 x-voxels of an output row are one
-// core matrix, consecutive rows are one halo row (160 bytes) apart and the
-// next 8 channels one group apart; the weights likewise as [tap][cin/8][cout].
+// halo (10 x 18 x 3 voxels) channel-group-major, [cin/8][z][y][x] of 16
+// bytes, so that for any tap the 8 x-voxels of an output row are one core
+// matrix, consecutive rows one halo row (160 bytes) apart and the next 8
+// channels one group apart; the weights likewise as [tap][cin/8][cout].
+//
+// The CTAs are persistent (one per SM): each stages all 27 taps' weights
+// once and walks its share of the tiles.  Each 8-channel group of a tile's
+// input is one 4-D tensor-memory-access copy (cp.async.bulk.tensor, box
+// 8 channels x 10 x 18 x 3 voxels; the zero padding in r and theta is the
+// copy's out-of-bounds fill), into a ring of two stages, so the next tile's
+// input streams in while this tile's MMAs and epilogue run.  The periodic
+// phi halo rows of the first and last y-tiles are fetched by a one-row copy
+// into a side buffer and moved into place by the threads.
 constexpr int kUX = 8, kUY = 16;
 constexpr int kUHX = kUX + 2, kUHY = kUY + 2, kUHZ = 3;
 constexpr int kUHalo = kUHX * kUHY * kUHZ;
+constexpr int kUSlab = (kUHalo * 16 + 127) / 128 * 128;   // one channel group of a stage, 128-B aligned
+constexpr int kURow = (kUHX * kUHZ * 16 + 127) / 128 * 128;  // one wrapped phi row of one channel group
 constexpr long long kUmmaSpins = 1LL << 24;
 __device__ int g_umma_error;  // set when a wait of the tcgen05 form ran out
 
@@ -360,6 +372,13 @@ __device__ __forceinline__ bool umma_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// Bounded wait for a phase of an mbarrier.
+__device__ __forceinline__ bool umma_wait(uint64_t* bar, uint32_t parity) {
+  long long n = 0;
+  while (!umma_try_wait(bar, parity))
+    if (++n > kUmmaSpins) return false;
+  return true;
+}
 
 #define TT_LD16(taddr, r)                                                                                          \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
@@ -369,96 +388,171 @@ __device__ __forceinline__ bool umma_try_wait(uint64_t* bar, uint32_t parity) {
                  "=r"(r[15])                                                                                     \
                : "r"(taddr))
 
+// Shared memory of the tcgen05 form: two input stages, their side rows
+// (two wrapped rows each), the weights.
 static size_t conv_tc_smem_bytes(int cin, int cout) {
-  return (size_t)(cin / 8) * kUHalo * 16 + (size_t)27 * (cin / 8) * cout * 16;
+  const size_t G = cin / 8;
+  return 2 * G * kUSlab + 2 * 2 * G * kURow + (size_t)27 * G * cout * 16 + 128;
+}
+
+struct TcTile {
+  int x0, y0, z0;
+  int lo, hi;  // halo rows to take from the wrapped phi rows (0 / 17, or -1)
+};
+__device__ __forceinline__ TcTile tc_tile(const ConvArgs& a, long long t) {
+  const int XT = (a.X + kUX - 1) / kUX, YT = (a.Y + kUY - 1) / kUY;
+  TcTile r;
+  r.x0 = (int)(t % XT) * kUX;
+  r.y0 = (int)((t / XT) % YT) * kUY;
+  r.z0 = (int)(t / ((long long)XT * YT));
+  r.lo = r.y0 == 0 ? 0 : -1;                 // halo row y0-1 = -1 is row Y-1
+  const int h = a.Y - r.y0 + 1;              // the halo row that holds y = Y (row 0)
+  r.hi = h <= kUHY - 1 ? h : -1;
+  return r;
+}
+
+// Thread 0: queue the copies of a tile into stage s (8-channel groups; the
+// wrapped rows into the stage's side rows), completing on bar.
+__device__ __forceinline__ void tc_issue(const CUtensorMap* tm, const CUtensorMap* tr, const ConvArgs& a,
+                                         const TcTile& t, unsigned char* stage, unsigned char* side, uint64_t* bar) {
+  const int G = a.cin >> 3;
+  const uint32_t bytes = (uint32_t)G * (kUHalo * 16 + ((t.lo >= 0) + (t.hi >= 0)) * kUHX * kUHZ * 16);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+  for (int g = 0; g < G; ++g) {
+    const int c = a.in_co + 8 * g;
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(saddr(stage + (size_t)g * kUSlab)),
+        "l"((unsigned long long)tm), "r"(c), "r"(t.x0 - 1), "r"(t.y0 - 1), "r"(t.z0 - 1), "r"(saddr(bar))
+        : "memory");
+    if (t.lo >= 0)
+      asm volatile(
+          "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+          "[%6];" ::"r"(saddr(side + (size_t)(2 * g) * kURow)),
+          "l"((unsigned long long)tr), "r"(c), "r"(t.x0 - 1), "r"(a.Y - 1), "r"(t.z0 - 1), "r"(saddr(bar))
+          : "memory");
+    if (t.hi >= 0)
+      asm volatile(
+          "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+          "[%6];" ::"r"(saddr(side + (size_t)(2 * g + 1) * kURow)),
+          "l"((unsigned long long)tr), "r"(c), "r"(t.x0 - 1), "r"(0), "r"(t.z0 - 1), "r"(saddr(bar))
+          : "memory");
+  }
 }
 
 template <int N>
-__global__ void __launch_bounds__(128) conv3_tc_kernel(ConvArgs a) {
-  extern __shared__ __align__(128) unsigned char usm[];
-  __shared__ __align__(8) uint64_t mbar;
+__global__ void __launch_bounds__(128, 1) conv3_tc_kernel(ConvArgs a, const __grid_constant__ CUtensorMap tmain,
+                                                          const __grid_constant__ CUtensorMap trow, long long ntiles) {
+  extern __shared__ __align__(128) unsigned char usm_raw[];
+  unsigned char* usm = (unsigned char*)(((uintptr_t)usm_raw + 127) & ~(uintptr_t)127);
+  __shared__ __align__(8) uint64_t full_bar[2];
+  __shared__ __align__(8) uint64_t mma_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int ok_sh;
   const int G = a.cin >> 3;
-  unsigned char* tin = usm;
-  unsigned char* tw = usm + (size_t)G * kUHalo * 16;
-  const int XT = (a.X + kUX - 1) / kUX, YT = (a.Y + kUY - 1) / kUY;
-  const int bx = (int)(blockIdx.x % XT), by = (int)((blockIdx.x / XT) % YT), z0 = (int)(blockIdx.x / (XT * YT));
-  const int x0 = bx * kUX, y0 = by * kUY;
-  for (int q = threadIdx.x; q < kUHalo * G; q += blockDim.x) {
-    const int g = q / kUHalo, hv = q % kUHalo;
-    const int hx = hv % kUHX, hy = (hv / kUHX) % kUHY, hz = hv / (kUHX * kUHY);
-    const int x = x0 + hx - 1, z = z0 + hz - 1;
-    const int y = ((y0 + hy - 1) % a.Y + a.Y) % a.Y;  // periodic phi
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (x >= 0 && x < a.X && z >= 0 && z < a.Z)
-      v = *reinterpret_cast<const uint4*>(a.in + (((size_t)z * a.Y + y) * a.X + x) * a.in_cs + a.in_co + g * 8);
-    *reinterpret_cast<uint4*>(tin + ((size_t)g * kUHalo + hv) * 16) = v;
+  unsigned char* stage[2] = {usm, usm + (size_t)G * kUSlab};
+  unsigned char* side[2] = {usm + 2 * (size_t)G * kUSlab, usm + 2 * (size_t)G * kUSlab + 2 * (size_t)G * kURow};
+  unsigned char* tw = usm + 2 * (size_t)G * kUSlab + 4 * (size_t)G * kURow;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&full_bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&full_bar[1])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&mma_bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ok_sh = 1;
   }
+  __syncthreads();
+  // the first two tiles' input streams in while the weights are staged
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 2; ++q) {
+      const long long t = blockIdx.x + (long long)q * gridDim.x;
+      if (t < ntiles) tc_issue(&tmain, &trow, a, tc_tile(a, t), stage[q], side[q], &full_bar[q]);
+    }
   for (int q = threadIdx.x; q < 27 * G * N; q += blockDim.x) {
     const int n = q % N, g = (q / N) % G, t = q / (N * G);
     *reinterpret_cast<uint4*>(tw + (size_t)q * 16) =
         *reinterpret_cast<const uint4*>(a.w + ((size_t)t * N + n) * a.cin + g * 8);
-  }
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&mbar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (threadIdx.x < 32) {  // warp 0 owns the tensor-memory allocation
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(saddr(&tmem_base))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the operands, for the tensor core
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the weights, for the tensor core
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  if (threadIdx.x == 0) {
-    const uint32_t idesc = umma_idesc(N);
-    const uint32_t ta = saddr(tin), wa = saddr(tw);
-    const uint32_t lbo_a = kUHalo * 16, sbo_a = kUHX * 16;
-    const uint32_t lbo_b = N * 16, sbo_b = 8 * 16;
-    uint32_t acc = 0;
-    for (int t = 0; t < 27; ++t) {
-      const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
-      const uint32_t voff = (uint32_t)((dz * kUHY + dy) * kUHX + dx) * 16;
-      for (int k2 = 0; k2 < G; k2 += 2) {
-        const uint64_t ad = umma_desc(ta + (uint32_t)k2 * lbo_a + voff, lbo_a, sbo_a);
-        const uint64_t bd = umma_desc(wa + (uint32_t)((t * G + k2) * N) * 16, lbo_b, sbo_b);
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-            : "memory");
-        acc = 1;
-      }
-    }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(&mbar))
-                 : "memory");
-    long long n = 0;
-    bool ok = true;
-    while (!umma_try_wait(&mbar, 0)) {
-      if (++n > kUmmaSpins) { ok = false; break; }
-    }
-    ok_sh = ok ? 1 : 0;
-    if (!ok) atomicExch(&g_umma_error, 1);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (ok_sh) {
-    // warp w reads tensor-memory lanes 32w .. 32w+31: output row m = 32w + lane
+  long long issued = blockIdx.x + 2LL * gridDim.x;  // the next tile to queue
+  int it = 0;
+  bool mma_pending = false;  // thread 0: MMAs committed but not yet seen complete
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it & 1;
+    const TcTile t = tc_tile(a, tile);
+    // 1. this tile's input has landed
+    if (!umma_wait(&full_bar[s], (uint32_t)((it >> 1) & 1))) atomicExch(&ok_sh, 0);
+    // 2. the wrapped phi halo rows into place
+    if ((t.lo >= 0 || t.hi >= 0) && ok_sh) {
+      for (int q = threadIdx.x; q < 2 * G * kUHX * kUHZ; q += blockDim.x) {
+        const int which = q / (G * kUHX * kUHZ), r = q % (G * kUHX * kUHZ);
+        const int g = r / (kUHX * kUHZ), v = r % (kUHX * kUHZ), hz = v / kUHX, hx = v % kUHX;
+        const int hy = which ? t.hi : t.lo;
+        if (hy < 0) continue;
+        *reinterpret_cast<uint4*>(stage[s] + (size_t)g * kUSlab + (size_t)((hz * kUHY + hy) * kUHX + hx) * 16) =
+            *reinterpret_cast<const uint4*>(side[s] + (size_t)(2 * g + which) * kURow + (size_t)v * 16);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // the stage is complete; the last epilogue's tensor-memory reads are done
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok_sh) break;
+    // 3. the MMAs of this tile, committed to mma_bar
+    if (threadIdx.x == 0) {
+      const uint32_t idesc = umma_idesc(N);
+      const uint32_t ta = saddr(stage[s]), wa = saddr(tw);
+      const uint32_t lbo_a = kUSlab, sbo_a = kUHX * 16;
+      const uint32_t lbo_b = N * 16, sbo_b = 8 * 16;
+      uint32_t acc = 0;
+      for (int tp = 0; tp < 27; ++tp) {
+        const int dz = tp / 9, dy = (tp / 3) % 3, dx = tp % 3;
+        const uint32_t voff = (uint32_t)((dz * kUHY + dy) * kUHX + dx) * 16;
+        for (int k2 = 0; k2 < G; k2 += 2) {
+          const uint64_t ad = umma_desc(ta + (uint32_t)k2 * lbo_a + voff, lbo_a, sbo_a);
+          const uint64_t bd = umma_desc(wa + (uint32_t)((tp * G + k2) * N) * 16, lbo_b, sbo_b);
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+              : "memory");
+          acc = 1;
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       saddr(&mma_bar))
+                   : "memory");
+      // 4. the MMAs are done: the accumulators are ready and the stage is free
+      mma_pending = !umma_wait(&mma_bar, (uint32_t)(it & 1));
+      if (mma_pending) ok_sh = 0;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok_sh) break;
+    // 5. queue the tile two ahead into this stage
+    if (threadIdx.x == 0 && issued < ntiles) {
+      tc_issue(&tmain, &trow, a, tc_tile(a, issued), stage[s], side[s], &full_bar[s]);
+      issued += gridDim.x;
+    }
+    // 6. epilogue: warp w reads tensor-memory lanes 32w .. 32w+31 (output row m = 32w + lane)
     uint32_t r[N];
-    const uint32_t ta = tmem + ((uint32_t)(32 * w) << 16);
-    TT_LD16(ta, r);
-    if (N == 32) TT_LD16(ta + 16, (r + 16));
+    const uint32_t tl = tmem + ((uint32_t)(32 * w) << 16);
+    TT_LD16(tl, r);
+    if (N == 32) TT_LD16(tl + 16, (r + 16));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int m = 32 * w + lane;
-    const int x = x0 + (m & 7), y = y0 + (m >> 3);
+    const int x = t.x0 + (m & 7), y = t.y0 + (m >> 3);
     if (x < a.X && y < a.Y) {
-      bf16* po = a.out + (((size_t)z0 * a.Y + y) * a.X + x) * a.out_cs + a.out_co;
+      bf16* po = a.out + (((size_t)t.z0 * a.Y + y) * a.X + x) * a.out_cs + a.out_co;
 #pragma unroll
       for (int c = 0; c < N; c += 2) {
         float v0 = __uint_as_float(r[c]), v1 = __uint_as_float(r[c + 1]);
@@ -468,11 +562,28 @@ __global__ void __launch_bounds__(128) conv3_tc_kernel(ConvArgs a) {
         *reinterpret_cast<uint32_t*>(po + c) = pack2(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
       }
     }
-  } else if (threadIdx.x == 0) {
-    // the copies in flight must end before the tensor memory is released
-    long long n = 0;
-    while (!umma_try_wait(&mbar, 0) && ++n < kUmmaSpins) {
+  }
+  __syncthreads();
+  if (!ok_sh) {
+    if (threadIdx.x == 0) {
+      atomicExch(&g_umma_error, 1);
+      // the copies and MMAs in flight end before the shared and tensor
+      // memory go (bounded waits): the MMAs of tile `it` if they were left
+      // running, and the copies of tiles it and it+1 (a phase already
+      // observed passes at once)
+      if (mma_pending) {
+        long long n = 0;
+        while (!umma_try_wait(&mma_bar, (uint32_t)(it & 1)) && ++n < kUmmaSpins) {
+        }
+      }
+      for (int q = 0; q < 2; ++q) {
+        if (blockIdx.x + (long long)(it + q) * gridDim.x >= ntiles) continue;  // never queued
+        long long n = 0;
+        while (!umma_try_wait(&full_bar[(it + q) & 1], (uint32_t)(((it + q) >> 1) & 1)) && ++n < kUmmaSpins) {
+        }
+      }
     }
+    __syncthreads();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -481,18 +592,68 @@ __global__ void __launch_bounds__(128) conv3_tc_kernel(ConvArgs a) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
 }
 
+// cuTensorMapEncodeTiled, reached through the runtime (the library links
+// only cudart).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+// The input activations as a 4-D BF16 tensor (channels of the whole
+// buffer, x, y, z), boxes of 8 channels x 10 x ny x 3 voxels.
+static bool tc_tensor_map(CUtensorMap* tm, const ConvArgs& a, int ny) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)a.in_cs, (cuuint64_t)a.X, (cuuint64_t)a.Y, (cuuint64_t)a.Z};
+  const cuuint64_t strides[3] = {(cuuint64_t)a.in_cs * 2, (cuuint64_t)a.in_cs * 2 * a.X,
+                                 (cuuint64_t)a.in_cs * 2 * a.X * a.Y};
+  const cuuint32_t box[4] = {8, (cuuint32_t)kUHX, (cuuint32_t)ny, (cuuint32_t)kUHZ};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.in, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Whether the tcgen05 form takes this layer: input and weights in the
+// supported shapes and a tensor map can be made.
+static bool tc_usable(const ConvArgs& a) {
+  return a.cin <= 48 && a.cin % 16 == 0 && (a.cout == 16 || a.cout == 32) && a.in_cs % 8 == 0 &&
+         a.in_co % 8 == 0 && a.Y >= kUY && ((uintptr_t)a.in & 15) == 0 && encode_tiled() != nullptr;
+}
+
 template <int N>
 static int launch_conv_tc(cudaStream_t s, const ConvArgs& a) {
+  CUtensorMap tm, tr;
+  if (!tc_tensor_map(&tm, a, kUHY) || !tc_tensor_map(&tr, a, 1)) return TTFLD_E_UNSUPPORTED;
   const size_t smem = conv_tc_smem_bytes(a.cin, N);
-  static bool opted = false;
+  static int opted = 0, sms = 0;
   if (!opted) {
-    if (cudaFuncSetAttribute(conv3_tc_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) !=
+    if (cudaFuncSetAttribute(conv3_tc_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024) !=
         cudaSuccess)
       return TTFLD_E_CUDA;
-    opted = true;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+    opted = 1;
   }
-  const long long blocks = (long long)((a.X + kUX - 1) / kUX) * ((a.Y + kUY - 1) / kUY) * a.Z;
-  conv3_tc_kernel<N><<<(unsigned)blocks, 128, smem, s>>>(a);
+  const long long ntiles = (long long)((a.X + kUX - 1) / kUX) * ((a.Y + kUY - 1) / kUY) * a.Z;
+  const int blocks = (int)(ntiles < sms ? ntiles : sms);
+  conv3_tc_kernel<N><<<blocks, 128, smem, s>>>(a, tm, tr, ntiles);
   count_launches(1);
   TT_CHECK_LAUNCH();
   return 0;
@@ -521,9 +682,9 @@ static int check_umma(cudaStream_t s) {
 
 static int conv_fwd(cudaStream_t s, const ConvArgs& a) {
   if (a.cin % 16 || a.cout % 16 || a.in_cs % 2 || a.in_co % 2 || a.out_cs % 2 || a.out_co % 2) return TTFLD_E_ARGS;
-  if (a.cin <= 48 && a.in_cs % 8 == 0 && a.in_co % 8 == 0 && a.out_cs % 2 == 0) {
-    if (g_conv_tc && a.cout == 16) return launch_conv_tc<16>(s, a);
-    if (g_conv_tc && a.cout == 32) return launch_conv_tc<32>(s, a);
+  if (g_conv_tc && tc_usable(a)) {
+    if (a.cout == 16) return launch_conv_tc<16>(s, a);
+    if (a.cout == 32) return launch_conv_tc<32>(s, a);
   }
   // shared-memory tiles up to 96 input channels (a 150 KB input tile; the
   // weights stay in global memory above 100 KB of tile + weights)
