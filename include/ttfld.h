@@ -78,7 +78,14 @@ enum ttfld_field {
 /* Grid sizes of the one subdomain (the reference's locNX/locNY/locNZ). */
 typedef struct {
   int32_t nx, ny, nz;
-  int32_t poles;  /* inc_poles (ipp:20); only 0 is implemented */
+  int32_t poles;  /* inc_poles (ipp:20).  1: the one-rank pole shifts
+                     (ppshift.f:2217-2453) -- planes NZ-1..NZ-3 mirrored
+                     onto NZ..NZ+2 and planes 1, 2 onto 0, -1 after every
+                     phi exchange, no theta boundary rows, the SOR stopping
+                     at NZ-1 (ppsor.f:39-43).  The exact and FP32/FP64 SOR
+                     of COUPLED_ENERGY_EQS take it; the fast FP64 SOR, PCG,
+                     SOLVE_WITH_HYPRE, RADDIF and DIFFUSION return
+                     TTFLD_E_UNSUPPORTED */
 } ttfld_dims;
 
 /* 1-D metric arrays of GITTER (ppinit.f:1028-1406), each passed with the

@@ -353,6 +353,24 @@ static void shift_halo(ttor_state* s, double* a) {
 #undef A
 }
 
+/* NORTH_POLE_SHIFT and SOUTH_POLE_SHIFT (ppshift.f:2217-2453) with one
+ * rank: the partner across each pole (myid -/+ numprocs/2, ppshift.f:
+ * 820-833) is the rank itself, so the exchanges copy planes NZ-1, NZ-2,
+ * NZ-3 onto NZ, NZ+1, NZ+2 and planes 1, 2 onto 0, -1, over the whole
+ * (i, j) extent including the ghosts; nothing without poles. */
+static void pole_shift(ttor_state* s, double* a) {
+  if (!s->poles) return;
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+#define A(i, j, k) a[(size_t)((i) + 1) + (size_t)NXH * ((size_t)((j) + 1) + (size_t)NYH * (size_t)((k) + 1))]
+  for (int m = 0; m < 3; ++m)
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) A(i, j, nz + m) = A(i, j, nz - 1 - m);
+  for (int m = 0; m < 2; ++m)
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) A(i, j, -m) = A(i, j, 1 + m);
+#undef A
+}
+
 int ttor_planetshift(ttor_state* s, const char* field) {
   size_t n;
   double* a = ttor_field(s, field, &n);
@@ -990,8 +1008,9 @@ int ttor_stellarinput_heating(ttor_state* s) {
  * (ppbou.f:1833-1846, 1946-1958), and the PLANETSHIFT calls around them. */
 int ttor_bounds(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
-  if (s->bcxmin != 9 || s->poles) return -4;
+  if (s->bcxmin != 9) return -4;
   shift_halo(s, s->T); shift_halo(s, s->RH);
+  pole_shift(s, s->T); pole_shift(s, s->RH);
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j) {
       int ub = nx + 1, found = 0;
@@ -1052,7 +1071,8 @@ int ttor_bounds(ttor_state* s) {
       }
       if (ub == nx) { H(RH, nx, j, k) = (double)1.0e-10f; H(T, nx, j, k) = tj; }
     }
-  /* BOUNDZMIN(0) / BOUNDZMAX(0) */
+  /* BOUNDZMIN(0) / BOUNDZMAX(0), without poles only (ppbou.f:188-193) */
+  if (!s->poles) {
   for (int j = -1; j <= ny + 2; ++j)
     for (int i = -1; i <= nx + 2; ++i) {
       H(RH, i, j, 1) = H(RH, i, j, 2);
@@ -1071,7 +1091,9 @@ int ttor_bounds(ttor_state* s) {
       H(T, i, j, nz + 1) = H(T, i, j, nz);
       H(T, i, j, nz + 2) = H(T, i, j, nz);
     }
+  }
   shift_halo(s, s->T); shift_halo(s, s->RH);
+  pole_shift(s, s->T); pole_shift(s, s->RH);
   return 0;
 }
 
@@ -1191,7 +1213,7 @@ static double sor_colour(ttor_state* s, double* x, const double* b, int colour, 
 
 /* The red-black iteration with the ppsor.f:161-177 stopping rule. */
 static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int itmax) {
-  const int zmax = s->nz; /* poles=.false., ppsor.f:39-43 */
+  const int zmax = s->poles ? s->nz - 1 : s->nz; /* ppsor.f:39-43 */
   double rhsnorm = 0.0;
   for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(b[c]);
   s->global_rhsnorm = rhsnorm;
@@ -1200,8 +1222,10 @@ static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int it
     ++it;
     double rnorm = sor_colour(s, x, b, 0, zmax);
     shift_halo(s, x);
+    pole_shift(s, x);
     rnorm = rnorm + sor_colour(s, x, b, 1, zmax);
     shift_halo(s, x);
+    pole_shift(s, x);
     s->global_rnorm = rnorm;
     if (it == itmax) { s->sor_iter = it; return 1; }
     if (rnorm / rhsnorm > s->epsmat || it < itmin) continue;
@@ -1213,7 +1237,6 @@ static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int it
 
 /* SOLVE_WITH_SOR ppsor.f:2-187 */
 int ttor_solve_with_sor(ttor_state* s, int fill, int use_guess) {
-  if (s->poles) return -4;
   if (fill) { ttor_fill_sor_matrix(s); ttor_b_vector_boundaries(s); }
   if (!use_guess) {
     for (size_t q = 0; q < nhalo(s); ++q) s->DELTA_ER[q] = 0.0;
@@ -1224,6 +1247,7 @@ int ttor_solve_with_sor(ttor_state* s, int fill, int use_guess) {
         for (int i = -1; i <= s->nx + 2; ++i)
           if (i < 1 || i > s->nx || j < 1 || j > s->ny || k < 1 || k > s->nz) H(DELTA_ER, i, j, k) = 0.0;
     shift_halo(s, s->DELTA_ER);
+    pole_shift(s, s->DELTA_ER);
   }
   int rc = sor_loop(s, s->DELTA_ER, s->RHS_ER, 1, s->itmax);
   s->sor_total += s->sor_iter;
@@ -1393,11 +1417,14 @@ int ttor_sor_sweeps(ttor_state* s, int nsweeps) {
   double rhsnorm = 0.0;
   for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(s->RHS_ER[c]);
   s->global_rhsnorm = rhsnorm;
+  const int zmax = s->poles ? s->nz - 1 : s->nz;
   for (int it = 0; it < nsweeps; ++it) {
-    double r = sor_colour(s, s->DELTA_ER, s->RHS_ER, 0, s->nz);
+    double r = sor_colour(s, s->DELTA_ER, s->RHS_ER, 0, zmax);
     shift_halo(s, s->DELTA_ER);
-    r = r + sor_colour(s, s->DELTA_ER, s->RHS_ER, 1, s->nz);
+    pole_shift(s, s->DELTA_ER);
+    r = r + sor_colour(s, s->DELTA_ER, s->RHS_ER, 1, zmax);
     shift_halo(s, s->DELTA_ER);
+    pole_shift(s, s->DELTA_ER);
     s->global_rnorm = r;
   }
   s->sor_iter = nsweeps;
@@ -1505,7 +1532,6 @@ int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
   const double delta_max = 0.005, conv_parm = 0.1, theta = 1.0;   /* :42, :49, :60 */
   int rc;
-  if (s->poles) return -4;
   s->status = 0;
   s->sor_total = 0; s->solves = 0;
   for (size_t q = 0; q < nhalo(s); ++q) s->DELTA_ER[q] = 0.0;     /* :52-53 */
@@ -1523,6 +1549,7 @@ int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds) {
   if ((rc = left_bc(s))) return rc;
   z_bc(s);
   shift_halo(s, s->ER);                                           /* :230-245 */
+  pole_shift(s, s->ER);
   memcpy(s->Q_OLD, s->Q, nhalo(s) * sizeof(double));             /* :248-249 */
   memcpy(s->ER_OLD, s->ER, nhalo(s) * sizeof(double));
   if ((rc = ttor_calculateflux(s))) return rc;                    /* :253-255 */
@@ -1531,6 +1558,7 @@ int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds) {
   for (;;) {
     s->energy_iter += 1;                                          /* :260 */
     shift_halo(s, s->ER);                                         /* :264-279 */
+    pole_shift(s, s->ER);
     if ((rc = ttor_calculateflux(s))) return rc;                  /* :283-285 */
     ttor_flux_bc(s);
     ttor_calculatedivf_withf(s, 0, theta);
@@ -1624,6 +1652,7 @@ int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds) {
  * halo field SCALAR; the SOR system is stored in SOR_A..G / RHS_DIF. */
 int ttor_diffusion(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
+  if (s->poles) return -4;   /* DIFFUSION's pole branches (ppdif.f:82, 125) are not restated */
   const double dconst = s->xnue / s->pr_num;
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j)

@@ -113,9 +113,12 @@ def test_hypre_solve_against_direct(small):
 
 
 def test_hypre_iteration_limit_reports_status(small):
+    """One iteration cannot reach 1e-14 however strong the preconditioner:
+    the sweep count is raised to its limit (32), and the last attempt ends at
+    the iteration limit with status 1."""
     o, f, x_ref = _hypre_case(small)
-    st = f.solve_with_hypre(tol=1e-14, maxit=3)
-    assert st.status == 1 and st.sor_iter == 3
+    st = f.solve_with_hypre(tol=1e-14, maxit=1)
+    assert st.status == 1 and st.sor_iter == 1 and st.gs_sweeps == 32
 
 
 def test_hypre_strengthens_its_preconditioner_to_meet_the_cap():

@@ -1,0 +1,135 @@
+"""GPU against the CPU oracle with inc_poles on one rank.
+
+The partner across each pole is the rank itself (ppshift.f:820-833): every
+phi exchange is followed by the pole shifts that mirror planes NZ-1..NZ-3 onto
+NZ..NZ+2 and planes 1, 2 onto 0, -1 (NORTH/SOUTH_POLE_SHIFT,
+ppshift.f:2217-2453), the theta edges are ordinary rows of the SOR system
+(ppsor.f:228-272) and SOLVE_WITH_SOR stops at NZ-1 (ppsor.f:39-43).
+
+Bars as for the shells without poles: bitwise for BOUNDS, KAPPA and the exact
+FP64 sweeps and solve; the exact step's counts identical and its fields
+within 1e-9; the FP32/FP64 solver's step within 1e-9 of the oracle converged
+to 1e-12.  The solvers that have no pole rows refuse the context.
+"""
+import numpy as np
+import pytest
+
+from conftest import fld_from_shell, oracle_from_shell, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def polar():
+    from ttcode_gb300.synthetic import make_shell
+    return make_shell(40, 64, 32, seed=11, delt=100.0, poles=True)
+
+
+def _same_system(f, o):
+    for n in ("SOR_A", "SOR_B", "SOR_C", "SOR_D", "SOR_E", "SOR_F", "SOR_G", "RHS_ER"):
+        f.upload(n, o.f(n))
+
+
+def test_poles_bounds_and_kappa_bitwise(polar):
+    o = oracle_from_shell(polar)
+    f = fld_from_shell(polar)
+    for n in ("T", "RH", "XKAPR", "XKAPP", "XKAPA"):
+        assert np.array_equal(f.download(n), o.f(n)), n
+    f.close()
+
+
+def test_poles_exact_step(polar):
+    o = oracle_from_shell(polar)
+    f = fld_from_shell(polar)
+    f.set_solver("sor64_exact")
+    assert o.call("coupled_energy_eqs", 1) == 0
+    st = f.coupled_energy_eqs(True)
+    assert st.energy_iter == int(o.get("energy_iter"))
+    assert st.sor_total == int(o.get("sor_total"))
+    for n in ("ER", "T", "DELTA_ER"):
+        assert rel_l2(f.download(n), o.f(n)) <= TOL, n
+    f.close()
+
+
+@pytest.mark.parametrize("nsweeps", [1, 4])
+def test_poles_exact_sweeps_and_solve_bitwise(polar, nsweeps):
+    o = oracle_from_shell(polar)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    f = fld_from_shell(polar)
+    _same_system(f, o)
+    f.upload("DELTA_ER", np.zeros_like(o.f("DELTA_ER")))
+    o.f("DELTA_ER")[...] = 0.0
+    f.sor_sweeps(nsweeps)
+    assert o.call("sor_sweeps", nsweeps) == 0
+    assert np.array_equal(f.download("DELTA_ER"), o.f("DELTA_ER"))
+    # the whole solve from zero: same sweep count, same bits
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("solve_with_sor", 0, 0) == 0
+    f.set_solver("sor64_exact")
+    f.begin_step(new_run=True)
+    st = f.solve_system()
+    assert st.sor_iter == int(o.get("sor_iter"))
+    assert np.array_equal(f.download("DELTA_ER"), o.f("DELTA_ER"))
+    f.close()
+
+
+def test_poles_mixed_steps(polar):
+    """Two consecutive steps of the FP32/FP64 solver, the second from the
+    previous solution, against the oracle at 1e-12."""
+    o = oracle_from_shell(polar, eps=1e-12)
+    f = fld_from_shell(polar)
+    f.set_solver("mixed", guess="previous", tol=1e-10)
+    for step in (1, 2):
+        o.set("iii", step)
+        f.set_params(iii=step)
+        assert o.call("coupled_energy_eqs", 1) == 0
+        st = f.coupled_energy_eqs(True)
+        assert st.status == 0
+        assert st.energy_iter == int(o.get("energy_iter")), step
+        for n in ("ER", "T"):
+            assert rel_l2(f.download(n), o.f(n)) <= TOL, (step, n)
+    f.close()
+
+
+@pytest.mark.parametrize("solver", ["sor64_fast", "pcg"])
+def test_poles_unsupported_solvers_refuse(polar, solver):
+    from ttcode_gb300._ffi import TTFLDError
+    f = fld_from_shell(polar)
+    f.set_solver(solver)
+    with pytest.raises(TTFLDError) as e:
+        f.coupled_energy_eqs(True)
+    assert e.value.status == -3
+    with pytest.raises(TTFLDError) as e:
+        f.solve_with_hypre()
+    assert e.value.status == -3
+    f.close()
+
+
+def test_poles_run_directory_step(tmp_path):
+    """A run directory whose ipp keeps inc_poles = 1 (the shipped value,
+    ipp:20) opens without poles_off and starts a context with the pole
+    shifts; its exact step is the oracle's."""
+    from test_ipp import _ipp
+    from ttcode_gb300 import akttd as A
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.grid import RJUP
+    from ttcode_gb300.ipp import open_run_directory
+    from ttcode_gb300.synthetic import make_shell
+    ipp = _ipp(l24=f"24 {RJUP!r} {1.1 * RJUP!r} 0.0", l25="32 0.0 1.0 0.0", l26="16 -0.95 0.95 0.0")
+    (tmp_path / "ipp").write_text("\n".join(ipp) + "\n")
+    s0 = make_shell(24, 32, 16, seed=5, delt=100.0)
+    A.write_restart(str(tmp_path / "AKTTD"), A.combine([A.snapshot_of(s0, zeit=10.0, num_iter=4)]))
+    sh, _, d, _ = open_run_directory(str(tmp_path), kappa_model=0, adjust_sor=0)
+    assert d["inc_poles"] == 1 and sh.params["poles"] == 1
+    o = oracle_from_shell(sh, eps=sh.params["epsmat"], itmax=sh.params["itmax"])
+    f = start_run(sh)
+    f.set_solver("sor64_exact")
+    assert o.call("coupled_energy_eqs", 1) == 0
+    st = f.coupled_energy_eqs(True)
+    assert st.energy_iter == int(o.get("energy_iter"))
+    assert st.sor_total == int(o.get("sor_total"))
+    for n in ("ER", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= TOL, n
+    f.close()

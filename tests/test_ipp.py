@@ -80,9 +80,9 @@ def test_null_values_and_bad_items():
 
 def test_params_and_grid():
     d = read_ipp(SHIPPED.splitlines())
-    with pytest.raises(IppError):
-        params_of_ipp(d, 100.0)                          # inc_poles = 1
+    assert params_of_ipp(d, 100.0)["poles"] == 1         # inc_poles = 1
     p = params_of_ipp(d, 250.0, poles_off=True)
+    assert p["poles"] == 0
     assert (p["delt"], p["sorparam"], p["epsmat"], p["itmax"], p["fbottom"]) == (250.0, 1.71, 1e-7, 500, 15844.23)
     assert p["adjust_sor"] == 1 and p["kappa_model"] == 2      # IRAD = 3; IKAPTYP 21: the Burrows table
     d3 = read_ipp(_ipp(l9="3 0 1.0 0.1"))

@@ -590,3 +590,52 @@ def test_raddif_uniform_state_is_a_fixed_point():
     assert int(o.get("sor_iter")) == 5
     assert o.get("global_rnorm") / o.get("global_rhsnorm") <= 1e-14
     assert np.max(np.abs(o.f("T")[2:-2, 2:-2, 2:-2] - 1500.0)) <= 1e-9
+
+
+def _mirrored(a, nz):
+    """Whether halo array a (index k+1 for k = -1..NZ+2) holds the one-rank
+    pole shifts: planes NZ-1, NZ-2, NZ-3 on NZ, NZ+1, NZ+2 and planes 1, 2 on
+    0, -1."""
+    return (np.array_equal(a[:, :, nz + 1], a[:, :, nz]) and np.array_equal(a[:, :, nz + 2], a[:, :, nz - 1])
+            and np.array_equal(a[:, :, nz + 3], a[:, :, nz - 2]) and np.array_equal(a[:, :, 1], a[:, :, 2])
+            and np.array_equal(a[:, :, 0], a[:, :, 3]))
+
+
+def test_poles_mirror_rows_and_manufactured_solution():
+    """inc_poles with one rank (the partner across each pole is the rank
+    itself, ppshift.f:820-833): BOUNDS leaves T and RH mirrored at the theta
+    edges (NORTH/SOUTH_POLE_SHIFT,
+    ppshift.f:2217-2453), the theta edges are ordinary rows of the SOR system
+    (ppsor.f:228-272), and SOLVE_WITH_SOR solves the rows k = 1..NZ-1
+    (ppsor.f:39-43): a manufactured solution of those rows, with the mirrored
+    ghosts as the closure, is recovered."""
+    from ttcode_gb300.synthetic import make_shell
+    nx, ny, nz = 16, 24, 12
+    sh = make_shell(nx, ny, nz, seed=7, delt=100.0, poles=True)
+    o = oracle_from_shell(sh, eps=1e-10)
+    assert _mirrored(o.f("T"), nz) and _mirrored(o.f("RH"), nz)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    assert np.isfinite(o.f("ER")).all()   # E_R is shifted at the next iteration's start
+    A = {n: o.f(n) for n in ("SOR_A", "SOR_B", "SOR_C", "SOR_D", "SOR_E", "SOR_F", "SOR_G")}
+    assert np.all(A["SOR_F"][:nx - 3, :, 0] != 0.0) and np.all(A["SOR_G"][:nx - 3, :, nz - 2] != 0.0)
+    # x* on k = 1..NZ-1, mirrored ghosts, zero radial ghosts; b = A x* on those rows
+    rng = np.random.default_rng(3)
+    xs = np.zeros((nx + 4, ny + 4, nz + 4))
+    xs[2:nx + 2, 2:ny + 2, 2:nz + 1] = rng.uniform(-1.0, 1.0, (nx, ny, nz - 1))
+    xs[:, 0:2, :] = xs[:, ny:ny + 2, :]
+    xs[:, ny + 2:ny + 4, :] = xs[:, 2:4, :]
+    for m in range(3):
+        xs[:, :, nz + 1 + m] = xs[:, :, nz - m]
+    xs[:, :, 1], xs[:, :, 0] = xs[:, :, 2], xs[:, :, 3]
+    c = np.s_[2:nx + 2, 2:ny + 2, 2:nz + 2]
+    sh3 = lambda di, dj, dk: xs[2 + di:nx + 2 + di, 2 + dj:ny + 2 + dj, 2 + dk:nz + 2 + dk]
+    ax = (A["SOR_A"] * xs[c] + A["SOR_B"] * sh3(-1, 0, 0) + A["SOR_C"] * sh3(1, 0, 0) + A["SOR_D"] * sh3(0, -1, 0)
+          + A["SOR_E"] * sh3(0, 1, 0) + A["SOR_F"] * sh3(0, 0, -1) + A["SOR_G"] * sh3(0, 0, 1))
+    b = ax.copy()
+    b[:, :, nz - 1] = 0.0                                  # row NZ is not solved
+    o.f("RHS_ER")[...] = b
+    o.set("epsmat", 1e-14)
+    assert o.call("solve_with_sor", 0, 0) == 0
+    x = o.f("DELTA_ER")
+    assert rel_l2(x[2:nx + 2, 2:ny + 2, 2:nz + 1], xs[2:nx + 2, 2:ny + 2, 2:nz + 1]) <= 1e-9
+    assert _mirrored(x, nz)

@@ -22,6 +22,23 @@ int halo_shift(ttfld_ctx* c, double* a) {
   return 0;
 }
 
+// NORTH_POLE_SHIFT / SOUTH_POLE_SHIFT ppshift.f:2217-2453 with one rank: the
+// partner across each pole (myid -/+ numprocs/2, ppshift.f:820-833) is the
+// rank itself, so planes NZ-1, NZ-2, NZ-3 are copied onto NZ, NZ+1, NZ+2 and
+// planes 1, 2 onto 0, -1, over the whole (i, j) extent with the ghosts.
+// Nothing without poles.
+int pole_shift(ttfld_ctx* c, double* a) {
+  Dev d = c->d;
+  if (!d.poles) return 0;
+  launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, 0, 0), [=] __device__(int i, int j, int) {
+    const int nz = d.nz;
+    for (int m = 0; m < 3; ++m) a[hidx(d, i, j, nz + m)] = a[hidx(d, i, j, nz - 1 - m)];
+    for (int m = 0; m < 2; ++m) a[hidx(d, i, j, -m)] = a[hidx(d, i, j, 1 + m)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
 // Synthetic analytic opacity in KAPPA's IKAPTYP 20:25 branch
 // (pprphy.f:321-351): evaluated for i = -1..UPPERBND, then i = UPPERBND..NX+2
 // copied from UPPERBND-1.  kappa_P = kappa_A = kappa_R, zero T-derivatives
@@ -715,6 +732,7 @@ static int bounds(ttfld_ctx* c) {
   int rc;
   if (d.bcxmin != 9) return TTFLD_E_UNSUPPORTED;
   if ((rc = halo_shift(c, d.T)) || (rc = halo_shift(c, d.RH))) return rc;
+  if ((rc = pole_shift(c, d.T)) || (rc = pole_shift(c, d.RH))) return rc;
   launch_box(c->stream, box(0, 0, 1, d.ny, 1, d.nz), [=] __device__(int, int j, int k) {
     int ub = d.nx - 1;
     for (int i = 1; i <= d.nx; ++i)
@@ -782,8 +800,8 @@ static int bounds(ttfld_ctx* c) {
     if (ub == d.nx) { HA(RH, d.nx, j, k) = (double)1.0e-10f; HA(T, d.nx, j, k) = tj; }
   });
   TT_CHECK_LAUNCH();
-  // BOUNDZMIN(0) then BOUNDZMAX(0)
-  launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, 0, 0), [=] __device__(int i, int j, int) {
+  // BOUNDZMIN(0) then BOUNDZMAX(0), without poles only (ppbou.f:188-193)
+  if (!d.poles) launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, 0, 0), [=] __device__(int i, int j, int) {
     const int nz = d.nz;
     HA(RH, i, j, 1) = HA(RH, i, j, 2); HA(RH, i, j, 0) = HA(RH, i, j, 1); HA(RH, i, j, -1) = HA(RH, i, j, 1);
     HA(T, i, j, 1) = HA(T, i, j, 2); HA(T, i, j, 0) = HA(T, i, j, 1); HA(T, i, j, -1) = HA(T, i, j, 1);
@@ -794,6 +812,7 @@ static int bounds(ttfld_ctx* c) {
   });
   TT_CHECK_LAUNCH();
   if ((rc = halo_shift(c, d.T)) || (rc = halo_shift(c, d.RH))) return rc;
+  if ((rc = pole_shift(c, d.T)) || (rc = pole_shift(c, d.RH))) return rc;
   return 0;
 }
 

@@ -173,7 +173,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   if (!out || !dims || !m || !params) return TTFLD_E_ARGS;
   *out = nullptr;
   if (dims->nx < 4 || dims->ny < 4 || dims->nz < 4) return TTFLD_E_ARGS;
-  if (dims->poles) return TTFLD_E_UNSUPPORTED;
+  if (dims->poles != 0 && dims->poles != 1) return TTFLD_E_ARGS;
   if (dims->ny % 2) return TTFLD_E_UNSUPPORTED;  // periodic red-black needs even NY
   int rc = validate_params(params);
   if (rc) return rc;
@@ -191,6 +191,7 @@ int ttfld_create(ttfld_ctx** out, const ttfld_dims* dims, const ttfld_metrics* m
   c->prev_scale = 0.9;
   Dev& d = c->d;
   d.nx = dims->nx; d.ny = dims->ny; d.nz = dims->nz;
+  d.poles = dims->poles;
   apply_params(c);
 
   const size_t H = nhalo(d), Cn = ncell(d), Fn = nface(d), Pn = nplane(d);

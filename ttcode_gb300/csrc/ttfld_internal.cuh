@@ -58,6 +58,7 @@ struct StepDev {
 // 1-D metrics are stored on (-1:N+2) and addressed with G(a, i) = a[i+1].
 struct Dev {
   int nx, ny, nz;
+  int poles;  // inc_poles: the theta edges are the self-mirrored pole shifts of one rank
   // 1-D grid metrics
   const double *xxa, *xxb, *dxa, *dxb, *xya, *xyb, *dya, *dyb, *xza, *xzb, *dza, *dzb;
   const double *ddx0, *ddx1, *ddy0, *ddy1, *ddz0, *ddz1;
@@ -303,6 +304,21 @@ int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, i
 void krylov_free(ttfld_ctx* c);
 int fill_sor_matrix(ttfld_ctx* c, bool zero_rhs = true);
 int halo_shift(ttfld_ctx* c, double* a);
+int pole_shift(ttfld_ctx* c, double* a);
+
+// The last theta row the SOR updates (zmax_sor_index, ppsor.f:39-43): with
+// poles the row NZ is the north pole's mirror of NZ-1.
+__host__ __device__ __forceinline__ int sor_zmax(const Dev& d) { return d.poles ? d.nz - 1 : d.nz; }
+// The theta neighbours of cell (i,j,k) of halo array x at q for the rows the
+// SOR updates: with poles the ghost plane 0 holds plane 1 and the plane NZ
+// holds NZ-1 (the pole shifts after every colour), which for the cell's own
+// column is the cell itself, so its current value is read in their place.
+__device__ __forceinline__ double x_km(const Dev& d, const double* x, size_t q, int k, size_t sk) {
+  return (d.poles && k == 1) ? x[q] : x[q - sk];
+}
+__device__ __forceinline__ double x_kp(const Dev& d, const double* x, size_t q, int k, size_t sk) {
+  return (d.poles && k == d.nz - 1) ? x[q] : x[q + sk];
+}
 int rhs_norm(ttfld_ctx* c, const double* b, double* out_host);
 int true_residual(ttfld_ctx* c, const double* x, const double* b, double* l1);
 int unet_guess(ttfld_ctx* c, double* x_out, double* resid_l1);
@@ -346,12 +362,13 @@ __device__ __forceinline__ bool sor_row(const Dev& d, int i, int j, int k, size_
   double b = -e8 * r.e2, cc = -e8 * r.e1, dd = -e8 * r.e4;
   double e = -e8 * r.e3, f = -e8 * r.e6, g = -e8 * r.e5;
   int ub = PA(UB, j, k);
-  bool ident = (i >= ub) || (i == d.nx) || (k == 1) || (k == d.nz);
+  // the theta edges are boundary rows only without poles (ppsor.f:228-272)
+  bool ident = (i >= ub) || (i == d.nx) || (!d.poles && (k == 1 || k == d.nz));
   if (ident) { a = 1.0; b = 0.0; cc = 0.0; dd = 0.0; e = 0.0; f = 0.0; g = 0.0; }
   if (i == ub - 1) cc = 0.0;
   if (i == d.nx - 1) cc = 0.0;
-  if (k == 2) f = 0.0;
-  if (k == d.nz - 1) g = 0.0;
+  if (!d.poles && k == 2) f = 0.0;
+  if (!d.poles && k == d.nz - 1) g = 0.0;
   d.SA[q] = a; d.SB[q] = b; d.SC[q] = cc; d.SD[q] = dd; d.SE[q] = e; d.SF[q] = f; d.SG[q] = g;
   return ident;
 }

@@ -867,6 +867,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
 }  // namespace
 
 int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
+  if (c->d.poles) return TTFLD_E_UNSUPPORTED;  // the symmetrised system assumes theta boundary rows
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
   return pcg_core(c, x, b, false, c->opts.tol, budget, false, 0, guess_test, fallback, st);
 }
@@ -886,6 +887,7 @@ extern "C" {
 int ttfld_solve_with_hypre(ttfld_ctx* c, double tol, int maxit, ttfld_solve_stats* st) {
   using namespace ttfld;
   if (!c) return TTFLD_E_ARGS;
+  if (c->d.poles) return TTFLD_E_UNSUPPORTED;  // hypre's pole graph (pphypre.f:458-540) is not built
   if (!(tol > 0.0)) tol = 1e-6;  // pphypre.f:45
   if (maxit <= 0) maxit = 50;    // pphypre.f:54-55
   TT_CHECK(cudaSetDevice(c->device));

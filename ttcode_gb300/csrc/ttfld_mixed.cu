@@ -28,6 +28,7 @@ namespace ttfld {
 
 struct Cmp {
   int nx, ny, nz, nxp;  // nxp: padded slots per colour row (multiple of 4)
+  int poles;            // theta rows 1 and NZ-1 read themselves for the mirror; row NZ is not swept
   long long rows;       // ny * nz
   size_t csz;           // slots per colour array (no ghost planes)
   size_t gsz;           // slots per colour array with theta ghost planes
@@ -36,6 +37,7 @@ struct Cmp {
 static Cmp make_cmp(const Dev& d) {
   Cmp g;
   g.nx = d.nx; g.ny = d.ny; g.nz = d.nz;
+  g.poles = d.poles;
   int nxh = (d.nx + 1) / 2;
   g.nxp = (nxh + 3) / 4 * 4;
   g.rows = (long long)d.ny * d.nz;
@@ -184,6 +186,7 @@ __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float o
   const int hv = (int)(t % nv);
   const long long rr = t / nv;
   const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
+  if (g.poles && k0 == g.nz - 1) return;  // the north pole's mirror row (zmax_sor_index, ppsor.f:39-43)
   const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
   const int h0 = hv * 4;
   const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
@@ -201,9 +204,10 @@ __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float o
   }
   const float4 s = lde4(eo + gslot(g, jm, k0, h0));
   const float4 nn = lde4(eo + gslot(g, jp, k0, h0));
-  const float4 b = lde4(eo + eb - plane);
-  const float4 tt = lde4(eo + eb + plane);
   const float4 e = lde4(es + eb);
+  // with poles the theta neighbour across either edge is the cell itself
+  const float4 b = (g.poles && k0 == 0) ? e : lde4(eo + eb - plane);
+  const float4 tt = (g.poles && k0 == g.nz - 2) ? e : lde4(eo + eb + plane);
   float4 out;
 #define UPD(L, IDX, XM, XP)                                                                \
   {                                                                                        \
@@ -539,8 +543,8 @@ __global__ void __launch_bounds__(kThreads) resid32_kernel(Dev d, Cmp g, Mix32 m
                                                            const double* __restrict__ b, double* partials) {
   __shared__ double sh[32];
   __shared__ bool last;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const long long n = (long long)nx * ny * nz;
+  const int nx = d.nx, ny = d.ny;
+  const long long n = (long long)nx * ny * sor_zmax(d);  // the rows the SOR solves
   const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
   double acc = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -555,8 +559,8 @@ __global__ void __launch_bounds__(kThreads) resid32_kernel(Dev d, Cmp g, Mix32 m
     ax = fma(d.SC[t], x[q + 1], ax);
     ax = fma(d.SD[t], x[qjm], ax);
     ax = fma(d.SE[t], x[qjp], ax);
-    ax = fma(d.SF[t], x[q - sk], ax);
-    ax = fma(d.SG[t], x[q + sk], ax);
+    ax = fma(d.SF[t], x_km(d, x, q, k, sk), ax);
+    ax = fma(d.SG[t], x_kp(d, x, q, k, sk), ax);
     double rr = b[t] - ax;
     acc += fabs(rr);
     int col = (i + j + k) & 1;
@@ -834,7 +838,7 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     if (c->host_sol->iter == it0) { status = TTFLD_MAXITER; break; }  // no progress possible
     if ((rc = add_correction(c, x))) return rc;
   }
-  if ((rc = halo_shift(c, x))) return rc;
+  if ((rc = halo_shift(c, x)) || (rc = pole_shift(c, x))) return rc;
   if (st) {
     st->sor_iter = c->host_sol->iter;
     st->corrections = corrections;
@@ -989,6 +993,7 @@ int launch_sweeps64(ttfld_ctx* c, int nsweeps, int itmin, int itmax, double eps)
 
 int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
   int rc;
+  if (c->d.poles) return TTFLD_E_UNSUPPORTED;  // its ghost folding assumes theta boundary rows
   if ((rc = ensure64(c))) return rc;
   MixWork* w = work(c);
   TT_CHECK(cudaMemsetAsync(w->m64.x[0], 0, 2 * w->g.gsz * sizeof(double), c->stream));

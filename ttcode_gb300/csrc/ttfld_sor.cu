@@ -65,9 +65,9 @@ __global__ void __launch_bounds__(kThreads) sor_exact_kernel(Dev d, double* __re
   __shared__ double sh[32];
   __shared__ bool last;
   if (solver_done(d)) return;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int nx = d.nx, ny = d.ny;
   const int nxh = (nx + 1) >> 1;
-  const long long n = (long long)nxh * ny * nz;
+  const long long n = (long long)nxh * ny * sor_zmax(d);  // rows k = 1..zmax_sor_index
   const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
   double acc = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) sor_exact_kernel(Dev d, double* __re
     size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
     double xc = x[q];
     double resid = d.SA[c] * xc + d.SB[c] * x[q - 1] + d.SC[c] * x[q + 1] + d.SD[c] * x[qjm] +
-                   d.SE[c] * x[qjp] + d.SF[c] * x[q - sk] + d.SG[c] * x[q + sk] - b[c];
+                   d.SE[c] * x[qjp] + d.SF[c] * x_km(d, x, q, k, sk) + d.SG[c] * x_kp(d, x, q, k, sk) - b[c];
     acc = acc + fabs(resid);
     x[q] = xc - omega * resid / d.SA[c];
   }
@@ -108,8 +108,8 @@ __global__ void __launch_bounds__(kThreads) resid_l1_kernel(Dev d, const double*
                                                             const double* __restrict__ b, double* partials) {
   __shared__ double sh[32];
   __shared__ bool last;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const long long n = (long long)nx * ny * nz;
+  const int nx = d.nx, ny = d.ny;
+  const long long n = (long long)nx * ny * sor_zmax(d);  // the rows the SOR solves
   const size_t sj = (size_t)(nx + 4), sk = (size_t)(nx + 4) * (ny + 4);
   double acc = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kThreads) resid_l1_kernel(Dev d, const double*
     size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
     size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
     double rr = d.SA[t] * x[q] + d.SB[t] * x[q - 1] + d.SC[t] * x[q + 1] + d.SD[t] * x[qjm] +
-                d.SE[t] * x[qjp] + d.SF[t] * x[q - sk] + d.SG[t] * x[q + sk] - b[t];
+                d.SE[t] * x[qjp] + d.SF[t] * x_km(d, x, q, k, sk) + d.SG[t] * x_kp(d, x, q, k, sk) - b[t];
     acc = acc + fabs(rr);
   }
   double s = block_sum(acc, sh);
@@ -260,7 +260,8 @@ int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax
     if (launched >= itmax + 2) return TTFLD_E_CUDA;  // the rule must have fired by ITMAX
     chunk = chunk < 128 ? chunk * 2 : 256;
   }
-  if ((rc = halo_shift(c, x))) return rc;  // PLANETSHIFT(8) after the last colour
+  // PLANETSHIFT(8) and the pole shifts after the last colour
+  if ((rc = halo_shift(c, x)) || (rc = pole_shift(c, x))) return rc;
   int status = c->host_sol->nonfinite ? TTFLD_E_NONFINITE : (c->host_sol->maxit ? TTFLD_MAXITER : TTFLD_OK);
   fill_stats(c, st, status);
   return status;
@@ -408,7 +409,7 @@ int ttfld_sor_sweeps(ttfld_ctx* c, int n, double* rnorm, double* rhsnorm) {
   if (rc) return rc;
   // itmax beyond n so the rule never stops the requested sweeps
   if ((rc = launch_exact_sweeps(c, c->d.DELTA_ER, c->d.RHS, n, n + 1, n + 2, -1.0))) return rc;
-  if ((rc = halo_shift(c, c->d.DELTA_ER))) return rc;
+  if ((rc = halo_shift(c, c->d.DELTA_ER)) || (rc = pole_shift(c, c->d.DELTA_ER))) return rc;
   TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
   TT_CHECK(cudaStreamSynchronize(c->stream));
   if (rnorm) *rnorm = c->host_sol->rnorm;
@@ -503,6 +504,7 @@ namespace ttfld {
 // SOR with ITMIN=5 and SORITMAX=500 (ppdif.f:14-15), in place on SCALAR.
 static int diffusion(ttfld_ctx* c, ttfld_solve_stats* st) {
   Dev d = c->d;
+  if (d.poles) return TTFLD_E_UNSUPPORTED;  // DIFFUSION's pole branches (ppdif.f:82, 125) are not built
   if (!(d.pr_num != 0.0)) return TTFLD_E_ARGS;
   const double dconst = d.xnue / d.pr_num;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {

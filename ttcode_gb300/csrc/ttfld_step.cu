@@ -64,6 +64,7 @@ static int left_bc(ttfld_ctx* c) {
 // theta boundaries (poles=.false.), ppenergy.f:204-227 and :706-733.
 static int z_bc(ttfld_ctx* c) {
   Dev d = c->d;
+  if (d.poles) return 0;  // the pole shifts of ER take their place
   launch_box(c->stream, box(-1, d.nx + 2, -1, d.ny + 2, 0, 0), [=] __device__(int i, int j, int) {
     const int nz = d.nz;
     HA(Q, i, j, 1) = HA(Q, i, j, 2);
@@ -224,7 +225,7 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
   // forms every face again
   if ((rc = asm_top_fluxes(c, kappa_done))) return rc;
   if ((rc = upper_bc(c)) || (rc = left_bc(c)) || (rc = z_bc(c))) return rc;
-  if ((rc = halo_shift(c, d.ER))) return rc;                            // :230-245
+  if ((rc = halo_shift(c, d.ER)) || (rc = pole_shift(c, d.ER))) return rc;   // :230-245
   TT_CHECK(cudaMemcpyAsync(d.Q_OLD, d.Q, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
   TT_CHECK(cudaMemcpyAsync(d.ER_OLD, d.ER, nhalo(d) * 8, cudaMemcpyDeviceToDevice, c->stream));
   if ((rc = asm_calculateflux(c, 0, true, true))) return rc;            // :253-255
@@ -234,7 +235,7 @@ int coupled_energy_eqs(ttfld_ctx* c, int do_bounds, ttfld_step_stats* out) {
   double solve_ms = 0.0;
   for (;;) {
     ++energy_iter;                                                      // :260
-    if ((rc = halo_shift(c, d.ER))) return rc;                          // :264-279
+    if ((rc = halo_shift(c, d.ER)) || (rc = pole_shift(c, d.ER))) return rc; // :264-279
     // :283-285.  In the first iteration the fluxes are those of :253-255
     // already in FLUX_X/Y/Z: E_R, T and rho are unchanged since, the halo
     // shift just done repeats the one of :230-245, and FLIM at energy_iter

@@ -57,7 +57,7 @@ class FLD:
         self.grid = grid
         self.nx, self.ny, self.nz = grid.nx, grid.ny, grid.nz
         self.params = dict(params)
-        dims = _ffi.Dims(self.nx, self.ny, self.nz, 0)
+        dims = _ffi.Dims(self.nx, self.ny, self.nz, int(self.params.get("poles", 0)))
         self._metric_keep = {}
         m = _ffi.Metrics()
         for n in _ffi.METRIC_NAMES:

@@ -125,18 +125,17 @@ def params_of_ipp(ipp: dict, delt: float, poles_off: bool = False, **overrides) 
     of ``set_burrows_table``; 4-5 and 9-12, 14: prescribed, the arrays of
     ``opacity.freedman_kappa`` / ``opacity.burrows_kappa`` uploaded before
     each step; any other IKAPTYP needs ``kappa_model`` among the
-    overrides).  DELT is the run's (the restart file's) time step.  The
-    library has no poles: inc_poles >= 1 is refused unless ``poles_off``."""
+    overrides).  DELT is the run's (the restart file's) time step.
+    inc_poles >= 1 gives ``poles`` = 1 (the one-rank pole shifts; the IRAD=3
+    step with the exact or FP32/FP64 SOR), unless ``poles_off``."""
     _need(ipp, "sorparam", "epsmat", "itmax", "fbot", "tirr", "xnue", "pr_num", "ibdrad", "iflimtyp",
           "f_incident", "bcxmin", "ieta", "isigtyp", "ikaptyp", "irad")
     misc_checks(ipp)
-    if ipp["poles"] and not poles_off:
-        raise IppError("inc_poles >= 1: the library implements poles = .false. only (pass poles_off=True "
-                       "to run without them)")
     p = dict(delt=float(delt), sorparam=ipp["sorparam"], epsmat=ipp["epsmat"], fbottom=ipp["fbot"],
              tirr=ipp["tirr"], xnue=ipp["xnue"], pr_num=ipp["pr_num"], kap0=1.0e-2, itmax=ipp["itmax"],
              bcxmin=ipp["bcxmin"], ibdrad=ipp["ibdrad"], iflimtyp=ipp["iflimtyp"], f_incident=ipp["f_incident"],
-             ieta=ipp["ieta"], isigtyp=ipp["isigtyp"], iii=1, adjust_sor=int(ipp["irad"] == 3))
+             ieta=ipp["ieta"], isigtyp=ipp["isigtyp"], iii=1, adjust_sor=int(ipp["irad"] == 3),
+             poles=int(bool(ipp["poles"]) and not poles_off))
     if 20 <= ipp["ikaptyp"] <= 25:
         p["kappa_model"] = 2
     elif ipp["ikaptyp"] in (4, 5, 9, 10, 11, 12, 14):

@@ -48,7 +48,7 @@ def default_params(delt: float = 100.0) -> dict:
     return dict(delt=delt, sorparam=1.7, epsmat=1e-10, fbottom=15844.23, tirr=2048.0,
                 xnue=1.0e9, pr_num=1.0, kap0=1.0e-2, itmax=200000, bcxmin=9, ibdrad=9,
                 iflimtyp=2, f_incident=2, ieta=4, isigtyp=0, iii=1, adjust_sor=0,
-                kappa_model=0)
+                kappa_model=0, poles=0)
 
 
 @dataclass
@@ -86,7 +86,7 @@ def mu_star_tincident(g: Grid, tirr: float, f_incident: int = 2):
 
 
 def make_shell(nx: int, ny: int, nz: int, seed: int = 0, delt: float = 100.0,
-               contrast: float | None = None, noise: float = 0.05) -> Shell:
+               contrast: float | None = None, noise: float = 0.05, poles: bool = False) -> Shell:
     r0 = 1.0 * RJUP
     r1 = 1.1 * RJUP
     g = gitter(nx, ny, nz, r0, r1)
@@ -114,6 +114,7 @@ def make_shell(nx: int, ny: int, nz: int, seed: int = 0, delt: float = 100.0,
         KMUL = KMUL * np.exp(-s * frac)[:, None, None]
     KMUL = np.asfortranarray(KMUL)
     params = default_params(delt)
+    params["poles"] = int(poles)
     mu, tinc = mu_star_tincident(g, params["tirr"], params["f_incident"])
     fields = dict(T=T, RH=RH, CV=CV, ER=ER, KMUL=KMUL, MU_STAR=mu, TINCIDENT=tinc)
     return Shell(g, fields, params, seed)
