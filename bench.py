@@ -274,6 +274,41 @@ def run_profile_step(args):
     f.close()
 
 
+def run_profile_conv(args):
+    """For the convolution summaries under profiles/: the learned guess's
+    network (seeded random weights) on the shell256 shell's half-resolution
+    grid; after one inference with each form outside the profiled range,
+    one inference with the mma.sync convolutions and one with the tcgen05
+    ones inside cudaProfilerStart/Stop."""
+    import torch
+    from ttcode_gb300 import guess
+    from ttcode_gb300._ffi import check
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import shell
+    torch.cuda.set_device(0)
+    sh = shell(SHELL, seed=1)
+    f = start_run(sh)
+    guess.init(f, seed=5)
+    n = sh.dims[0] * sh.dims[1] * sh.dims[2]
+    feat = np.random.default_rng(1).uniform(-1.0, 1.0, (n, 5)).astype(np.float32)
+    pred = np.zeros(n, dtype=np.float32)
+
+    def infer(form):
+        check("ttfld_guess_set_conv", f.L.ttfld_guess_set_conv(form))
+        check("ttfld_guess_predict", f.L.ttfld_guess_predict(f.h, feat.ctypes.data, pred.ctypes.data))
+        return pred.copy()
+
+    infer(0), infer(1)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    p0, p1 = infer(0), infer(1)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    check("ttfld_guess_set_conv", f.L.ttfld_guess_set_conv(0))
+    print(json.dumps({"pred_rel_diff": float(np.linalg.norm(p1 - p0) / np.linalg.norm(p0))}), flush=True)
+    f.close()
+
+
 def run_profile_sweeps(args):
     """For the ncu capture of the dominant kernel: the shell256 system (or a
     shell of --profile-dims NX,NY,NZ, e.g. 160,256,128 for a working set
@@ -684,6 +719,8 @@ def main():
     ap.add_argument("--profile-dims", default="", help="NX,NY,NZ of the --profile-sweeps shell (default shell256)")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run three implicit steps, the third inside cudaProfilerStart/Stop")
+    ap.add_argument("--profile-conv", action="store_true",
+                    help="only run one inference of the guess network with each convolution form")
     ap.add_argument("--profile-pcg", action="store_true",
                     help="only build the system and run one PCG and one SOLVE_WITH_HYPRE solve")
     args = ap.parse_args()
@@ -698,6 +735,9 @@ def main():
         return
     if args.profile_pcg:
         run_profile_pcg(args)
+        return
+    if args.profile_conv:
+        run_profile_conv(args)
         return
     if args.warmup < 3:
         args.warmup = 3

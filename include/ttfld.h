@@ -494,9 +494,9 @@ int ttfld_guess_save(ttfld_ctx* ctx, void* blob, size_t bytes, size_t* needed);
  * GPU work overlaps race and must be serialised by the caller.  The first
  * call on a device (in each CUDA context: a caller's own context on the
  * device counts as a new one) looks up the array's device address in that
- * context; make that first call before any stream capture.  Every call
- * returns only after its solve has finished on the GPU: it waits on
- * `stream` to read the stopping flag between chunks of sweeps.  NY must be
+ * context.  Every call returns only after its solve has finished on the
+ * GPU (it blocks the calling host thread): it waits on `stream` to read
+ * the stopping flag between chunks of sweeps.  NY must be
  * even. */
 int ttfld_sor_solve_noalloc(const double* sor_a, const double* sor_b, const double* sor_c,
                             const double* sor_d, const double* sor_e, const double* sor_f,

@@ -176,8 +176,11 @@ __device__ __forceinline__ float4 ldc4(const float* p) { return *reinterpret_cas
 // order), i.e. the reference's RNORM (ppsor.f:73) of the iterate x + e.
 // Item t is the t-th group of four colour slots (row-major over (k, j, h));
 // its coefficients (aw..at: the W E S N B T couplings over A, r: rhat, dg:
-// A) come in as arguments, from global or from shared memory.
-template <int COL, bool NORM>
+// A) come in as arguments, from global or from shared memory.  POLES (a
+// compile-time copy of Cmp::poles, so that the kernels without poles carry
+// no test of it): theta rows 1 and NZ-1 take the cell itself as their
+// neighbour across the edge, and row NZ is not swept.
+template <int COL, bool NORM, bool POLES>
 __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
                                            size_t plane, float4 aw, float4 ae, float4 as, float4 an, float4 ab,
                                            float4 at, float4 r, float4 dg, float& nacc) {
@@ -186,7 +189,7 @@ __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float o
   const int hv = (int)(t % nv);
   const long long rr = t / nv;
   const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
-  if (g.poles && k0 == g.nz - 1) return;  // the north pole's mirror row (zmax_sor_index, ppsor.f:39-43)
+  if (POLES && k0 == g.nz - 1) return;  // the north pole's mirror row (zmax_sor_index, ppsor.f:39-43)
   const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
   const int h0 = hv * 4;
   const int ncol = (g.nx - off + 1) >> 1;  // valid slots in this row
@@ -206,8 +209,8 @@ __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float o
   const float4 nn = lde4(eo + gslot(g, jp, k0, h0));
   const float4 e = lde4(es + eb);
   // with poles the theta neighbour across either edge is the cell itself
-  const float4 b = (g.poles && k0 == 0) ? e : lde4(eo + eb - plane);
-  const float4 tt = (g.poles && k0 == g.nz - 2) ? e : lde4(eo + eb + plane);
+  const float4 b = (POLES && k0 == 0) ? e : lde4(eo + eb - plane);
+  const float4 tt = (POLES && k0 == g.nz - 2) ? e : lde4(eo + eb + plane);
   float4 out;
 #define UPD(L, IDX, XM, XP)                                                                \
   {                                                                                        \
@@ -225,7 +228,7 @@ __device__ __forceinline__ void update_vec(const Cmp& g, const Mix32& m, float o
 
 // The same with the coefficients loaded from global memory (item t's four
 // slots are floats 4t .. 4t+3 of each coefficient array).
-template <int COL, bool NORM>
+template <int COL, bool NORM, bool POLES>
 __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float omega, long long t, int nv,
                                           size_t plane, float& nacc) {
   const size_t cb = (size_t)t * 4;
@@ -235,13 +238,13 @@ __device__ __forceinline__ void sweep_vec(const Cmp& g, const Mix32& m, float om
   const float4 r = ldc4(m.rhat[COL] + cb);
   float4 dg = make_float4(0.f, 0.f, 0.f, 0.f);
   if (NORM) dg = ldc4(m.diag[COL] + cb);
-  update_vec<COL, NORM>(g, m, omega, t, nv, plane, aw, ae, as, an, ab, at, r, dg, nacc);
+  update_vec<COL, NORM, POLES>(g, m, omega, t, nv, plane, aw, ae, as, an, ab, at, r, dg, nacc);
 }
 
 // One colour per launch.  NORM launches of the second colour end with the
 // last block applying the stop rule: once RNORM / RHSNORM <= stop_ratio the
 // inner loop is done, and sweeps queued after that return at once.
-template <int COL, bool NORM>
+template <int COL, bool NORM, bool POLES>
 __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float omega, SolverDev* sol,
                                                            double* partials, double stop_ratio) {
   __shared__ double sh[32];
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
   const size_t plane = (size_t)g.ny * g.nxp;
   float nacc = 0.f;  // per-thread partial (a few cells): FP32, widened once below
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    sweep_vec<COL, NORM>(g, m, omega, t, nv, plane, nacc);
+    sweep_vec<COL, NORM, POLES>(g, m, omega, t, nv, plane, nacc);
   if (COL == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&sol->iter, 1);
   if (NORM) {
     double sb = block_sum((double)nacc, sh);
@@ -298,6 +301,7 @@ constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
 // barrier every block adds all partials in the same fixed order, so all of
 // them reach the same stop decision and leave the loop together.  Every
 // thread keeps the same items from sweep to sweep.
+template <bool POLES>
 __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mix32 m, float omega, SolverDev* sol,
                                                                       double* partials, double stop_ratio,
                                                                       int nsweeps, int norm_every, int stall_check) {
@@ -313,11 +317,11 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
   for (int sw = 1; sw <= nsweeps; ++sw) {
     const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
     float nacc = 0.f;
-    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<0, true>(g, m, omega, t, nv, plane, nacc); }
-    else { for (long long t = t0; t < n; t += ts) sweep_vec<0, false>(g, m, omega, t, nv, plane, nacc); }
+    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = t0; t < n; t += ts) sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); }
     if (!grid_sync(sol, nb)) return;
-    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<1, true>(g, m, omega, t, nv, plane, nacc); }
-    else { for (long long t = t0; t < n; t += ts) sweep_vec<1, false>(g, m, omega, t, nv, plane, nacc); }
+    if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = t0; t < n; t += ts) sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); }
     if (norm) {
       const double sb = block_sum((double)nacc, sh);
       if (threadIdx.x == 0) partials[blockIdx.x] = sb;
@@ -428,6 +432,7 @@ __device__ __forceinline__ void issue_chunk(const Mix32& m, const TmaPlan& pl, l
     bulk_to_smem(base + (size_t)q * kTmaThreads * 16, src[q] + ta * 4, bytes, bars + st);
 }
 
+template <bool POLES>
 __global__ void __launch_bounds__(kTmaThreads) sweeps32_tma(Cmp g, Mix32 m, float omega, SolverDev* sol,
                                                             double* partials, double stop_ratio, int nsweeps,
                                                             int norm_every, int stall_check) {
@@ -472,8 +477,8 @@ __global__ void __launch_bounds__(kTmaThreads) sweeps32_tma(Cmp g, Mix32 m, floa
           const float4 dg = norm ? sb[7 * kTmaThreads] : make_float4(0.f, 0.f, 0.f, 0.f);
 #define UPD_ARGS g, m, omega, t, nv, plane, sb[0], sb[kTmaThreads], sb[2 * kTmaThreads], sb[3 * kTmaThreads], \
                  sb[4 * kTmaThreads], sb[5 * kTmaThreads], sb[6 * kTmaThreads], dg, nacc
-          if (col == 0) { if (norm) update_vec<0, true>(UPD_ARGS); else update_vec<0, false>(UPD_ARGS); }
-          else { if (norm) update_vec<1, true>(UPD_ARGS); else update_vec<1, false>(UPD_ARGS); }
+          if (col == 0) { if (norm) update_vec<0, true, POLES>(UPD_ARGS); else update_vec<0, false, POLES>(UPD_ARGS); }
+          else { if (norm) update_vec<1, true, POLES>(UPD_ARGS); else update_vec<1, false, POLES>(UPD_ARGS); }
 #undef UPD_ARGS
         }
         ++done_chunks;
@@ -654,13 +659,14 @@ static int persistent_grid(K kernel, int threads, size_t smem, long long items) 
 enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2 };
 
 // Blocks of the two persistent kernels for nvec items (0: not available),
-// sized once per grid size.
+// sized once per grid size and pole form.
+template <bool POLES>
 static void sweep_grids(long long nvec, int* pers, int* tma) {
   static int tma_blocks = -1, pers_blocks = -1;
   static long long sized_for = -1;
   if (sized_for != nvec) {
-    tma_blocks = persistent_grid(sweeps32_tma, kTmaThreads, kTmaSmem, nvec);
-    pers_blocks = persistent_grid(sweeps32_persistent, kPersistThreads, 0, nvec);
+    tma_blocks = persistent_grid(sweeps32_tma<POLES>, kTmaThreads, kTmaSmem, nvec);
+    pers_blocks = persistent_grid(sweeps32_persistent<POLES>, kPersistThreads, 0, nvec);
     sized_for = nvec;
   }
   if (pers) *pers = pers_blocks;
@@ -674,8 +680,9 @@ static void sweep_grids(long long nvec, int* pers, int* tma) {
 // is unavailable.  The TMA-staged persistent kernel is kept for comparison:
 // it is slower on this workload (the per-chunk block barriers and cache
 // latencies of e outweigh the staged coefficient traffic).
-int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0,
-                    SweepForm form = kFormPersistent, bool stall_check = true) {
+template <bool POLES>
+static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, double stop_ratio, SweepForm form,
+                                bool stall_check) {
   MixWork* w = work(c);
   Cmp g = w->g;
   Mix32 m = w->m32;
@@ -686,33 +693,39 @@ int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_r
   int stall = stall_check ? 1 : 0;
   void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall};
   int pers_blocks = 0, tma_blocks = 0;
-  sweep_grids(nvec, &pers_blocks, &tma_blocks);
+  sweep_grids<POLES>(nvec, &pers_blocks, &tma_blocks);
   if (form == kFormTma && tma_blocks > 0) {
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma, dim3(tma_blocks), dim3(kTmaThreads), args,
-                                         kTmaSmem, c->stream));
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma<POLES>, dim3(tma_blocks), dim3(kTmaThreads),
+                                         args, kTmaSmem, c->stream));
     count_launches(1);
     return 0;
   }
   if (form != kFormSplit && pers_blocks > 0) {
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent, dim3(pers_blocks), dim3(kPersistThreads),
-                                         args, 0, c->stream));
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent<POLES>, dim3(pers_blocks),
+                                         dim3(kPersistThreads), args, 0, c->stream));
     count_launches(1);
     return 0;
   }
-  int nb = wave_grid(sweep32_kernel<1, true>, nvec);
+  int nb = wave_grid(sweep32_kernel<1, true, POLES>, nvec);
   for (int s = 1; s <= nsweeps; ++s) {
     bool norm = norm_every > 0 && (s % norm_every == 0 || s == nsweeps);
     if (norm) {
-      sweep32_kernel<0, true><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
-      sweep32_kernel<1, true><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<0, true, POLES><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, true, POLES><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
     } else {
-      sweep32_kernel<0, false><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
-      sweep32_kernel<1, false><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<0, false, POLES><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
+      sweep32_kernel<1, false, POLES><<<nb, kThreads, 0, c->stream>>>(g, m, omega, c->sol, c->partials, stop_ratio);
     }
   }
   count_launches(2 * nsweeps);
   TT_CHECK_LAUNCH();
   return 0;
+}
+
+int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0,
+                    SweepForm form = kFormPersistent, bool stall_check = true) {
+  return work(c)->g.poles ? launch_sweeps32_form<true>(c, nsweeps, norm_every, stop_ratio, form, stall_check)
+                          : launch_sweeps32_form<false>(c, nsweeps, norm_every, stop_ratio, form, stall_check);
 }
 
 static int poll(ttfld_ctx* c) {
@@ -756,7 +769,8 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   const SweepForm form =
       c->opts.sweep_form == 1 ? kFormTma : (c->opts.sweep_form == 2 ? kFormSplit : kFormPersistent);
   int pers_blocks = 0, tma_blocks = 0;
-  sweep_grids(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
+  if (g.poles) sweep_grids<true>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
+  else sweep_grids<false>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
   // one launch per anchor needs a persistent kernel (it stops itself)
   const bool one_launch = (form == kFormPersistent && pers_blocks > 0) || (form == kFormTma && tma_blocks > 0);
   if (guess_test) {

@@ -24,8 +24,7 @@
 //    device) race on it and must be serialised by the caller.
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (host code must not use the symbol's name as a
-//    device pointer); make that first call before any stream capture.  The
-//    address belongs to the CUDA context the module was loaded in, so it is
+//    device pointer).  The address belongs to the CUDA context the module was loaded in, so it is
 //    cached per context, keyed by the context's process-unique id
 //    (cuCtxGetId): after cudaDeviceReset, or in a context the caller made
 //    itself with the driver API, the first call there looks it up again.

@@ -651,8 +651,15 @@ static int launch_conv_tc(cudaStream_t s, const ConvArgs& a) {
     if (sms <= 0) sms = 152;
     opted = 1;
   }
+  // as many persistent CTAs as fit on an SM (shared memory bounds it): while
+  // one CTA's epilogue reads its accumulators and stores, another's MMAs run
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3_tc_kernel<N>, 128, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
   const long long ntiles = (long long)((a.X + kUX - 1) / kUX) * ((a.Y + kUY - 1) / kUY) * a.Z;
-  const int blocks = (int)(ntiles < sms ? ntiles : sms);
+  const long long slots = (long long)sms * per_sm;
+  const int blocks = (int)(ntiles < slots ? ntiles : slots);
   conv3_tc_kernel<N><<<blocks, 128, smem, s>>>(a, tm, tr, ntiles);
   count_launches(1);
   TT_CHECK_LAUNCH();
