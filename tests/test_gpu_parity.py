@@ -230,14 +230,17 @@ def test_mixed_solver_multi_chunk_grid(form):
     assert abs(st.sor_iter - st64.sor_iter) <= max(16, st64.sor_iter // 20), (st.sor_iter, st64.sor_iter)
 
 
-def test_golden_fixture_on_the_gpu():
-    """The GPU step (exact FP64 solver) on the shell of the committed oracle
-    fixture (tests/golden/make_golden.py): the same sweep and outer-iteration
+@pytest.mark.parametrize("name", ["shell_step", "poles_step"])
+def test_golden_fixture_on_the_gpu(name):
+    """The GPU step (exact FP64 solver) on the shell of a committed oracle
+    fixture (tests/golden/make_golden.py; with the theta boundary rows and
+    with the one-rank pole shifts): the same sweep and outer-iteration
     counts, E_R and T within the parity tolerance."""
     import os
     from ttcode_gb300.synthetic import make_shell
-    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shell_step.npz"))
-    sh = make_shell(int(z["nx"]), int(z["ny"]), int(z["nz"]), seed=int(z["seed"]), delt=float(z["delt"]))
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    sh = make_shell(int(z["nx"]), int(z["ny"]), int(z["nz"]), seed=int(z["seed"]), delt=float(z["delt"]),
+                    poles="poles" in z.files)
     f = fld_from_shell(sh, eps=float(z["eps"]))
     f.set_solver("sor64_exact")
     st = f.coupled_energy_eqs(True)

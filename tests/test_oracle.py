@@ -254,13 +254,15 @@ def test_mustar_tincident_match_oracle(shell):
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "shell_step.npz")), reason="no golden fixture")
-def test_golden_step_fixture():
-    """The committed fixture (made by tests/golden/make_golden.py) reproduces:
+@pytest.mark.parametrize("name", ["shell_step", "poles_step"])
+def test_golden_step_fixture(name):
+    """The committed fixtures (made by tests/golden/make_golden.py, with the
+    theta boundary rows and with the one-rank pole shifts) reproduce:
     inputs -> one COUPLED_ENERGY_EQS step -> E_R, T and the counts."""
-    z = np.load(os.path.join(GOLDEN, "shell_step.npz"))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
     from ttcode_gb300.synthetic import make_shell
-    sh = make_shell(int(z["nx"]), int(z["ny"]), int(z["nz"]), seed=int(z["seed"]), delt=float(z["delt"]))
+    sh = make_shell(int(z["nx"]), int(z["ny"]), int(z["nz"]), seed=int(z["seed"]), delt=float(z["delt"]),
+                    poles="poles" in z.files)
     o = oracle_from_shell(sh, eps=float(z["eps"]))
     assert o.call("coupled_energy_eqs", 1) == 0
     assert int(o.get("sor_total")) == int(z["sor_total"])
