@@ -55,9 +55,13 @@ WORKLOAD = ("shell256: 100x256x128 (r x phi x theta) synthetic spherical shell, 
             "iteration, solved to ||b-Ax||_1/||b||_1 <= 1e-10")
 TRAIN_PAIRS, TRAIN_EPOCHS, TRAIN_LR = 16, 20, 5e-4
 # Algorithmic bytes per cell update of one sweep (both colours):
-#   FP32 scaled sweep: 6 coefficients + rhat + e read + e write  = 9 x 4 B
+#   FP32 scaled sweep: 6 coefficients + rhat + e read + e write, and the
+#                      other colour's e (each of its values read once per
+#                      half-sweep)                               = 10 x 4 B
 #   FP64 exact sweep : 7 coefficients + b + x read + x write      = 10 x 8 B
-BYTES_FP32_SWEEP = 36
+# (at 160x512x256, beyond L2, ncu measures 40.5 B of DRAM traffic per FP32
+# cell update)
+BYTES_FP32_SWEEP = 40
 BYTES_FP64_SWEEP = 80
 
 
@@ -304,7 +308,7 @@ def run_profile_conv(args):
     p0, p1 = infer(0), infer(1)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStop()
-    check("ttfld_guess_set_conv", f.L.ttfld_guess_set_conv(0))
+    check("ttfld_guess_set_conv", f.L.ttfld_guess_set_conv(2))   # the default form
     print(json.dumps({"pred_rel_diff": float(np.linalg.norm(p1 - p0) / np.linalg.norm(p0))}), flush=True)
     f.close()
 

@@ -83,9 +83,10 @@ typedef struct {
                      onto NZ..NZ+2 and planes 1, 2 onto 0, -1 after every
                      phi exchange, no theta boundary rows, the SOR stopping
                      at NZ-1 (ppsor.f:39-43).  The exact and FP32/FP64 SOR
-                     of COUPLED_ENERGY_EQS take it; the fast FP64 SOR, PCG,
-                     SOLVE_WITH_HYPRE, RADDIF and DIFFUSION return
-                     TTFLD_E_UNSUPPORTED */
+                     of COUPLED_ENERGY_EQS take it, and DIFFUSION (every
+                     theta row, the scalar pole-shifted after each colour,
+                     ppdif.f:45-135); the fast FP64 SOR, PCG,
+                     SOLVE_WITH_HYPRE and RADDIF return TTFLD_E_UNSUPPORTED */
 } ttfld_dims;
 
 /* 1-D metric arrays of GITTER (ppinit.f:1028-1406), each passed with the
@@ -463,8 +464,10 @@ int ttfld_guess_gradients(ttfld_ctx* ctx, const float* feat, const float* target
 int ttfld_guess_predict(ttfld_ctx* ctx, const float* feat, float* pred);
 size_t ttfld_guess_num_params(void);
 /* Kernel form of the network's large-level convolutions, for the process:
- * 0 (default) mma.sync on shared-memory tiles, 1 tcgen05 (5th-generation
- * tensor cores, accumulators in tensor memory).  Same results up to FP32
+ * 0 mma.sync on shared-memory tiles everywhere, 1 tcgen05 (5th-generation
+ * tensor cores, accumulators in tensor memory, operands by TMA) on every
+ * layer it takes, 2 (default) tcgen05 on the layers with 16 output channels,
+ * where it is the faster form, mma.sync elsewhere.  Same results up to FP32
  * summation order. */
 int ttfld_guess_set_conv(int use_tcgen05);
 /* Weights blob: "TTFLDNN2", uint64 parameter count, FP32 parameters. */

@@ -371,11 +371,14 @@ static void pole_shift(ttor_state* s, double* a) {
 #undef A
 }
 
+/* PLANETSHIFT followed by the pole shifts, as every caller in the
+ * reference pairs them when poles are on (e.g. ppenergy.f:230-245). */
 int ttor_planetshift(ttor_state* s, const char* field) {
   size_t n;
   double* a = ttor_field(s, field, &n);
   if (!a || n != nhalo(s)) return -1;
   shift_halo(s, a);
+  pole_shift(s, a);
   return 0;
 }
 
@@ -1211,9 +1214,9 @@ static double sor_colour(ttor_state* s, double* x, const double* b, int colour, 
   return sor_colour_k(s, x, b, colour, 1, zmax);
 }
 
-/* The red-black iteration with the ppsor.f:161-177 stopping rule. */
-static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int itmax) {
-  const int zmax = s->poles ? s->nz - 1 : s->nz; /* ppsor.f:39-43 */
+/* The red-black iteration with the ppsor.f:161-177 stopping rule over the
+ * rows k = 1..zmax, the halo and pole shifts after each colour. */
+static int sor_loop_rows(ttor_state* s, double* x, const double* b, int itmin, int itmax, int zmax) {
   double rhsnorm = 0.0;
   for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + fabs(b[c]);
   s->global_rhsnorm = rhsnorm;
@@ -1233,6 +1236,12 @@ static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int it
   }
   s->sor_iter = it;
   return 0;
+}
+
+/* SOLVE_WITH_SOR's loop: with poles the rows stop at zmax_sor_index = NZ-1
+ * (ppsor.f:39-43). */
+static int sor_loop(ttor_state* s, double* x, const double* b, int itmin, int itmax) {
+  return sor_loop_rows(s, x, b, itmin, itmax, s->poles ? s->nz - 1 : s->nz);
 }
 
 /* SOLVE_WITH_SOR ppsor.f:2-187 */
@@ -1652,7 +1661,6 @@ int ttor_coupled_energy_eqs(ttor_state* s, int do_bounds) {
  * halo field SCALAR; the SOR system is stored in SOR_A..G / RHS_DIF. */
 int ttor_diffusion(ttor_state* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
-  if (s->poles) return -4;   /* DIFFUSION's pole branches (ppdif.f:82, 125) are not restated */
   const double dconst = s->xnue / s->pr_num;
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j)
@@ -1682,7 +1690,9 @@ int ttor_diffusion(ttor_state* s) {
           C(SOR_F, i, j, k) = 0.0; C(SOR_G, i, j, k) = 0.0;
         }
       }
-  int rc = sor_loop(s, s->SCALAR, s->RHS_DIF, 5, 500);
+  /* every theta row (ppdif.f:45-46, 93-94), with the pole shifts of the
+   * scalar after each colour when poles are on (ppdif.f:80-89, 123-132) */
+  int rc = sor_loop_rows(s, s->SCALAR, s->RHS_DIF, 5, 500, nz);
   return rc;
 }
 

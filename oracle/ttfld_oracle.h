@@ -52,7 +52,7 @@ double ttor_get(ttor_state* s, const char* name);
 /* Reference subroutines (return 0 on success, <0 on error). */
 int ttor_gitter(ttor_state* s);               /* GITTER ncosys=2, linear   */
 int ttor_calcmustar(ttor_state* s);           /* CALCMUSTAR + CALC_TINCIDENT */
-int ttor_planetshift(ttor_state* s, const char* field); /* one-rank halo  */
+int ttor_planetshift(ttor_state* s, const char* field); /* one-rank halo (+ pole shifts) */
 int ttor_bounds(ttor_state* s);               /* BOUNDS (T, RH, UPPERBND)  */
 int ttor_kappa(ttor_state* s);                /* synthetic analytic KAPPA  */
 int ttor_qdens(ttor_state* s);

@@ -93,6 +93,28 @@ def test_poles_mixed_steps(polar):
     f.close()
 
 
+def test_poles_diffusion_bitwise(polar):
+    """DIFFUSION with poles: every theta row swept, the scalar pole-shifted
+    after each colour (ppdif.f:45-135); as in the reference the overwritten
+    row NZ keeps the residual above EPSMAT and the loop runs to SORITMAX.
+    The same count and the same scalar, bit for bit."""
+    o = oracle_from_shell(polar)
+    f = fld_from_shell(polar)
+    nx, ny, nz = polar.dims
+    rng = np.random.default_rng(7)
+    o.f("SCALAR")[...] = 1.0 + rng.random((nx + 4, ny + 4, nz + 4))
+    assert o.call("planetshift", "SCALAR") == 0      # callers pass an exchanged halo
+    o.set("pr_num", 1.0)
+    o.set("xnue", 1.0e15)
+    f.set_params(pr_num=1.0, xnue=1.0e15)
+    f.upload("SCALAR", o.f("SCALAR").copy())
+    rc = o.call("diffusion")
+    st = f.diffusion()
+    assert st.status == rc and st.sor_iter == int(o.get("sor_iter"))
+    assert np.array_equal(f.download("SCALAR"), o.f("SCALAR"))
+    f.close()
+
+
 @pytest.mark.parametrize("solver", ["sor64_fast", "pcg"])
 def test_poles_unsupported_solvers_refuse(polar, solver):
     from ttcode_gb300._ffi import TTFLDError

@@ -177,9 +177,10 @@ def test_trained_guess_saves_sweeps():
 
 
 def test_tcgen05_and_mma_sync_convolutions_agree():
-    """The two kernel forms of the large-level convolutions (tcgen05 with
-    tensor-memory accumulators, and mma.sync on shared-memory tiles) give the
-    same prediction on a grid of several tiles in every direction."""
+    """The kernel forms of the large-level convolutions (tcgen05 with
+    tensor-memory accumulators on every layer it takes, mma.sync on
+    shared-memory tiles everywhere, and the default mix) give the same
+    prediction on a grid of several tiles in every direction."""
     from ttcode_gb300 import guess
     from ttcode_gb300.fld import FLD
     from ttcode_gb300.grid import gitter
@@ -191,14 +192,16 @@ def test_tcgen05_and_mma_sync_convolutions_agree():
     feat = rng.uniform(-1, 1, (X * Y * Z, 5)).astype(np.float32)
     preds = []
     try:
-        for form in (1, 0):
+        assert f.L.ttfld_guess_set_conv(3) == -1          # TTFLD_E_ARGS
+        for form in (1, 0, 2):
             assert f.L.ttfld_guess_set_conv(form) == 0
             p = np.zeros(X * Y * Z, dtype=np.float32)
             assert f.L.ttfld_guess_predict(f.h, feat.ctypes.data, p.ctypes.data) == 0
             preds.append(p)
     finally:
-        f.L.ttfld_guess_set_conv(0)
-    assert np.linalg.norm(preds[0] - preds[1]) <= 1e-3 * np.linalg.norm(preds[1])
+        f.L.ttfld_guess_set_conv(2)   # the default form
+    for p in (preds[0], preds[2]):
+        assert np.linalg.norm(p - preds[1]) <= 1e-3 * np.linalg.norm(preds[1])
 
 
 def test_seeded_training_is_reproducible():

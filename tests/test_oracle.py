@@ -641,3 +641,26 @@ def test_poles_mirror_rows_and_manufactured_solution():
     x = o.f("DELTA_ER")
     assert rel_l2(x[2:nx + 2, 2:ny + 2, 2:nz + 1], xs[2:nx + 2, 2:ny + 2, 2:nz + 1]) <= 1e-9
     assert _mirrored(x, nz)
+
+
+def test_poles_diffusion_sweeps_every_row():
+    """DIFFUSION with poles (ppdif.f:45-135): every theta row k = 1..NZ is
+    swept (DIFFUSION has no zmax_sor_index) and the scalar is pole-shifted
+    after each colour, which overwrites row NZ with row NZ-1.  Row NZ's
+    residual therefore stays in RNORM, the ratio levels off, and the loop
+    runs to SORITMAX = 500 (status 1, the reference's message) with the
+    scalar mirrored."""
+    from ttcode_gb300.synthetic import make_shell
+    nx, ny, nz = 16, 24, 12
+    sh = make_shell(nx, ny, nz, seed=9, delt=100.0, poles=True)
+    o = oracle_from_shell(sh)
+    rng = np.random.default_rng(5)
+    o.f("SCALAR")[...] = 1.0 + rng.random((nx + 4, ny + 4, nz + 4))
+    assert o.call("planetshift", "SCALAR") == 0
+    assert _mirrored(o.f("SCALAR"), nz)
+    o.set("pr_num", 1.0)
+    o.set("xnue", 1.0e15)
+    assert o.call("diffusion") == 1
+    assert int(o.get("sor_iter")) == 500
+    assert 1e-4 < o.get("global_rnorm") / o.get("global_rhsnorm") < 1e-1
+    assert _mirrored(o.f("SCALAR"), nz)

@@ -246,13 +246,42 @@ static void fill_stats(ttfld_ctx* c, ttfld_solve_stats* st, int status) {
 // Red-black SOR to the ppsor.f:161-177 rule.  The host checks the device
 // flag after chunks of sweeps; sweeps queued after the rule fired return at
 // once, so the iteration count is exactly the reference's.
-int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
+// DIFFUSION's sweeps on a context with poles: every theta row k = 1..NZ
+// (ppdif.f:45-46, 93-94; no zmax_sor_index), the theta ghosts read as they
+// are, and the pole shifts of the scalar after each colour (ppdif.f:80-89,
+// 123-132), which row NZ needs: its k+1 ghost holds row NZ-2 from before
+// the half-sweep.
+static int launch_exact_sweeps_all_rows(ttfld_ctx* c, double* x, const double* b, int nsweeps, int itmin,
+                                        int itmax, double eps) {
+  const int nb = sweep_blocks(c->d);
+  const double omega = c->d.sorparam;
+  Dev d = c->d;
+  d.poles = 0;  // sor_zmax = NZ and x_km / x_kp read the ghosts
+  int rc;
+  for (int s = 0; s < nsweeps; ++s) {
+    sor_exact_kernel<0><<<nb, kThreads, 0, c->stream>>>(d, x, b, omega, c->partials, itmin, itmax, eps);
+    if ((rc = pole_shift(c, x))) return rc;
+    sor_exact_kernel<1><<<nb, kThreads, 0, c->stream>>>(d, x, b, omega, c->partials, itmin, itmax, eps);
+    if ((rc = pole_shift(c, x))) return rc;
+  }
+  count_launches(2 * nsweeps);
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
+// all_rows: DIFFUSION's row range and pole shifts (above) instead of
+// SOLVE_WITH_SOR's.
+static int solve_exact_rows(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st,
+                            bool all_rows) {
+  all_rows = all_rows && c->d.poles;
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   int rc = rhs_norm(c, b, nullptr);
   if (rc) return rc;
   int chunk = 4, launched = 0;
   for (;;) {
-    if ((rc = launch_exact_sweeps(c, x, b, chunk, itmin, itmax, c->d.epsmat))) return rc;
+    rc = all_rows ? launch_exact_sweeps_all_rows(c, x, b, chunk, itmin, itmax, c->d.epsmat)
+                  : launch_exact_sweeps(c, x, b, chunk, itmin, itmax, c->d.epsmat);
+    if (rc) return rc;
     launched += chunk;
     TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
     TT_CHECK(cudaStreamSynchronize(c->stream));
@@ -265,6 +294,10 @@ int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax
   int status = c->host_sol->nonfinite ? TTFLD_E_NONFINITE : (c->host_sol->maxit ? TTFLD_MAXITER : TTFLD_OK);
   fill_stats(c, st, status);
   return status;
+}
+
+int solve_exact64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
+  return solve_exact_rows(c, x, b, itmin, itmax, st, false);
 }
 
 }  // namespace ttfld
@@ -504,7 +537,6 @@ namespace ttfld {
 // SOR with ITMIN=5 and SORITMAX=500 (ppdif.f:14-15), in place on SCALAR.
 static int diffusion(ttfld_ctx* c, ttfld_solve_stats* st) {
   Dev d = c->d;
-  if (d.poles) return TTFLD_E_UNSUPPORTED;  // DIFFUSION's pole branches (ppdif.f:82, 125) are not built
   if (!(d.pr_num != 0.0)) return TTFLD_E_ARGS;
   const double dconst = d.xnue / d.pr_num;
   launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
@@ -531,7 +563,7 @@ static int diffusion(ttfld_ctx* c, ttfld_solve_stats* st) {
     }
   });
   TT_CHECK_LAUNCH();
-  return solve_exact64(c, d.SCALAR, d.RHS_DIF, 5, 500, st);
+  return solve_exact_rows(c, d.SCALAR, d.RHS_DIF, 5, 500, st, true);
 }
 }  // namespace ttfld
 

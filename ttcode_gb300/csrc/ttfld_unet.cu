@@ -640,23 +640,34 @@ static int launch_conv_tc(cudaStream_t s, const ConvArgs& a) {
   CUtensorMap tm, tr;
   if (!tc_tensor_map(&tm, a, kUHY) || !tc_tensor_map(&tr, a, 1)) return TTFLD_E_UNSUPPORTED;
   const size_t smem = conv_tc_smem_bytes(a.cin, N);
-  static int opted = 0, sms = 0;
+  static int opted = 0, sms = 0, smem_sm = 0, smem_rsv = 0, smem_static = 0;
   if (!opted) {
     if (cudaFuncSetAttribute(conv3_tc_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024) !=
         cudaSuccess)
+      return TTFLD_E_CUDA;
+    // the whole unified L1/shared array as shared memory, so that several
+    // CTAs fit on an SM (the default carveout left room for one)
+    if (cudaFuncSetAttribute(conv3_tc_kernel<N>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
       return TTFLD_E_CUDA;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 152;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, conv3_tc_kernel<N>) == cudaSuccess) smem_static = (int)fa.sharedSizeBytes;
     opted = 1;
   }
-  // as many persistent CTAs as fit on an SM (shared memory bounds it): while
-  // one CTA's epilogue reads its accumulators and stores, another's MMAs run
-  int per_sm = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3_tc_kernel<N>, 128, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  // as many persistent CTAs as the SM's shared memory holds (at most 4; 32
+  // tensor-memory columns each): while one CTA's epilogue reads its
+  // accumulators and stores, another's MMAs run.  CTAs beyond what is
+  // resident wait for a slot, so an overestimate costs nothing but order.
+  const long long per_cta = (long long)smem + smem_static + smem_rsv;
+  int per_sm = smem_sm > 0 ? (int)(smem_sm / per_cta) : 1;
+  if (per_sm > 4) per_sm = 4;
+  if (per_sm < 1) per_sm = 1;
   const long long ntiles = (long long)((a.X + kUX - 1) / kUX) * ((a.Y + kUY - 1) / kUY) * a.Z;
   const long long slots = (long long)sms * per_sm;
   const int blocks = (int)(ntiles < slots ? ntiles : slots);
@@ -666,13 +677,15 @@ static int launch_conv_tc(cudaStream_t s, const ConvArgs& a) {
   return 0;
 }
 
-// 1: convolutions of the large levels on tcgen05; 0 (default): on
-// mma.sync with shared-memory tiles, which is faster at these channel
-// counts (the whole inference at half of 256x128x100: 1.13 ms against
-// 1.72 ms -- a 128 x 16 tile per CTA leaves the tensor core mostly idle
-// while its operands are staged).  A wait of the tcgen05 form that ran out
-// turns it off for the process and fails the pass that saw it.
-static int g_conv_tc = 0;
+// Which layers run on tcgen05: 0 none (mma.sync with shared-memory tiles
+// everywhere), 1 every layer the tcgen05 form takes, 2 (default) those with
+// 16 output channels.  Measured on the half-resolution grid of 100x256x128
+// with up to 4 CTAs per SM: a 16 -> 16 layer takes 52-57 us on tcgen05
+// against 76 us on mma.sync, a 16 -> 32 layer 27.6 us against 21.3 us
+// (about one tile per CTA, so staging the weights is not amortised).  A
+// wait of the tcgen05 form that ran out turns it off for the process and
+// fails the pass that saw it.
+static int g_conv_tc = 2;
 
 static int check_umma(cudaStream_t s) {
   if (!g_conv_tc) return 0;
@@ -689,7 +702,8 @@ static int check_umma(cudaStream_t s) {
 
 static int conv_fwd(cudaStream_t s, const ConvArgs& a) {
   if (a.cin % 16 || a.cout % 16 || a.in_cs % 2 || a.in_co % 2 || a.out_cs % 2 || a.out_co % 2) return TTFLD_E_ARGS;
-  if (g_conv_tc && tc_usable(a)) {
+  const bool tc = g_conv_tc == 1 || (g_conv_tc == 2 && a.cout == 16);
+  if (tc && tc_usable(a)) {
     if (a.cout == 16) return launch_conv_tc<16>(s, a);
     if (a.cout == 32) return launch_conv_tc<32>(s, a);
   }
@@ -1714,7 +1728,7 @@ int ttfld_guess_predict(ttfld_ctx* c, const float* feat, float* pred) {
 }
 
 int ttfld_guess_set_conv(int use_tcgen05) {
-  if (use_tcgen05 != 0 && use_tcgen05 != 1) return TTFLD_E_ARGS;
+  if (use_tcgen05 < 0 || use_tcgen05 > 2) return TTFLD_E_ARGS;
   g_conv_tc = use_tcgen05;
   return 0;
 }
