@@ -82,11 +82,12 @@ typedef struct {
                      (ppshift.f:2217-2453) -- planes NZ-1..NZ-3 mirrored
                      onto NZ..NZ+2 and planes 1, 2 onto 0, -1 after every
                      phi exchange, no theta boundary rows, the SOR stopping
-                     at NZ-1 (ppsor.f:39-43).  The exact and FP32/FP64 SOR
-                     of COUPLED_ENERGY_EQS take it, and DIFFUSION (every
-                     theta row, the scalar pole-shifted after each colour,
-                     ppdif.f:45-135); the fast FP64 SOR, PCG,
-                     SOLVE_WITH_HYPRE and RADDIF return TTFLD_E_UNSUPPORTED */
+                     at NZ-1 (ppsor.f:39-43).  The SOR solvers of
+                     COUPLED_ENERGY_EQS (exact, scaled and FP32/FP64) take
+                     it, and so do DIFFUSION and RADDIF (every theta row,
+                     the pole shifts after each colour, ppdif.f:45-135,
+                     ppmat.f:39-136); PCG and SOLVE_WITH_HYPRE return
+                     TTFLD_E_UNSUPPORTED */
 } ttfld_dims;
 
 /* 1-D metric arrays of GITTER (ppinit.f:1028-1406), each passed with the

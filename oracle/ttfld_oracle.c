@@ -1699,7 +1699,8 @@ int ttor_diffusion(ttor_state* s) {
 /* ---- IRAD=1: RADDIF pprad.f:1-38, DIFFEL :40-72, SOLVMAT ppmat.f:1-186,
  * RADIATIVEBOUND ppbou.f:2049-2299 (RADBOUNDVER = IBDRAD 4, 7 or 9, the
  * top boundaries the rest of this library implements, with MODVER <= 5; one
- * rank, periodic phi, poles = .false.) ----------------------------------- */
+ * rank, periodic phi; with poles the theta ghosts come from the pole shifts
+ * after every PLANETSHIFT(6)) --------------------------------------------- */
 
 /* RADIATIVEBOUND: bottom T and ER (:2127-2139), top ER at i >= upperbnd
  * (:2145-2236), theta ghost copies (:2256-2271), PLANETSHIFT(6) (:2280). */
@@ -1747,7 +1748,8 @@ static int radiativebound(ttor_state* s, double d_t, double tinit_bottom, int mo
         H(ER, i, j, nz + 2) = H(ER, i, j, nz);
       }
   }
-  shift_halo(s, s->ER);
+  shift_halo(s, s->ER);  /* PLANETSHIFT(6) and the pole shifts (:2280-2290) */
+  pole_shift(s, s->ER);
   return 0;
 }
 
@@ -1772,7 +1774,7 @@ static void solvmat_colour(ttor_state* s, double* xs, int parity, double om) {
 
 int ttor_raddif(ttor_state* s, double d_t, double tinit_bottom, int modver, int energy_iter) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
-  if (s->poles || nz == 1) return -3;
+  if (nz == 1) return -3;
   /* ER = arad T^4 on the whole array (pprad.f:12) */
   for (size_t q = 0; q < nhalo(s); ++q) s->ER[q] = ARAD_C * p4(s->T[q]);
   /* DIFFEL (pprad.f:40-72): DIFF, then the couplings */
@@ -1801,7 +1803,8 @@ int ttor_raddif(ttor_state* s, double d_t, double tinit_bottom, int modver, int 
   for (size_t c = 0; c < ncell(s); ++c) rhsnorm = rhsnorm + s->RAD_RHS[c] * s->RAD_RHS[c];
   rhsnorm = sqrt(rhsnorm);
   s->global_rhsnorm = rhsnorm;
-  shift_halo(s, s->ER);
+  shift_halo(s, s->ER);  /* ppmat.f:39-49 */
+  pole_shift(s, s->ER);
   double* xs = (double*)calloc(ncell(s), sizeof(double));
   if (!xs) return -2;
   const double om = s->sorparam;
@@ -1810,10 +1813,12 @@ int ttor_raddif(ttor_state* s, double d_t, double tinit_bottom, int modver, int 
     ++it;
     solvmat_colour(s, xs, 0, om);
     if ((rc = radiativebound(s, d_t, tinit_bottom, modver))) break;
-    shift_halo(s, s->ER);
+    shift_halo(s, s->ER);  /* ppmat.f:87-97 */
+    pole_shift(s, s->ER);
     solvmat_colour(s, xs, 1, om);
     if ((rc = radiativebound(s, d_t, tinit_bottom, modver))) break;
-    shift_halo(s, s->ER);
+    shift_halo(s, s->ER);  /* ppmat.f:126-136 */
+    pole_shift(s, s->ER);
     double rnorm = 0.0;
     for (size_t c = 0; c < ncell(s); ++c) rnorm = rnorm + xs[c] * xs[c];
     rnorm = sqrt(rnorm);

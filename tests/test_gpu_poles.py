@@ -6,10 +6,12 @@ NZ..NZ+2 and planes 1, 2 onto 0, -1 (NORTH/SOUTH_POLE_SHIFT,
 ppshift.f:2217-2453), the theta edges are ordinary rows of the SOR system
 (ppsor.f:228-272) and SOLVE_WITH_SOR stops at NZ-1 (ppsor.f:39-43).
 
-Bars as for the shells without poles: bitwise for BOUNDS, KAPPA and the exact
-FP64 sweeps and solve; the exact step's counts identical and its fields
-within 1e-9; the FP32/FP64 solver's step within 1e-9 of the oracle converged
-to 1e-12.  The solvers that have no pole rows refuse the context.
+Bars as for the shells without poles: bitwise for BOUNDS, KAPPA, the exact
+FP64 sweeps and solve, DIFFUSION and RADDIF (where no exp() enters); the
+exact step's counts identical and its fields within 1e-9; the FP32/FP64
+solver's and the scaled FP64 SOR's steps within 1e-9 of the oracle
+converged to 1e-12.  PCG and SOLVE_WITH_HYPRE, which have no pole rows,
+refuse the context.
 """
 import numpy as np
 import pytest
@@ -115,11 +117,67 @@ def test_poles_diffusion_bitwise(polar):
     f.close()
 
 
-@pytest.mark.parametrize("solver", ["sor64_fast", "pcg"])
-def test_poles_unsupported_solvers_refuse(polar, solver):
+@pytest.mark.parametrize("ibdrad,eps,itmax", [(7, 1e-6, 3000), (4, 1e-10, 60), (9, 1e-10, 40)])
+def test_poles_raddif(ibdrad, eps, itmax):
+    """RADDIF with poles (SOLVMAT over k = 1..NZ, the pole shifts after every
+    PLANETSHIFT(6), RADIATIVEBOUND without its theta copies): the oracle's
+    iteration count, E_R bitwise for the tops without exp() (IBDRAD 4, 7),
+    within 1e-12 for IBDRAD 9."""
+    from test_oracle import rad_oracle
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(24, 16, 12, seed=11, delt=100.0, poles=True)
+    o = rad_oracle(sh, ibdrad, eps, itmax)
+    rc_o = o.call("raddif", 0.0, 0.0, 1, 0)
+    f = fld_from_shell(sh, eps=eps, itmax=itmax)
+    f.set_params(ibdrad=ibdrad, iii=2)
+    f.stellarinput_heating()
+    st = f.raddif(0.0, 0.0, 1, 0)
+    assert st.status == rc_o
+    assert st.sor_iter == int(o.get("sor_iter"))
+    if ibdrad in (4, 7):
+        assert np.array_equal(f.download("ER"), o.f("ER"))
+    else:
+        assert rel_l2(f.download("ER"), o.f("ER")) <= 1e-12
+    assert rel_l2(f.download("T"), o.f("T")) <= 1e-12
+    f.close()
+
+
+def test_poles_fast64_solve_and_step(polar):
+    """The scaled FP64 SOR with poles (FMA on Jacobi-scaled coefficients, the
+    same iteration as the reference loop): the step's system solved from zero
+    takes the oracle's sweep count up to a last-bit tie and meets the
+    oracle's 1e-12 solution to 1e-9; a full step matches the oracle's."""
+    o = oracle_from_shell(polar)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    f = fld_from_shell(polar)
+    _same_system(f, o)
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("solve_with_sor", 0, 0) == 0
+    n64 = int(o.get("sor_iter"))
+    o.set("epsmat", 1e-12)
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("solve_with_sor", 0, 0) == 0
+    f.set_solver("sor64_fast", tol=1e-10)
+    f.begin_step(new_run=True)
+    st = f.solve_system()
+    assert abs(st.sor_iter - n64) <= 1
+    assert rel_l2(f.download("DELTA_ER"), o.f("DELTA_ER")) <= TOL
+    f.close()
+    o = oracle_from_shell(polar, eps=1e-12)
+    f = fld_from_shell(polar)
+    f.set_solver("sor64_fast", tol=1e-10)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    st = f.coupled_energy_eqs(True)
+    assert st.energy_iter == int(o.get("energy_iter"))
+    for n in ("ER", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= TOL, n
+    f.close()
+
+
+def test_poles_unsupported_solvers_refuse(polar):
     from ttcode_gb300._ffi import TTFLDError
     f = fld_from_shell(polar)
-    f.set_solver(solver)
+    f.set_solver("pcg")
     with pytest.raises(TTFLDError) as e:
         f.coupled_energy_eqs(True)
     assert e.value.status == -3

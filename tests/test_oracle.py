@@ -643,6 +643,22 @@ def test_poles_mirror_rows_and_manufactured_solution():
     assert _mirrored(x, nz)
 
 
+@pytest.mark.parametrize("ibdrad,eps,itmax,rc", [(7, 1e-6, 3000, 0), (4, 1e-10, 60, 1)])
+def test_poles_raddif(ibdrad, eps, itmax, rc):
+    """RADDIF with poles: SOLVMAT sweeps k = 1..NZ, RADIATIVEBOUND leaves the
+    theta ghosts to the pole shifts that follow every PLANETSHIFT(6)
+    (ppmat.f:39-136, ppbou.f:2256-2290).  With the zero-gradient top it
+    still reaches EPSMAT; E_R and T come out mirrored at the theta edges."""
+    from ttcode_gb300.synthetic import make_shell
+    nx, ny, nz = 24, 16, 12
+    sh = make_shell(nx, ny, nz, seed=11, delt=100.0, poles=True)
+    o = rad_oracle(sh, ibdrad, eps, itmax)
+    assert o.call("raddif", 0.0, 0.0, 1, 0) == rc
+    assert 5 <= int(o.get("sor_iter")) <= itmax
+    assert _mirrored(o.f("ER"), nz) and _mirrored(o.f("T"), nz)
+    assert np.all(np.isfinite(o.f("T")))
+
+
 def test_poles_diffusion_sweeps_every_row():
     """DIFFUSION with poles (ppdif.f:45-135): every theta row k = 1..NZ is
     swept (DIFFUSION has no zmax_sor_index) and the scalar is pole-shifted

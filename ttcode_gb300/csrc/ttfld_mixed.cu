@@ -883,8 +883,10 @@ static int prep64(ttfld_ctx* c, const double* x, const double* b) {
     double bb = b[q];
     if (i == 1) bb = bb - d.SB[q] * x[hidx(d, 0, j, k)];
     if (i == d.nx) bb = bb - d.SC[q] * x[hidx(d, d.nx + 1, j, k)];
-    if (k == 1) bb = bb - d.SF[q] * x[hidx(d, i, j, 0)];
-    if (k == d.nz) bb = bb - d.SG[q] * x[hidx(d, i, j, d.nz + 1)];
+    // with poles the theta ghosts are the mirror, read in the sweep as the
+    // cell's own value, and row NZ is not swept: nothing to fold
+    if (!d.poles && k == 1) bb = bb - d.SF[q] * x[hidx(d, i, j, 0)];
+    if (!d.poles && k == d.nz) bb = bb - d.SG[q] * x[hidx(d, i, j, d.nz + 1)];
     m.a[0][col][s] = d.SB[q] * inv;
     m.a[1][col][s] = d.SC[q] * inv;
     m.a[2][col][s] = d.SD[q] * inv;
@@ -917,8 +919,10 @@ __device__ __forceinline__ void st2(double* p, double2 v) { *reinterpret_cast<do
 
 // One colour of the FP64 red-black sweep on the scaled system, 2 cells per
 // thread: rh = x + sum a_nb x_nb - bhat; resid = A*rh (the reference's
-// in-sweep residual, ppsor.f:64-73); x -= omega*rh.
-template <int COL>
+// in-sweep residual, ppsor.f:64-73); x -= omega*rh.  POLES as in
+// update_vec: theta rows 1 and NZ-1 take the cell itself across the edge,
+// row NZ is not swept.
+template <int COL, bool POLES>
 __global__ void __launch_bounds__(kThreads) sweep64_kernel(Dev d, Cmp g, Fast64 m, double omega, double* partials,
                                                            int itmin, int itmax, double eps) {
   __shared__ double sh[32];
@@ -934,6 +938,7 @@ __global__ void __launch_bounds__(kThreads) sweep64_kernel(Dev d, Cmp g, Fast64 
     const int hv = (int)(t % nv);
     const long long rr = t / nv;
     const int j0 = (int)(rr % g.ny), k0 = (int)(rr / g.ny);
+    if (POLES && k0 == g.nz - 1) continue;  // zmax_sor_index = NZ-1 (ppsor.f:39-43)
     const int off = (1 + ((j0 + k0) & 1) + COL) & 1;
     const int h0 = hv * 2;
     const int ncol = (g.nx - off + 1) >> 1;
@@ -950,9 +955,9 @@ __global__ void __launch_bounds__(kThreads) sweep64_kernel(Dev d, Cmp g, Fast64 
     }
     const double2 s = ld2(xo + gslot(g, jm, k0, h0));
     const double2 nn = ld2(xo + gslot(g, jp, k0, h0));
-    const double2 bz = ld2(xo + eb - plane);
-    const double2 tz = ld2(xo + eb + plane);
     const double2 xv = ld2(xs + eb);
+    const double2 bz = (POLES && k0 == 0) ? xv : ld2(xo + eb - plane);
+    const double2 tz = (POLES && k0 == g.nz - 2) ? xv : ld2(xo + eb + plane);
     const double2 aw = ld2(m.a[0][COL] + cb), ae = ld2(m.a[1][COL] + cb);
     const double2 as = ld2(m.a[2][COL] + cb), an = ld2(m.a[3][COL] + cb);
     const double2 ab = ld2(m.a[4][COL] + cb), at = ld2(m.a[5][COL] + cb);
@@ -997,8 +1002,15 @@ int launch_sweeps64(ttfld_ctx* c, int nsweeps, int itmin, int itmax, double eps)
   if (nb > kMaxPartials) nb = kMaxPartials;
   double omega = c->d.sorparam;
   for (int s = 0; s < nsweeps; ++s) {
-    sweep64_kernel<0><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
-    sweep64_kernel<1><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
+    if (g.poles) {
+      sweep64_kernel<0, true><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
+      sweep64_kernel<1, true><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax, eps);
+    } else {
+      sweep64_kernel<0, false><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax,
+                                                               eps);
+      sweep64_kernel<1, false><<<nb, kThreads, 0, c->stream>>>(c->d, g, w->m64, omega, c->partials, itmin, itmax,
+                                                               eps);
+    }
   }
   count_launches(2 * nsweeps);
   TT_CHECK_LAUNCH();
@@ -1007,7 +1019,6 @@ int launch_sweeps64(ttfld_ctx* c, int nsweeps, int itmin, int itmax, double eps)
 
 int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax, ttfld_solve_stats* st) {
   int rc;
-  if (c->d.poles) return TTFLD_E_UNSUPPORTED;  // its ghost folding assumes theta boundary rows
   if ((rc = ensure64(c))) return rc;
   MixWork* w = work(c);
   TT_CHECK(cudaMemsetAsync(w->m64.x[0], 0, 2 * w->g.gsz * sizeof(double), c->stream));
@@ -1024,7 +1035,7 @@ int solve_fast64(ttfld_ctx* c, double* x, const double* b, int itmin, int itmax,
     if (launched >= itmax + 2) return TTFLD_E_CUDA;
     chunk = chunk < 128 ? chunk * 2 : 256;
   }
-  if ((rc = unpack64(c, x)) || (rc = halo_shift(c, x))) return rc;
+  if ((rc = unpack64(c, x)) || (rc = halo_shift(c, x)) || (rc = pole_shift(c, x))) return rc;
   int status = c->host_sol->nonfinite ? TTFLD_E_NONFINITE : (c->host_sol->maxit ? TTFLD_MAXITER : TTFLD_OK);
   if (st) {
     st->sor_iter = c->host_sol->iter;

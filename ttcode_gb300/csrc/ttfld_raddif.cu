@@ -126,6 +126,13 @@ __global__ void __launch_bounds__(kThreads) radbound_xkernel(Dev d, double d_t, 
   }
 }
 
+// PLANETSHIFT(6) and, with poles, the pole shifts of E_R that follow it
+// everywhere in RADDIF (ppmat.f:39-49, 87-97, 126-136; ppbou.f:2280-2290).
+static int er_shift(ttfld_ctx* c) {
+  int rc = halo_shift(c, c->d.ER);
+  return rc ? rc : pole_shift(c, c->d.ER);
+}
+
 // RADIATIVEBOUND, part 2 (ppbou.f:2256-2271): theta ghosts from k = 1, NZ.
 __global__ void __launch_bounds__(kThreads) radbound_zkernel(Dev d) {
   if (solver_done(d)) return;
@@ -185,13 +192,18 @@ int cell_blocks(const Dev& d) {
   return nb > kMaxPartials ? kMaxPartials : nb;
 }
 
+// With poles the theta ghosts come from the pole shifts instead
+// (ppbou.f:2256-2271 run only without poles; :2280-2290).
 int radiativebound(ttfld_ctx* c, double d_t, double tinit_bottom) {
   const Dev& d = c->d;
   radbound_xkernel<<<grid_for((long long)(d.ny + 4) * (d.nz + 4)), kThreads, 0, c->stream>>>(d, d_t, tinit_bottom);
-  radbound_zkernel<<<grid_for((long long)(d.nx + 4) * (d.ny + 4)), kThreads, 0, c->stream>>>(d);
-  count_launches(2);
+  count_launches(1);
+  if (!d.poles) {
+    radbound_zkernel<<<grid_for((long long)(d.nx + 4) * (d.ny + 4)), kThreads, 0, c->stream>>>(d);
+    count_launches(1);
+  }
   TT_CHECK_LAUNCH();
-  return halo_shift(c, d.ER);
+  return er_shift(c);
 }
 
 }  // namespace
@@ -201,7 +213,7 @@ extern "C" int ttfld_raddif(ttfld_ctx* c, const ttfld_raddif_params* p, ttfld_so
   using namespace ttfld;
   if (!c || !p || !p->volxb || !p->volyb || !p->volzb) return TTFLD_E_ARGS;
   const Dev& d = c->d;
-  if (d.nz == 1 || c->dims.poles) return TTFLD_E_UNSUPPORTED;
+  if (d.nz == 1) return TTFLD_E_UNSUPPORTED;
   if (!(d.ibdrad == 4 || d.ibdrad == 7 || d.ibdrad == 9) || p->modver > 5)
     return TTFLD_E_UNSUPPORTED;
   TT_CHECK(cudaSetDevice(c->device));
@@ -234,7 +246,7 @@ extern "C" int ttfld_raddif(ttfld_ctx* c, const ttfld_raddif_params* p, ttfld_so
     const int nb = cell_blocks(d);
     l2_kernel<<<nb, kThreads, 0, c->stream>>>(d, w.rhs, c->partials, 0, d.itmax, d.epsmat);
     count_launches(1);
-    rc = halo_shift(c, d.ER);
+    rc = er_shift(c);
   }
   // iterations in chunks between polls of the stopping flag
   const int sweeps_nb = grid_for((long long)((d.nx + 1) / 2) * d.ny * d.nz);
@@ -243,10 +255,10 @@ extern "C" int ttfld_raddif(ttfld_ctx* c, const ttfld_raddif_params* p, ttfld_so
     for (int s = 0; s < chunk && !rc; ++s) {
       solvmat_colour_kernel<0><<<sweeps_nb, kThreads, 0, c->stream>>>(d, w, d.sorparam);
       count_launches(1);
-      if ((rc = radiativebound(c, p->d_t, p->tinit_bottom)) || (rc = halo_shift(c, d.ER))) break;
+      if ((rc = radiativebound(c, p->d_t, p->tinit_bottom)) || (rc = er_shift(c))) break;
       solvmat_colour_kernel<1><<<sweeps_nb, kThreads, 0, c->stream>>>(d, w, d.sorparam);
       count_launches(1);
-      if ((rc = radiativebound(c, p->d_t, p->tinit_bottom)) || (rc = halo_shift(c, d.ER))) break;
+      if ((rc = radiativebound(c, p->d_t, p->tinit_bottom)) || (rc = er_shift(c))) break;
       l2_kernel<<<cell_blocks(d), kThreads, 0, c->stream>>>(d, w.xs, c->partials, 1, d.itmax, d.epsmat);
       count_launches(1);
       TT_CHECK_LAUNCH();
