@@ -86,8 +86,9 @@ typedef struct {
                      COUPLED_ENERGY_EQS (exact, scaled and FP32/FP64) take
                      it, and so do DIFFUSION and RADDIF (every theta row,
                      the pole shifts after each colour, ppdif.f:45-135,
-                     ppmat.f:39-136); PCG and SOLVE_WITH_HYPRE return
-                     TTFLD_E_UNSUPPORTED */
+                     ppmat.f:39-136), and PCG (the mirror coupling of
+                     rows 1 and NZ-1 in their diagonal, row NZ decoupled);
+                     SOLVE_WITH_HYPRE returns TTFLD_E_UNSUPPORTED */
 } ttfld_dims;
 
 /* 1-D metric arrays of GITTER (ppinit.f:1028-1406), each passed with the

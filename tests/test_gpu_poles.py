@@ -9,9 +9,9 @@ ppshift.f:2217-2453), the theta edges are ordinary rows of the SOR system
 Bars as for the shells without poles: bitwise for BOUNDS, KAPPA, the exact
 FP64 sweeps and solve, DIFFUSION and RADDIF (where no exp() enters); the
 exact step's counts identical and its fields within 1e-9; the FP32/FP64
-solver's and the scaled FP64 SOR's steps within 1e-9 of the oracle
-converged to 1e-12.  PCG and SOLVE_WITH_HYPRE, which have no pole rows,
-refuse the context.
+solver's, the scaled FP64 SOR's and PCG's steps within 1e-9 of the oracle
+converged to 1e-12.  SOLVE_WITH_HYPRE, whose pole graph is hypre's,
+refuses the context.
 """
 import numpy as np
 import pytest
@@ -174,13 +174,45 @@ def test_poles_fast64_solve_and_step(polar):
     f.close()
 
 
-def test_poles_unsupported_solvers_refuse(polar):
+def test_poles_pcg_solve_and_step(polar):
+    """PCG on SOLVE_WITH_SOR's system with poles (rows 1 and NZ-1 take their
+    mirror coupling into the diagonal, row NZ is decoupled and then
+    pole-shifted; the weighted rows stay symmetric): the system from zero,
+    solved to 1e-11, meets the oracle's 1e-12 SOR solution to 1e-9, and a
+    full step at 1e-10 matches the oracle's with the same outer-iteration
+    count."""
+    o = oracle_from_shell(polar, eps=1e-12)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    f = fld_from_shell(polar)
+    _same_system(f, o)
+    for n in ("EVAL1", "EVAL2", "EVAL3", "EVAL4", "EVAL5", "EVAL6", "EVAL7", "EVAL8", "EVAL_1_6"):
+        f.upload(n, o.f(n))           # the symmetrising weight reads EVAL8
+    o.f("DELTA_ER")[...] = 0.0
+    assert o.call("solve_with_sor", 0, 0) == 0
+    f.set_solver("pcg", tol=1e-11)   # the error is ~10x the residual on this system
+    f.begin_step(new_run=True)
+    st = f.solve_system()
+    assert st.status == 0
+    r, b = f.true_residual()
+    assert r / b <= 1e-11
+    assert rel_l2(f.download("DELTA_ER"), o.f("DELTA_ER")) <= TOL
+    f.close()
+    o = oracle_from_shell(polar, eps=1e-12)
+    f = fld_from_shell(polar)
+    f.set_solver("pcg", guess="previous", tol=1e-10)
+    assert o.call("coupled_energy_eqs", 1) == 0
+    st = f.coupled_energy_eqs(True)
+    assert st.status == 0 and st.energy_iter == int(o.get("energy_iter"))
+    for n in ("ER", "T"):
+        assert rel_l2(f.download(n), o.f(n)) <= TOL, n
+    f.close()
+
+
+def test_poles_hypre_refuses(polar):
+    """SOLVE_WITH_HYPRE's pole graph (pphypre.f:458-540) goes through
+    hypre's neighbour boxes, which are not restated: status -3."""
     from ttcode_gb300._ffi import TTFLDError
     f = fld_from_shell(polar)
-    f.set_solver("pcg")
-    with pytest.raises(TTFLDError) as e:
-        f.coupled_energy_eqs(True)
-    assert e.value.status == -3
     with pytest.raises(TTFLDError) as e:
         f.solve_with_hypre()
     assert e.value.status == -3

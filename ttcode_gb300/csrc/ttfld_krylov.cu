@@ -81,22 +81,33 @@ struct Row {
 };
 // hypre's grid has only its extents (pphypre.f:404-413, no periodicity), so
 // the j-1 entry of rows j = 1 and the j+1 entry of rows j = NY reach outside
-// it and are dropped.
-__device__ __forceinline__ Row row_of(const Dev& d, size_t t, int i, int j, bool hypre) {
+// it and are dropped.  With poles (SOLVE_WITH_SOR's system only): the theta
+// neighbour across either edge is the cell itself (the mirror the pole
+// shifts keep), so rows 1 and NZ-1 take that coupling into their diagonal,
+// and row NZ, which the SOR does not solve (ppsor.f:39-43) and the pole
+// shift overwrites, is a decoupled identity row.  Both keep the symmetric
+// form: the couplings between rows 1 and 2, NZ-2 and NZ-1 are unchanged.
+__device__ __forceinline__ Row row_of(const Dev& d, size_t t, int i, int j, int k, bool hypre) {
   Row r{d.SA[t], d.SB[t], d.SC[t], d.SD[t], d.SE[t], d.SF[t], d.SG[t]};
   if (hypre) {
     if (i == 1) r = Row{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // pphypre.f:281-294
     else if (i == 2) r.b = 0.0;                               // pphypre.f:298-300
     if (j == 1) r.d = 0.0;
     if (j == d.ny) r.e = 0.0;
+  } else if (d.poles) {
+    if (k == d.nz) return Row{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (k == 1) { r.a += r.f; r.f = 0.0; }
+    if (k == d.nz - 1) { r.a += r.g; r.g = 0.0; }
   }
   return r;
 }
 
 // b of the hypre system (pphypre.f:137-205): zero at i >= upperbnd, i = 1,
-// i = NX, k = 1 and k = NZ (poles are not implemented).
+// i = NX, k = 1 and k = NZ; with poles, of SOLVE_WITH_SOR's system zero on
+// the identity row NZ.
 __device__ __forceinline__ double b_of(const Dev& d, const double* b, size_t t, int i, int j, int k, bool hypre) {
   if (hypre && (i >= PA(UB, j, k) || i == 1 || i == d.nx || k == 1 || k == d.nz)) return 0.0;
+  if (!hypre && d.poles && k == d.nz) return 0.0;
   return b[t];
 }
 
@@ -113,7 +124,7 @@ __global__ void __launch_bounds__(kThreads) kry_weights_kernel(Dev d, Kry kr, in
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     cell_of(d, t, i, j, k);
-    const Row r = row_of(d, t, i, j, hypre != 0);
+    const Row r = row_of(d, t, i, j, k, hypre != 0);
     const bool decoupled = r.b == 0.0 && r.c == 0.0 && r.d == 0.0 && r.e == 0.0 && r.f == 0.0 && r.g == 0.0;
     const double v = G(surxb, i) * G(dxa, i) * G(dya, j) * G(surzb, k) * G(dza, k);
     const double e8 = d.E8[t];
@@ -135,23 +146,23 @@ __global__ void __launch_bounds__(kThreads) kry_couplings_kernel(Dev d, Kry kr, 
     int i, j, k;
     cell_of(d, t, i, j, k);
     const bool h = hypre != 0;
-    const Row r = row_of(d, t, i, j, h);
+    const Row r = row_of(d, t, i, j, k, h);
     const double wn = kr.wgt[t], sn = kr.sig[t];
     float cr = 0.f, cp = 0.f, ct = 0.f;
     if (i < nx) {
       const size_t m = t + 1;
-      const Row rm = row_of(d, m, i + 1, j, h);
+      const Row rm = row_of(d, m, i + 1, j, k, h);
       cr = (float)(0.5 * (wn * r.c + kr.wgt[m] * rm.b) * sn * kr.sig[m]);
     }
     {
       const int jp = j == ny ? 1 : j + 1;
       const size_t m = cidx(d, i, jp, k);
-      const Row rm = row_of(d, m, i, jp, h);
+      const Row rm = row_of(d, m, i, jp, k, h);
       cp = (float)(0.5 * (wn * r.e + kr.wgt[m] * rm.d) * sn * kr.sig[m]);
     }
     if (k < nz) {
       const size_t m = cidx(d, i, j, k + 1);
-      const Row rm = row_of(d, m, i, j, h);
+      const Row rm = row_of(d, m, i, j, k + 1, h);
       ct = (float)(0.5 * (wn * r.g + kr.wgt[m] * rm.f) * sn * kr.sig[m]);
     }
     const size_t q = lq(kr, i, j, k);
@@ -199,7 +210,7 @@ __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, con
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     cell_of(d, t, i, j, k);
-    const Row r = row_of(d, t, i, j, hypre != 0);
+    const Row r = row_of(d, t, i, j, k, hypre != 0);
     const size_t q = hidx(d, i, j, k);
     const size_t qjm = (j == 1) ? hidx(d, i, ny, k) : q - sj;
     const size_t qjp = (j == ny) ? hidx(d, i, 1, k) : q + sj;
@@ -219,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) kry_anchor_kernel(Dev d, Kry kr, con
     if (L2) s[1] = fma(rs, rs, s[1]);
     if (WITH_B) {
       const double bs = sw * bb;
-      s[2] += fabs(bb);
+      s[2] += fabs(hypre ? bb : b[t]);  // RHSNORM over every row (ppsor.f:33)
       s[3] = fma(bs, bs, s[3]);
     }
     const size_t l = lq(kr, i, j, k);
@@ -850,7 +861,7 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
   // SOLVE_WITH_SOR leaves the phi halo of DELTA_ER refreshed (PLANETSHIFT(8)
   // after the last colour); SOLVE_WITH_HYPRE writes the interior only and its
   // caller shifts (ppenergy.f:353-356)
-  if (!hypre && (rc = halo_shift(c, x))) return rc;
+  if (!hypre && ((rc = halo_shift(c, x)) || (rc = pole_shift(c, x)))) return rc;
   if (st) {
     st->sor_iter = (int)total;
     st->corrections = anchors;
@@ -867,7 +878,6 @@ int pcg_core(ttfld_ctx* c, double* x, const double* b, bool hypre, double tol, l
 }  // namespace
 
 int solve_pcg(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st, int guess_test, int* fallback) {
-  if (c->d.poles) return TTFLD_E_UNSUPPORTED;  // the symmetrised system assumes theta boundary rows
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
   return pcg_core(c, x, b, false, c->opts.tol, budget, false, 0, guess_test, fallback, st);
 }
