@@ -16,7 +16,7 @@
 namespace ttfld {
 
 // FILL_SOR_MATRIX ppsor.f:189-277 and B_VECTOR_BOUNDARIES ppsor.f:280-329,
-// one rank, poles=.false.
+// one rank; with poles the theta-edge rows stay ordinary rows (sor_row).
 // zero_rhs = false leaves RHS_ER as it is (B_VECTOR_BOUNDARIES not applied).
 int fill_sor_matrix(ttfld_ctx* c, bool zero_rhs) {
   Dev d = c->d;

@@ -61,7 +61,7 @@ static int left_bc(ttfld_ctx* c) {
   return 0;
 }
 
-// theta boundaries (poles=.false.), ppenergy.f:204-227 and :706-733.
+// theta boundaries without poles, ppenergy.f:204-227 and :706-733.
 static int z_bc(ttfld_ctx* c) {
   Dev d = c->d;
   if (d.poles) return 0;  // the pole shifts of ER take their place

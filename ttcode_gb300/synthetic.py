@@ -5,7 +5,7 @@ not part of it; the benchmark shells are defined analytically instead:
 
 * grid: NCOSYS=2, linear, r in [1.0, 1.1] R_J (RJUP, ppmod.f:1078), phi in
   [0, 1] * 2 pi (periodic), theta in [-0.95, 0.95] * pi/2 (ipp:25-27),
-  poles off;
+  poles off unless asked for (``poles=True``: the one-rank pole shifts);
 * rho = 1e-2 exp(-(r - r0)/H) with H = (r1 - r0)/8 (8 scale heights);
 * T = 2500 - 1300 (r - r0)/(r1 - r0) K;
 * E_R = a T^4 (optically thick start);
