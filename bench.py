@@ -313,6 +313,31 @@ def run_profile_conv(args):
     f.close()
 
 
+def run_sweep_forms(args):
+    """For the sweep-form comparison under profiles/: on the shell of
+    --profile-dims (default 160,512,256), the first system of an implicit
+    step, then ttfld_time_sweeps (CUDA events, 48 sweeps in one launch, the
+    in-sweep norm every 8th, twice each) for the persistent kernel, the
+    TMA-staged form, two launches per sweep, and the wavefront form with its
+    own window size and with windows of 1, 2, 3, 4, 6 and 8 theta planes."""
+    import torch
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import make_shell
+    torch.cuda.set_device(0)
+    nx, ny, nz = (int(v) for v in (args.profile_dims or "160,512,256").split(","))
+    sh = make_shell(nx, ny, nz, seed=1, delt=100.0)
+    sh.params["epsmat"] = 1e-10
+    f = start_run(sh)
+    first_system(f)
+    forms = [("persistent", "mixed"), ("tma", "mixed_tma"), ("split", "mixed_split"), ("wave", "mixed_wave")]
+    forms += [(f"wave_{p}_planes", 16 + p) for p in (1, 2, 3, 4, 6, 8)]
+    out = {"dims": [nx, ny, nz], "unit": "us per sweep"}
+    for name, code in forms:
+        out[name] = [round(f.time_sweeps(code, 48) * 1e3, 2) for _ in range(2)]
+    print(json.dumps(out), flush=True)
+    f.close()
+
+
 def run_profile_sweeps(args):
     """For the ncu capture of the dominant kernel: the shell256 system (or a
     shell of --profile-dims NX,NY,NZ, e.g. 160,256,128 for a working set
@@ -723,6 +748,8 @@ def main():
     ap.add_argument("--profile-dims", default="", help="NX,NY,NZ of the --profile-sweeps shell (default shell256)")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run three implicit steps, the third inside cudaProfilerStart/Stop")
+    ap.add_argument("--sweep-forms", action="store_true",
+                    help="only time the FP32 sweep kernel's forms on the --profile-dims shell")
     ap.add_argument("--profile-conv", action="store_true",
                     help="only run one inference of the guess network with each convolution form")
     ap.add_argument("--profile-pcg", action="store_true",
@@ -742,6 +769,9 @@ def main():
         return
     if args.profile_conv:
         run_profile_conv(args)
+        return
+    if args.sweep_forms:
+        run_sweep_forms(args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -190,7 +190,10 @@ typedef struct {
                           (default; two launches per sweep where
                           cooperative launch is unavailable), 1 = the same
                           with TMA-staged coefficients (slower here),
-                          2 = two launches per sweep                      */
+                          2 = two launches per sweep, 3 = the sweeps in
+                          pairs, each pair one wavefront over windows of
+                          theta planes with a grid barrier per phase
+                          (temporal blocking through L2; the same iterate) */
 } ttfld_solve_opts;
 
 typedef struct {
@@ -429,8 +432,10 @@ int ttfld_set_freedman_table(ttfld_ctx* ctx, const ttfld_freedman_table* table);
  * the mean device time of one full sweep (both colours), CUDA events on the
  * library's stream.  MIXED times the solver's own kernel (all n sweeps in
  * one persistent launch, the in-sweep norm every 8th); for comparison,
- * solver = 3 times the same FP32 sweeps issued as two launches per sweep
- * and solver = 4 as one launch of the TMA-staged persistent kernel. */
+ * solver = 3 times the same FP32 sweeps issued as two launches per sweep,
+ * solver = 4 as one launch of the TMA-staged persistent kernel, solver = 5
+ * as one launch of the wavefront form (sweep_form 3) with its own window
+ * size and solver = 16 + P with windows of P theta planes (P = 1..256). */
 int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 /* Number of kernels this process has launched through libttfld. */
 uint64_t ttfld_kernel_launches(void);

@@ -200,12 +200,13 @@ def test_diffusion_parity(small):
     assert np.array_equal(f.download("SCALAR"), o.f("SCALAR"))
 
 
-@pytest.mark.parametrize("form", ["persistent", "tma", "split"])
+@pytest.mark.parametrize("form", ["persistent", "tma", "split", "wave"])
 def test_mixed_solver_multi_chunk_grid(form):
     """The FP32/FP64 solve on a 100x128x64 system with each form of its sweep
     kernel (persistent; TMA-staged, which gives each block two chunks, the
-    second partial; two launches per sweep) against the exact FP64 SOR (the
-    reference loop, bitwise) converged to 1e-12."""
+    second partial; two launches per sweep; the wavefront over theta
+    windows) against the exact FP64 SOR (the reference loop, bitwise)
+    converged to 1e-12."""
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
     sh = make_shell(100, 128, 64, seed=5, delt=100.0)
@@ -228,6 +229,36 @@ def test_mixed_solver_multi_chunk_grid(form):
     # same iteration, a different stopping test (true FP64 residual at the
     # anchors against the in-sweep norm): about the same count
     assert abs(st.sor_iter - st64.sor_iter) <= max(16, st64.sor_iter // 20), (st.sor_iter, st64.sor_iter)
+
+
+@pytest.mark.parametrize("poles", [False, True])
+def test_wave_form_is_the_persistent_iteration(poles):
+    """The wavefront form (sweeps in pairs, each pair a wavefront over windows
+    of theta planes, window sizes 1, 3 and the default) does the persistent
+    kernel's iteration in another order: the same sweep count, the same
+    anchors and the same solution bit for bit on a 60x96x40 system, with and
+    without poles."""
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(60, 96, 40, seed=8, delt=100.0, poles=poles)
+    f = start_run(sh)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)
+    f.set_solver("mixed", tol=1e-10, sweep_form="persistent")
+    f.begin_step(new_run=True)
+    st_p = f.solve_system()
+    x_p = f.download("DELTA_ER")
+    f.set_solver("mixed", tol=1e-10, sweep_form="wave")
+    f.begin_step(new_run=True)
+    st_w = f.solve_system()
+    x_w = f.download("DELTA_ER")
+    assert st_w.status == 0 and st_w.sor_iter == st_p.sor_iter, (st_w.sor_iter, st_p.sor_iter)
+    assert st_w.corrections == st_p.corrections
+    assert np.array_equal(x_w, x_p)       # the same sweeps between the same anchors
+    # the timing hook runs the same sweeps with explicit window sizes
+    for planes in (1, 3):
+        assert f.time_sweeps(16 + planes, 16) > 0.0
+    f.close()
 
 
 @pytest.mark.parametrize("name", ["shell_step", "poles_step"])

@@ -351,6 +351,126 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
   }
 }
 
+// ---- temporal blocking through L2 (sweep_form 3) ---------------------------
+// Two sweeps per pass of a wavefront over windows of win_planes theta
+// planes: in phase p the four half-sweeps of the pair (colour 0 and colour 1
+// of sweep A, then of sweep B) run on windows p, p - 2, p - 4 and p - 6,
+// with a grid barrier after every phase.  A half-sweep of plane k reads the
+// other colour at planes k-1, k and k+1 only, so a lag of two windows per
+// stage keeps every read after the write it needs and before the write that
+// replaces it: the iterate after each pair is the persistent kernel's, bit
+// for bit.  The seven windows between a window's first and last stage are
+// meant to stay in L2, so that each array crosses DRAM once per pair
+// instead of once per sweep; the price is nwin + 6 grid barriers per pair
+// instead of four.  A pair whose first sweep carries the in-sweep norm, and
+// an odd last sweep, run as single sweeps.
+constexpr int kWaveLag = 2;
+
+// Items [lo, lo + len) of window w (len 0 outside 0..nwin-1); the form is
+// launched only for fewer than 2^31 items.
+__device__ __forceinline__ void wave_window(int w, int nwin, int wlen, int n, int& lo, int& len) {
+  if (w < 0 || w >= nwin) { lo = 0; len = 0; return; }
+  lo = w * wlen;
+  len = (lo + wlen < n ? lo + wlen : n) - lo;
+}
+
+template <bool POLES>
+__global__ void __launch_bounds__(kPersistThreads) sweeps32_wave(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                                double* partials, double stop_ratio, int nsweeps,
+                                                                int norm_every, int stall_check, int win_planes) {
+  __shared__ double sh[32];
+  __shared__ int stop_sh;
+  if (*(volatile int*)&sol->done) return;
+  const int nv = g.nxp >> 2;
+  const int n = (int)(g.rows * nv);
+  const int wlen = win_planes * g.ny * nv;  // items of one window
+  const int nwin = (n + wlen - 1) / wlen;
+  const size_t plane = (size_t)g.ny * g.nxp;
+  const unsigned int nb = gridDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, ts = gridDim.x * blockDim.x;
+  double last_ratio = -1.0;
+  int sw = 0;
+  while (sw < nsweeps) {
+    const bool norm_a = norm_every > 0 && ((sw + 1) % norm_every == 0 || sw + 1 == nsweeps);
+    const bool pair = sw + 2 <= nsweeps && !norm_a;
+    const int last = sw + (pair ? 2 : 1);  // the last sweep of this round
+    const bool norm = norm_every > 0 && (last % norm_every == 0 || last == nsweeps);
+    float nacc = 0.f;
+    if (pair) {
+      const int nphase = nwin + 3 * kWaveLag;
+      for (int p = 0; p < nphase; ++p) {
+        // stage st (colour st & 1; sweep B from stage 2) works on window
+        // p - kWaveLag * st: its items [lo_st, lo_st + len_st), len 0 when idle
+        int lo0, lo1, lo2, lo3, len0, len1, len2, len3;
+        wave_window(p, nwin, wlen, n, lo0, len0);
+        wave_window(p - kWaveLag, nwin, wlen, n, lo1, len1);
+        wave_window(p - 2 * kWaveLag, nwin, wlen, n, lo2, len2);
+        wave_window(p - 3 * kWaveLag, nwin, wlen, n, lo3, len3);
+        const int total = len0 + len1 + len2 + len3;
+        for (int u = t0; u < total; u += ts) {
+          int q;
+          int t;
+          if (u < len0) { q = 0; t = lo0 + u; }
+          else if (u < len0 + len1) { q = 1; t = lo1 + (u - len0); }
+          else if (u < len0 + len1 + len2) { q = 2; t = lo2 + (u - len0 - len1); }
+          else { q = 3; t = lo3 + (u - len0 - len1 - len2); }
+          switch (q) {
+            case 0: sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); break;
+            case 1: sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); break;
+            case 2:
+              if (norm) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc);
+              else sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc);
+              break;
+            default:
+              if (norm) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc);
+              else sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc);
+          }
+        }
+        if (p == nphase - 1) {
+          if (norm) {
+            const double sb = block_sum((double)nacc, sh);
+            if (threadIdx.x == 0) partials[blockIdx.x] = sb;
+          }
+          if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 2;
+        }
+        if (!grid_sync(sol, nb)) return;
+      }
+    } else {
+      if (norm) { for (int t = t0; t < n; t += ts) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+      else { for (int t = t0; t < n; t += ts) sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); }
+      if (!grid_sync(sol, nb)) return;
+      if (norm) { for (int t = t0; t < n; t += ts) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+      else { for (int t = t0; t < n; t += ts) sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); }
+      if (norm) {
+        const double sb = block_sum((double)nacc, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = sb;
+      }
+      if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+      if (!grid_sync(sol, nb)) return;
+    }
+    if (norm) {  // the persistent kernel's decision, on the same kind of sum
+      const double tot = block_sum_array(partials, nb, sh);
+      if (threadIdx.x == 0) {
+        const double ratio = tot / sol->rhsnorm;
+        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
+        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
+        last_ratio = ratio;
+        if (blockIdx.x == 0) {
+          sol->rnorm = tot;
+          sol->ratio = ratio;
+          if (!isfinite(tot)) sol->nonfinite = 1;
+          if (stall) sol->stalled = 1;
+          if (stop) sol->done = 1;
+        }
+        stop_sh = stop;
+      }
+      __syncthreads();
+      if (stop_sh) return;
+    }
+    sw = last;
+  }
+}
+
 // ---- TMA-staged persistent sweeps (measured alternative) -------------------
 // The same sweeps as sweeps32_persistent, with each block's coefficients
 // streamed through shared memory by bulk asynchronous copies
@@ -656,21 +776,40 @@ static int persistent_grid(K kernel, int threads, size_t smem, long long items) 
   return (int)(need < coresident ? need : coresident);
 }
 
-enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2 };
+enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2, kFormWave = 3 };
+
+// Theta planes per window of the wavefront form: the seven windows a pair
+// keeps in flight should take at most 60 % of L2 (40 B per cell of the FP32
+// system).  g_wave_planes > 0 overrides it (timing runs only).
+static int g_wave_planes = 0;
+static int wave_planes(const Cmp& g) {
+  if (g_wave_planes > 0) return g_wave_planes;
+  int dev = 0, l2 = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+  if (l2 <= 0) l2 = 126 << 20;
+  const double plane_bytes = 2.0 * g.nxp * g.ny * 40.0;
+  int p = (int)(0.6 * l2 / (7.0 * plane_bytes));
+  if (p < 1) p = 1;
+  if (p > g.nz) p = g.nz;
+  return p;
+}
 
 // Blocks of the two persistent kernels for nvec items (0: not available),
 // sized once per grid size and pole form.
 template <bool POLES>
-static void sweep_grids(long long nvec, int* pers, int* tma) {
-  static int tma_blocks = -1, pers_blocks = -1;
+static void sweep_grids(long long nvec, int* pers, int* tma, int* wave = nullptr) {
+  static int tma_blocks = -1, pers_blocks = -1, wave_blocks = -1;
   static long long sized_for = -1;
   if (sized_for != nvec) {
     tma_blocks = persistent_grid(sweeps32_tma<POLES>, kTmaThreads, kTmaSmem, nvec);
     pers_blocks = persistent_grid(sweeps32_persistent<POLES>, kPersistThreads, 0, nvec);
+    wave_blocks = persistent_grid(sweeps32_wave<POLES>, kPersistThreads, 0, nvec);
     sized_for = nvec;
   }
   if (pers) *pers = pers_blocks;
   if (tma) *tma = tma_blocks;
+  if (wave) *wave = wave_blocks;
 }
 
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
@@ -692,8 +831,16 @@ static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, doubl
   double* partials = c->partials;
   int stall = stall_check ? 1 : 0;
   void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall};
-  int pers_blocks = 0, tma_blocks = 0;
-  sweep_grids<POLES>(nvec, &pers_blocks, &tma_blocks);
+  int pers_blocks = 0, tma_blocks = 0, wave_blocks = 0;
+  sweep_grids<POLES>(nvec, &pers_blocks, &tma_blocks, &wave_blocks);
+  if (form == kFormWave && wave_blocks > 0 && nvec < (1LL << 31)) {
+    int planes = wave_planes(g);
+    void* wargs[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall, &planes};
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_wave<POLES>, dim3(wave_blocks),
+                                         dim3(kPersistThreads), wargs, 0, c->stream));
+    count_launches(1);
+    return 0;
+  }
   if (form == kFormTma && tma_blocks > 0) {
     TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma<POLES>, dim3(tma_blocks), dim3(kTmaThreads),
                                          args, kTmaSmem, c->stream));
@@ -766,13 +913,16 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   bool hit_tol = false;
   bool resume = false;  // the first anchor and its first sweeps are done already
   if (fallback) *fallback = 0;
-  const SweepForm form =
-      c->opts.sweep_form == 1 ? kFormTma : (c->opts.sweep_form == 2 ? kFormSplit : kFormPersistent);
-  int pers_blocks = 0, tma_blocks = 0;
-  if (g.poles) sweep_grids<true>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
-  else sweep_grids<false>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks);
+  const SweepForm form = c->opts.sweep_form == 1   ? kFormTma
+                         : c->opts.sweep_form == 2 ? kFormSplit
+                         : c->opts.sweep_form == 3 ? kFormWave
+                                                   : kFormPersistent;
+  int pers_blocks = 0, tma_blocks = 0, wave_blocks = 0;
+  if (g.poles) sweep_grids<true>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks, &wave_blocks);
+  else sweep_grids<false>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks, &wave_blocks);
   // one launch per anchor needs a persistent kernel (it stops itself)
-  const bool one_launch = (form == kFormPersistent && pers_blocks > 0) || (form == kFormTma && tma_blocks > 0);
+  const bool one_launch = (form == kFormPersistent && pers_blocks > 0) || (form == kFormTma && tma_blocks > 0) ||
+                          (form == kFormWave && wave_blocks > 0 && g.rows * (g.nxp >> 2) < (1LL << 31));
   if (guess_test) {
     if ((rc = rhat_of_b(c, b))) return rc;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
@@ -1059,9 +1209,16 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   if ((rc = rhs_norm(c, c->d.RHS, nullptr))) return rc;
   // TTFLD_SOLVER_MIXED times the solver's kernel (one persistent launch for
   // the n sweeps); 3 the same sweeps as two launches per sweep, 4 as one
-  // launch of the TMA-staged persistent kernel.  No stall test: all n run.
-  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3 || solver == 4;
-  const SweepForm form = solver == 3 ? kFormSplit : (solver == 4 ? kFormTma : kFormPersistent);
+  // launch of the TMA-staged persistent kernel, 5 as one launch of the
+  // wavefront form with its own window size, 16 + P the wavefront with
+  // windows of P theta planes.  No stall test: all n run.
+  const bool wave = solver == 5 || solver >= 16;
+  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3 || solver == 4 || wave;
+  const SweepForm form = solver == 3 ? kFormSplit : (solver == 4 ? kFormTma : (wave ? kFormWave : kFormPersistent));
+  struct PlanesOverride {  // restored however the timing ends
+    PlanesOverride(int p) { g_wave_planes = p; }
+    ~PlanesOverride() { g_wave_planes = 0; }
+  } planes_override(solver >= 16 ? solver - 16 : 0);
   if (mixed) {
     if ((rc = ensure32(c)) || (rc = prep32(c))) return rc;
     double l1;
@@ -1089,6 +1246,6 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
 }  // namespace ttfld
 
 extern "C" int ttfld_time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
-  if (!c || !ms || solver < 0 || solver > 4) return TTFLD_E_ARGS;
+  if (!c || !ms || solver < 0 || (solver > 5 && solver < 17) || solver > 16 + 256) return TTFLD_E_ARGS;
   return ttfld::time_sweeps(c, solver, n, ms);
 }

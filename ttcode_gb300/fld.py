@@ -253,9 +253,12 @@ class FLD:
         """The cudaStream_t the library issues this context's work on."""
         return int(self.L.ttfld_stream(self.h))
 
-    def time_sweeps(self, solver: str, n: int) -> float:
+    def time_sweeps(self, solver, n: int) -> float:
+        """Mean device time of one sweep: solver is a key of TIMED_SWEEPS or
+        the ABI's code (16 + P: the wavefront form with P-plane windows)."""
+        code = solver if isinstance(solver, int) else _ffi.TIMED_SWEEPS[solver]
         ms = ctypes.c_double()
-        check("time_sweeps", self.L.ttfld_time_sweeps(self.h, _ffi.TIMED_SWEEPS[solver], n, ctypes.byref(ms)))
+        check("time_sweeps", self.L.ttfld_time_sweeps(self.h, code, n, ctypes.byref(ms)))
         return ms.value
 
     def synchronize(self):
