@@ -37,10 +37,11 @@ def _freedman_pair(sh, tab, mu=2.3):
     return o, f
 
 
-def test_freedman_kappa_and_step_match_oracle():
+@pytest.mark.parametrize("poles", [False, True])
+def test_freedman_kappa_and_step_match_oracle(poles):
     from ttcode_gb300 import opacity as O
     from ttcode_gb300.synthetic import make_shell
-    sh = make_shell(40, 64, 32, seed=8, delt=100.0)
+    sh = make_shell(40, 64, 32, seed=8, delt=100.0, poles=poles)
     o, f = _freedman_pair(sh, O.analytic_freedman_table())
     for n in ("XKAPR", "XKAPP", "XKAPA", "DXKAPP_DT", "DXKAPA_DT", "T"):
         assert rel_l2(f.download(n), o.f(n)) <= 1e-13, n
@@ -81,9 +82,10 @@ def _wave_pair(sh, nbins=30, rstar=1.155, semi=6.8e11, seed=2):
     return o, f
 
 
-def test_binned_heating_matches_oracle():
+@pytest.mark.parametrize("poles", [False, True])
+def test_binned_heating_matches_oracle(poles):
     from ttcode_gb300.synthetic import make_shell
-    sh = make_shell(40, 64, 32, seed=9, delt=100.0)
+    sh = make_shell(40, 64, 32, seed=9, delt=100.0, poles=poles)
     o, f = _wave_pair(sh)
     assert o.call("stellarinput_heating") == 0
     f.stellarinput_heating()

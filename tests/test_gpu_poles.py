@@ -78,12 +78,12 @@ def test_poles_exact_sweeps_and_solve_bitwise(polar, nsweeps):
 
 
 def test_poles_mixed_steps(polar):
-    """Two consecutive steps of the FP32/FP64 solver, the second from the
-    previous solution, against the oracle at 1e-12."""
+    """Five consecutive steps of the FP32/FP64 solver, each from the previous
+    solution, against the oracle at 1e-12."""
     o = oracle_from_shell(polar, eps=1e-12)
     f = fld_from_shell(polar)
     f.set_solver("mixed", guess="previous", tol=1e-10)
-    for step in (1, 2):
+    for step in (1, 2, 3, 4, 5):
         o.set("iii", step)
         f.set_params(iii=step)
         assert o.call("coupled_energy_eqs", 1) == 0
