@@ -467,10 +467,25 @@ __global__ void __launch_bounds__(128, 1) conv3_tc_kernel(ConvArgs a, const __gr
       const long long t = blockIdx.x + (long long)q * gridDim.x;
       if (t < ntiles) tc_issue(&tmain, &trow, a, tc_tile(a, t), stage[q], side[q], &full_bar[q]);
     }
-  for (int q = threadIdx.x; q < 27 * G * N; q += blockDim.x) {
-    const int n = q % N, g = (q / N) % G, t = q / (N * G);
-    *reinterpret_cast<uint4*>(tw + (size_t)q * 16) =
-        *reinterpret_cast<const uint4*>(a.w + ((size_t)t * N + n) * a.cin + g * 8);
+  // the weights in batches of kWBatch loads per thread before their stores,
+  // so that a thread waits one memory latency per batch, not per 16 bytes
+  constexpr int kWBatch = 4;
+  const int nw = 27 * G * N;
+  for (int q0 = threadIdx.x; q0 < nw; q0 += kWBatch * blockDim.x) {
+    uint4 v[kWBatch];
+#pragma unroll
+    for (int u = 0; u < kWBatch; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < nw) {
+        const int n = q % N, g = (q / N) % G, t = q / (N * G);
+        v[u] = *reinterpret_cast<const uint4*>(a.w + ((size_t)t * N + n) * a.cin + g * 8);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kWBatch; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < nw) *reinterpret_cast<uint4*>(tw + (size_t)q * 16) = v[u];
+    }
   }
   if (threadIdx.x < 32) {  // warp 0 owns the tensor-memory allocation
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(saddr(&tmem_base))
