@@ -318,8 +318,9 @@ def run_sweep_forms(args):
     --profile-dims (default 160,512,256), the first system of an implicit
     step, then ttfld_time_sweeps (CUDA events, 48 sweeps in one launch, the
     in-sweep norm every 8th, twice each) for the persistent kernel, the
-    TMA-staged form, two launches per sweep, and the wavefront form with its
-    own window size and with windows of 1, 2, 3, 4, 6 and 8 theta planes."""
+    neighbour-flag form, the TMA-staged form, two launches per sweep, and the
+    wavefront form with its own window size and with windows of 1, 2, 3, 4,
+    6 and 8 theta planes."""
     import torch
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
@@ -329,7 +330,8 @@ def run_sweep_forms(args):
     sh.params["epsmat"] = 1e-10
     f = start_run(sh)
     first_system(f)
-    forms = [("persistent", "mixed"), ("tma", "mixed_tma"), ("split", "mixed_split"), ("wave", "mixed_wave")]
+    forms = [("persistent", "mixed"), ("local", "mixed_local"), ("tma", "mixed_tma"), ("split", "mixed_split"),
+             ("wave", "mixed_wave")]
     forms += [(f"wave_{p}_planes", 16 + p) for p in (1, 2, 3, 4, 6, 8)]
     out = {"dims": [nx, ny, nz], "unit": "us per sweep"}
     for name, code in forms:

@@ -193,7 +193,12 @@ typedef struct {
                           2 = two launches per sweep, 3 = the sweeps in
                           pairs, each pair one wavefront over windows of
                           theta planes with a grid barrier per phase
-                          (temporal blocking through L2; the same iterate) */
+                          (temporal blocking through L2; the same iterate),
+                          4 = one persistent launch in which each block
+                          waits only for the blocks within one theta plane
+                          of its items between the colours (per-block
+                          flags; a grid barrier after norm sweeps only; the
+                          same iterate) */
 } ttfld_solve_opts;
 
 typedef struct {
@@ -435,7 +440,8 @@ int ttfld_set_freedman_table(ttfld_ctx* ctx, const ttfld_freedman_table* table);
  * solver = 3 times the same FP32 sweeps issued as two launches per sweep,
  * solver = 4 as one launch of the TMA-staged persistent kernel, solver = 5
  * as one launch of the wavefront form (sweep_form 3) with its own window
- * size and solver = 16 + P with windows of P theta planes (P = 1..256). */
+ * size, solver = 16 + P with windows of P theta planes (P = 1..256) and
+ * solver = 6 as one launch of the neighbour-flag form (sweep_form 4). */
 int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 /* Number of kernels this process has launched through libttfld. */
 uint64_t ttfld_kernel_launches(void);

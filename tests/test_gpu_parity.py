@@ -200,13 +200,13 @@ def test_diffusion_parity(small):
     assert np.array_equal(f.download("SCALAR"), o.f("SCALAR"))
 
 
-@pytest.mark.parametrize("form", ["persistent", "tma", "split", "wave"])
+@pytest.mark.parametrize("form", ["persistent", "tma", "split", "wave", "local"])
 def test_mixed_solver_multi_chunk_grid(form):
     """The FP32/FP64 solve on a 100x128x64 system with each form of its sweep
     kernel (persistent; TMA-staged, which gives each block two chunks, the
     second partial; two launches per sweep; the wavefront over theta
-    windows) against the exact FP64 SOR (the reference loop, bitwise)
-    converged to 1e-12."""
+    windows; neighbour flags between the colours) against the exact FP64
+    SOR (the reference loop, bitwise) converged to 1e-12."""
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
     sh = make_shell(100, 128, 64, seed=5, delt=100.0)
@@ -258,6 +258,40 @@ def test_wave_form_is_the_persistent_iteration(poles):
     # the timing hook runs the same sweeps with explicit window sizes
     for planes in (1, 3):
         assert f.time_sweeps(16 + planes, 16) > 0.0
+    f.close()
+
+
+@pytest.mark.parametrize("dims", [(60, 96, 40), (60, 2048, 6), (100, 256, 128)])
+@pytest.mark.parametrize("poles", [False, True])
+def test_local_form_is_the_persistent_iteration(dims, poles):
+    """The neighbour-flag form (each block waits between the colours only
+    for the blocks within one theta plane of its items) does the persistent
+    kernel's iteration: the same solution bit for bit, the same sweep and
+    anchor counts, on grids where a block waits on its nearest one to four
+    blocks and on up to 44 (more than one per lane of the polling warp),
+    with and without poles.  Three solves in a row check
+    that the flags carry from launch to launch; the timing hook runs the form
+    as one launch of 24 sweeps."""
+    from ttcode_gb300.fld import start_run
+    from ttcode_gb300.synthetic import make_shell
+    sh = make_shell(*dims, seed=9, delt=100.0, poles=poles)
+    f = start_run(sh)
+    f.set_solver("mixed", tol=1e-10)
+    f.coupled_energy_eqs(True)
+    out = {}
+    for form in ("persistent", "local"):
+        f.set_solver("mixed", tol=1e-10, sweep_form=form)
+        runs = []
+        for _ in range(3):
+            f.begin_step(new_run=True)
+            st = f.solve_system()
+            runs.append((st.status, st.sor_iter, st.corrections, f.download("DELTA_ER")))
+        out[form] = runs
+    for (sp, ip, cp, xp), (sl, il, cl, xl) in zip(out["persistent"], out["local"]):
+        assert sp == 0 and sl == 0
+        assert (il, cl) == (ip, cp), ((il, cl), (ip, cp))
+        assert np.array_equal(xl, xp)
+    assert f.time_sweeps("mixed_local", 24) > 0.0
     f.close()
 
 

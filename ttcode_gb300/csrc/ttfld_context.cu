@@ -318,7 +318,7 @@ int ttfld_set_solver(ttfld_ctx* c, const ttfld_solve_opts* o) {
   if (o->solver < 0 || o->solver > 3 || o->guess < 0 || o->guess > 2) return TTFLD_E_ARGS;
   if (o->solver == TTFLD_SOLVER_MIXED && !(o->tol > 0.0)) return TTFLD_E_ARGS;
   if (o->fallback_rule < 0 || o->fallback_rule > 3) return TTFLD_E_ARGS;
-  if (o->sweep_form < 0 || o->sweep_form > 3) return TTFLD_E_ARGS;
+  if (o->sweep_form < 0 || o->sweep_form > 4) return TTFLD_E_ARGS;
   c->opts = *o;
   if (c->opts.inner_digits <= 0) c->opts.inner_digits = 4;
   if (c->opts.inner_digits > 12) c->opts.inner_digits = 12;

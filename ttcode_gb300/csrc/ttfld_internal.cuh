@@ -38,11 +38,9 @@ struct SolverDev {
   int bar_timeout;     // 1 if a grid barrier wait ran out (the kernel gave up)
   int stalled;         // 1 if the FP32 inner loop stopped at its rounding floor
   int bad_weights;     // PCG: a row without a valid symmetrising weight
-  // grid barrier of the persistent kernels: arrivals and generation, each on
-  // a cache line of its own so that the waiters' polls of the generation do
-  // not contend with the arrivals' atomics
-  alignas(128) unsigned int bar_count;
-  alignas(128) unsigned int bar_gen;
+  // arrivals at the grid barrier of the persistent kernels (zeroed by the
+  // host before each launch), on a cache line of its own
+  alignas(128) unsigned long long arrivals;
 };
 
 // Reduction targets of the outer Newton loop.
@@ -174,39 +172,51 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* a, double 
   atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }
 
-// Grid-wide barrier of the persistent kernel (a cooperative launch, so all
-// blocks are resident).  Thread 0 of each block arrives on a counter; the
-// last arrival resets it and advances the generation the others wait on.
-// The wait is bounded: after kBarrierSpins polls (seconds of polling at an
-// L2 round trip each) or once another block has given up, the block records the
-// timeout and returns false, and the kernel returns without further work.
+// Grid-wide barrier of the persistent kernels (cooperative launches, so all
+// blocks are resident), on a monotonic 64-bit arrival counter that the host
+// zeroes before each launch: the k-th barrier of a launch is complete once
+// the counter has reached k * nblocks.  Thread 0 of each block releases the
+// block's writes (a block barrier, a fence, a release reduction) and polls
+// the counter with acquire loads, 32 ns apart, then a fence and a block
+// barrier order every thread's later loads after the other blocks' writes.
+// With no reset and no generation word, the last block to arrive adds one
+// round trip to L2 to the barrier.  `passed` counts this block's barriers
+// (the same value in every thread).  The wait is bounded: after
+// kBarrierSpins polls (seconds of polling) or once another block has given
+// up (tested every kGiveUpPolls polls, so that a poll is one load), the
+// block records the timeout and returns false, and the kernel returns
+// without further work.
 constexpr long long kBarrierSpins = 1LL << 23;
+constexpr long long kGiveUpPolls = 256;
+__device__ __forceinline__ bool give_up(long long polls, const SolverDev* sol) {
+  return polls % kGiveUpPolls == 0 && (polls > kBarrierSpins || *(volatile const int*)&sol->bar_timeout);
+}
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-
-__device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks) {
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ bool grid_sync(SolverDev* sol, unsigned int nblocks, unsigned long long& passed) {
   __shared__ int ok_sh;
   __syncthreads();
+  ++passed;
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned int g0 = ld_acquire(&sol->bar_gen);
     __threadfence();
-    if (atomicAdd(&sol->bar_count, 1u) == nblocks - 1) {
-      atomicExch(&sol->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&sol->bar_gen, 1u);
-    } else {
-      long long polls = 0;
-      while (ld_acquire(&sol->bar_gen) == g0) {
-        __nanosleep(32);
-        if (++polls > kBarrierSpins || *(volatile int*)&sol->bar_timeout) {
-          atomicExch(&sol->bar_timeout, 1);
-          ok = 0;
-          break;
-        }
+    asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(&sol->arrivals) : "memory");
+    const unsigned long long target = passed * nblocks;
+    long long polls = 0;
+    while (ld_acquire64(&sol->arrivals) < target) {
+      __nanosleep(32);
+      if (give_up(++polls, sol)) {
+        atomicExch(&sol->bar_timeout, 1);
+        ok = 0;
+        break;
       }
     }
     __threadfence();

@@ -529,20 +529,21 @@ __device__ __forceinline__ float op_one(const Kry& k, const float* po, float* pn
 // pass).  False if a barrier gave up.
 template <bool UPDATE, bool SGS>
 __device__ __forceinline__ bool precondition(const Kry& k, SolverDev* sol, unsigned int nb, long long col0,
-                                             long long colstride, float alpha, float& acc, int sweeps) {
+                                             long long colstride, float alpha, float& acc, int sweeps,
+                                             unsigned long long& passed) {
   if (!SGS) {
     for (long long c = col0; c < k.ncol; c += colstride) acc += line_pass<UPDATE>(k, c, alpha);
     return true;
   }
   const long long half = k.ncol >> 1;
   for (long long m = col0; m < half; m += colstride) (void)line_pass<UPDATE>(k, col_of(m, 0, k.ny), alpha);
-  if (!grid_sync(sol, nb)) return false;
+  if (!grid_sync(sol, nb, passed)) return false;
   float ab = 0.f;  // r.z of the black lines' first pass (their last with one sweep)
   for (long long m = col0; m < half; m += colstride) ab += line_gs<UPDATE>(k, col_of(m, 1, k.ny), alpha);
   if (sweeps == 1) acc += ab;
 #pragma unroll 1
   for (int p = 2; p <= 2 * sweeps; ++p) {
-    if (!grid_sync(sol, nb)) return false;
+    if (!grid_sync(sol, nb, passed)) return false;
     float ap = 0.f;
     for (long long m = col0; m < half; m += colstride) ap += line_gs<false>(k, col_of(m, p & 1, k.ny), 0.f);
     if (p >= 2 * sweeps - 1) acc += ap;  // the last pass of its colour
@@ -567,6 +568,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   __shared__ double sh[32];
   __shared__ double bc[3];
   const unsigned int nb = gridDim.x;
+  unsigned long long passed = 0;  // grid barriers this block has passed
   const long long n = k.n;
   const int ny = k.ny;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -581,12 +583,12 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
   // terms) are FP32 -- GB300's FP64 pipe is narrow -- and widened to FP64
   // for the block and grid sums.
   float acc = 0.f;
-  if (!precondition<false, SGS>(k, sol, nb, col0, colstride, 0.f, acc, sweeps)) return;
+  if (!precondition<false, SGS>(k, sol, nb, col0, colstride, 0.f, acc, sweeps, passed)) return;
   {
     const double v = block_sum((double)acc, sh);
     if (threadIdx.x == 0) pb[blockIdx.x] = v;
   }
-  if (!grid_sync(sol, nb)) return;
+  if (!grid_sync(sol, nb, passed)) return;
   {
     const double tot = block_sum_array(pb, nb, sh);
     if (threadIdx.x == 0) bc[0] = tot;
@@ -621,7 +623,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
       const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pa[blockIdx.x] = v;
     }
-    if (!grid_sync(sol, nb)) return;
+    if (!grid_sync(sol, nb, passed)) return;
     {
       const double tot = block_sum_array(pa, nb, sh);
       if (threadIdx.x == 0) bc[1] = tot;
@@ -638,7 +640,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     const float alpha = (float)(gamma / ps);
     // line phase: r -= alpha s, z = M^-1 r, r.z
     acc = 0.f;
-    if (!precondition<true, SGS>(k, sol, nb, col0, colstride, alpha, acc, sweeps)) return;
+    if (!precondition<true, SGS>(k, sol, nb, col0, colstride, alpha, acc, sweeps, passed)) return;
     {
       const double v = block_sum((double)acc, sh);
       if (threadIdx.x == 0) pb[blockIdx.x] = v;
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg32_persistent(Kry k, Solver
     alpha_prev = alpha;
     pending = true;
     cur = 1 - cur;  // p[cur] is now this iteration's p
-    if (!grid_sync(sol, nb)) return;
+    if (!grid_sync(sol, nb, passed)) return;
     {
       const double tot = block_sum_array(pb, nb, sh);
       if (threadIdx.x == 0) bc[2] = tot;
@@ -754,6 +756,7 @@ int launch_inner(ttfld_ctx* c, KryWork* w, int maxit, double stop_ratio, int gs,
   int sweeps = gs > 0 ? gs : 1;
   void* args[] = {&k, &sol, &partials, &maxit, &stop_ratio, &sweeps};
   const void* kern = gs > 0 ? (const void*)pcg32_persistent<true> : (const void*)pcg32_persistent<false>;
+  TT_CHECK(cudaMemsetAsync(&sol->arrivals, 0, sizeof(unsigned long long), c->stream));  // grid barrier
   TT_CHECK(cudaLaunchCooperativeKernel(kern, dim3(nb), dim3(kPcgThreads), args, 0, c->stream));
   count_launches(1);
   int rc = poll_sol(c);

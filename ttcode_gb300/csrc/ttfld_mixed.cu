@@ -61,6 +61,11 @@ struct Fast64 {
   double* x[2];     // iterate, with theta ghost planes
 };
 
+// Per-block flags of the neighbour-flag sweep form (below).
+constexpr int kFlagStride = 32;        // unsigned ints per flag: one 128-byte line per block
+constexpr int kMaxLocalBlocks = 1024;  // flags in the workspace
+constexpr size_t kFlagBytes = (size_t)kMaxLocalBlocks * kFlagStride * sizeof(unsigned int);
+
 struct MixWork {
   Cmp g;
   int have32, have64;
@@ -68,6 +73,8 @@ struct MixWork {
   void* mem64;
   Mix32 m32;
   Fast64 m64;
+  unsigned int* flags;     // per-block half-sweep counters of the neighbour-flag sweep form
+  unsigned int flag_base;  // their value when the next launch of that form starts
 };
 
 __host__ __device__ __forceinline__ size_t cslot(const Cmp& g, int j0, int k0, int h) {
@@ -90,11 +97,15 @@ static int ensure32(ttfld_ctx* c) {
   MixWork* w = work(c);
   if (w->have32) return 0;
   const Cmp& g = w->g;
-  size_t n = 2 * (6 + 3) * g.csz + 2 * g.gsz;
+  const size_t flag_floats = kFlagBytes / sizeof(float);  // the flags first: 128-byte lines
+  size_t n = flag_floats + 2 * (6 + 3) * g.csz + 2 * g.gsz;
   float* p = nullptr;
   TT_CHECK(cudaMalloc((void**)&p, n * sizeof(float)));
   TT_CHECK(cudaMemset(p, 0, n * sizeof(float)));
   w->mem32 = p;
+  w->flags = reinterpret_cast<unsigned int*>(p);
+  w->flag_base = 0;
+  p += flag_floats;
   for (int q = 0; q < 6; ++q)
     for (int col = 0; col < 2; ++col) { w->m32.a[q][col] = p; p += g.csz; }
   for (int col = 0; col < 2; ++col) { w->m32.ainv[col] = p; p += g.csz; }
@@ -293,6 +304,26 @@ __global__ void __launch_bounds__(kThreads) sweep32_kernel(Cmp g, Mix32 m, float
 // continues the same iteration.  A false alarm costs one FP64 residual.
 constexpr double kStallFactor = 0.999;
 
+// The decision after a norm sweep, taken by thread 0 of every block on the
+// same fixed-order total tot (so every block decides alike): stop at the
+// target ratio, on a non-finite norm, or (stall_check) at the FP32 rounding
+// floor.  Block 0 records it in sol; the result is 1 to stop.
+__device__ __forceinline__ int norm_stop(SolverDev* sol, double tot, double stop_ratio, int stall_check,
+                                         double& last_ratio) {
+  const double ratio = tot / sol->rhsnorm;
+  const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
+  const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
+  last_ratio = ratio;
+  if (blockIdx.x == 0) {
+    sol->rnorm = tot;
+    sol->ratio = ratio;
+    if (!isfinite(tot)) sol->nonfinite = 1;
+    if (stall) sol->stalled = 1;
+    if (stop) sol->done = 1;
+  }
+  return stop;
+}
+
 constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
 
 // nsweeps FP32 sweeps in one launch: both colours of every sweep with a grid
@@ -314,12 +345,13 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
   const unsigned int nb = gridDim.x;
   const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, ts = (long long)gridDim.x * blockDim.x;
   double last_ratio = -1.0;  // in-sweep ratio of the previous norm sweep of this launch (thread 0)
+  unsigned long long passed = 0;  // grid barriers this block has passed
   for (int sw = 1; sw <= nsweeps; ++sw) {
     const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
     float nacc = 0.f;
     if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc); }
     else { for (long long t = t0; t < n; t += ts) sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); }
-    if (!grid_sync(sol, nb)) return;
+    if (!grid_sync(sol, nb, passed)) return;
     if (norm) { for (long long t = t0; t < n; t += ts) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc); }
     else { for (long long t = t0; t < n; t += ts) sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); }
     if (norm) {
@@ -327,28 +359,139 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
       if (threadIdx.x == 0) partials[blockIdx.x] = sb;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
-    if (!grid_sync(sol, nb)) return;
+    if (!grid_sync(sol, nb, passed)) return;
     if (norm) {
       const double tot = block_sum_array(partials, nb, sh);
-      if (threadIdx.x == 0) {
-        const double ratio = tot / sol->rhsnorm;
-        // every block holds the same tot, so all reach the same decision
-        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
-        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
-        last_ratio = ratio;
-        if (blockIdx.x == 0) {
-          sol->rnorm = tot;
-          sol->ratio = ratio;
-          if (!isfinite(tot)) sol->nonfinite = 1;
-          if (stall) sol->stalled = 1;
-          if (stop) sol->done = 1;
-        }
-        stop_sh = stop;
-      }
+      if (threadIdx.x == 0) stop_sh = norm_stop(sol, tot, stop_ratio, stall_check, last_ratio);
       __syncthreads();
       if (stop_sh) return;
     }
   }
+}
+
+// ---- neighbour flags instead of grid barriers (sweep_form 4) ---------------
+// Block b owns the contiguous items [n b / nb, n (b + 1) / nb).  A
+// half-sweep of item t reads the other colour within one theta plane of t
+// only (the theta neighbours one plane away, the phi neighbours in the same
+// plane, the periodic wrap included, the r neighbours in the same row), so
+// before its h-th half-sweep a block needs only the blocks that own items
+// within one plane of its own (its neighbours) to have finished h - 1
+// half-sweeps.  Each block publishes the half-sweeps it has finished in a
+// flag of its own (a block barrier, a fence, a release store) and waits on
+// its neighbours' flags (acquire loads, a fence, a block barrier) instead of
+// on a grid barrier.  The relation is symmetric, so neighbours are never
+// more than one half-sweep apart and no block overwrites a colour that a
+// neighbour is still reading: every update reads the values it reads in the
+// grid-barrier form, whose iterate this is, bit for bit.  Norm sweeps still
+// end with a grid barrier: the stop decision needs every block's partial.
+// Flags count half-sweeps from a base that the host advances by 2 nsweeps
+// per launch, and every block leaves its flag at base + 2 nsweeps whenever
+// it returns, so all flags equal the base when the next launch starts.
+
+__device__ __forceinline__ void st_release(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The block whose items [n b / nb, n (b + 1) / nb) hold item t (0 <= t < n).
+__device__ __forceinline__ int owner_block(long long t, long long n, int nb) {
+  int b = (int)(t * nb / n);
+  while (b + 1 < nb && n * (b + 1) / nb <= t) ++b;
+  while (b > 0 && n * b / nb > t) --b;
+  return b;
+}
+
+// This block has finished v half-sweeps: after every thread's stores.
+__device__ __forceinline__ void publish_flag(unsigned int* flag, unsigned int v) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(flag, v);
+  }
+}
+
+// Wait until blocks lo..hi other than this one have finished at least
+// `target` half-sweeps; warp 0 polls, one flag per lane.  Bounded like the
+// grid barriers: false after kBarrierSpins polls or once another block has
+// given up.
+__device__ __forceinline__ bool wait_flags(const unsigned int* flags, int lo, int hi, unsigned int target,
+                                           SolverDev* sol) {
+  __shared__ int ok_sh;
+  if (threadIdx.x < 32) {
+    int ok = 1;
+    long long polls = 0;
+    for (;;) {
+      bool ready = true;
+      for (int q = lo + (int)threadIdx.x; q <= hi; q += 32)
+        if (q != (int)blockIdx.x && (int)(ld_acquire(flags + (size_t)q * kFlagStride) - target) < 0) ready = false;
+      if (__all_sync(0xffffffffu, ready)) break;
+      if (__any_sync(0xffffffffu, give_up(++polls, sol))) { ok = 0; break; }
+      __nanosleep(32);
+    }
+    __threadfence();
+    if (threadIdx.x == 0) {
+      if (!ok) atomicExch(&sol->bar_timeout, 1);
+      ok_sh = ok;
+    }
+  }
+  __syncthreads();
+  return ok_sh != 0;
+}
+
+template <bool POLES>
+__global__ void __launch_bounds__(kPersistThreads) sweeps32_local(Cmp g, Mix32 m, float omega, SolverDev* sol,
+                                                                 double* partials, double stop_ratio, int nsweeps,
+                                                                 int norm_every, int stall_check, unsigned int* flags,
+                                                                 unsigned int base) {
+  __shared__ double sh[32];
+  __shared__ int stop_sh;
+  unsigned int* own = flags + (size_t)blockIdx.x * kFlagStride;
+  const unsigned int fin = base + 2u * (unsigned int)nsweeps;
+  if (*(volatile int*)&sol->done) {  // set before the launch, so the same for every block
+    if (threadIdx.x == 0) *own = fin;
+    return;
+  }
+  const int nv = g.nxp >> 2;
+  const long long n = g.rows * nv;
+  const size_t plane = (size_t)g.ny * g.nxp;
+  const int nb = (int)gridDim.x;
+  const long long t0 = n * blockIdx.x / nb, t1 = n * (blockIdx.x + 1) / nb;
+  const long long reach = (long long)g.ny * nv;  // items within one theta plane
+  const int lo = owner_block(t0 > reach ? t0 - reach : 0, n, nb);
+  const int hi = owner_block(t1 - 1 + reach < n ? t1 - 1 + reach : n - 1, n, nb);
+  const long long ta = t0 + threadIdx.x;
+  const int bt = (int)blockDim.x;
+  double last_ratio = -1.0;
+  unsigned long long passed = 0;  // grid barriers this block has passed
+  unsigned int half = base;  // half-sweeps this block has finished
+  bool synced = true;        // every block has finished as many (launch start, grid barrier)
+  for (int sw = 1; sw <= nsweeps; ++sw) {
+    const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
+    float nacc = 0.f;
+    if (!synced && !wait_flags(flags, lo, hi, half, sol)) break;
+    if (norm) { for (long long t = ta; t < t1; t += bt) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = ta; t < t1; t += bt) sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); }
+    publish_flag(own, ++half);
+    if (!wait_flags(flags, lo, hi, half, sol)) break;
+    if (norm) { for (long long t = ta; t < t1; t += bt) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc); }
+    else { for (long long t = ta; t < t1; t += bt) sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); }
+    publish_flag(own, ++half);
+    synced = false;
+    if (norm) {
+      const double sb = block_sum((double)nacc, sh);
+      if (threadIdx.x == 0) partials[blockIdx.x] = sb;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
+    if (norm) {
+      if (!grid_sync(sol, (unsigned int)nb, passed)) break;
+      synced = true;
+      const double tot = block_sum_array(partials, nb, sh);
+      if (threadIdx.x == 0) stop_sh = norm_stop(sol, tot, stop_ratio, stall_check, last_ratio);
+      __syncthreads();
+      if (stop_sh) break;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *own = fin;
 }
 
 // ---- temporal blocking through L2 (sweep_form 3) ---------------------------
@@ -389,6 +532,7 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_wave(Cmp g, Mix32 m,
   const unsigned int nb = gridDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x, ts = gridDim.x * blockDim.x;
   double last_ratio = -1.0;
+  unsigned long long passed = 0;  // grid barriers this block has passed
   int sw = 0;
   while (sw < nsweeps) {
     const bool norm_a = norm_every > 0 && ((sw + 1) % norm_every == 0 || sw + 1 == nsweeps);
@@ -433,12 +577,12 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_wave(Cmp g, Mix32 m,
           }
           if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 2;
         }
-        if (!grid_sync(sol, nb)) return;
+        if (!grid_sync(sol, nb, passed)) return;
       }
     } else {
       if (norm) { for (int t = t0; t < n; t += ts) sweep_vec<0, true, POLES>(g, m, omega, t, nv, plane, nacc); }
       else { for (int t = t0; t < n; t += ts) sweep_vec<0, false, POLES>(g, m, omega, t, nv, plane, nacc); }
-      if (!grid_sync(sol, nb)) return;
+      if (!grid_sync(sol, nb, passed)) return;
       if (norm) { for (int t = t0; t < n; t += ts) sweep_vec<1, true, POLES>(g, m, omega, t, nv, plane, nacc); }
       else { for (int t = t0; t < n; t += ts) sweep_vec<1, false, POLES>(g, m, omega, t, nv, plane, nacc); }
       if (norm) {
@@ -446,24 +590,11 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_wave(Cmp g, Mix32 m,
         if (threadIdx.x == 0) partials[blockIdx.x] = sb;
       }
       if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
-      if (!grid_sync(sol, nb)) return;
+      if (!grid_sync(sol, nb, passed)) return;
     }
     if (norm) {  // the persistent kernel's decision, on the same kind of sum
       const double tot = block_sum_array(partials, nb, sh);
-      if (threadIdx.x == 0) {
-        const double ratio = tot / sol->rhsnorm;
-        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
-        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
-        last_ratio = ratio;
-        if (blockIdx.x == 0) {
-          sol->rnorm = tot;
-          sol->ratio = ratio;
-          if (!isfinite(tot)) sol->nonfinite = 1;
-          if (stall) sol->stalled = 1;
-          if (stop) sol->done = 1;
-        }
-        stop_sh = stop;
-      }
+      if (threadIdx.x == 0) stop_sh = norm_stop(sol, tot, stop_ratio, stall_check, last_ratio);
       __syncthreads();
       if (stop_sh) return;
     }
@@ -582,11 +713,12 @@ __global__ void __launch_bounds__(kTmaThreads) sweeps32_tma(Cmp g, Mix32 m, floa
     for (; issued < kStages && issued < total; ++issued) issue_chunk(m, pl, issued, norm_every, nsweeps, stages, bars);
   bool ok = true, synced = true;  // no barrier before the launch's first half-sweep
   double last_ratio = -1.0;       // in-sweep ratio of the previous norm sweep of this launch (thread 0)
+  unsigned long long passed = 0;  // grid barriers this block has passed
   for (int sw = 1; sw <= nsweeps && ok; ++sw) {
     const bool norm = norm_every > 0 && (sw % norm_every == 0 || sw == nsweeps);
     float nacc = 0.f;
     for (int col = 0; col < 2 && ok; ++col) {
-      if (!synced && !grid_sync(sol, nb)) { ok = false; break; }
+      if (!synced && !grid_sync(sol, nb, passed)) { ok = false; break; }
       synced = false;
       for (int k = 0; k < pl.nk; ++k) {
         const int st = (int)(done_chunks % kStages);
@@ -617,24 +749,10 @@ __global__ void __launch_bounds__(kTmaThreads) sweeps32_tma(Cmp g, Mix32 m, floa
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) sol->iter += 1;
     if (norm) {
-      if (!grid_sync(sol, nb)) { ok = false; break; }
+      if (!grid_sync(sol, nb, passed)) { ok = false; break; }
       synced = true;
       const double tot = block_sum_array(partials, nb, sh);
-      if (threadIdx.x == 0) {
-        const double ratio = tot / sol->rhsnorm;
-        // every block holds the same tot, so all reach the same decision
-        const bool stall = stall_check && last_ratio > 0.0 && !(ratio < kStallFactor * last_ratio);
-        const int stop = !isfinite(tot) || !(ratio > stop_ratio) || stall;
-        last_ratio = ratio;
-        if (blockIdx.x == 0) {
-          sol->rnorm = tot;
-          sol->ratio = ratio;
-          if (!isfinite(tot)) sol->nonfinite = 1;
-          if (stall) sol->stalled = 1;
-          if (stop) sol->done = 1;
-        }
-        stop_sh = stop;
-      }
+      if (threadIdx.x == 0) stop_sh = norm_stop(sol, tot, stop_ratio, stall_check, last_ratio);
       __syncthreads();
       if (stop_sh) break;
     }
@@ -776,7 +894,7 @@ static int persistent_grid(K kernel, int threads, size_t smem, long long items) 
   return (int)(need < coresident ? need : coresident);
 }
 
-enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2, kFormWave = 3 };
+enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2, kFormWave = 3, kFormLocal = 4 };
 
 // Theta planes per window of the wavefront form: the seven windows a pair
 // keeps in flight should take at most 60 % of L2 (40 B per cell of the FP32
@@ -795,21 +913,33 @@ static int wave_planes(const Cmp& g) {
   return p;
 }
 
-// Blocks of the two persistent kernels for nvec items (0: not available),
+// Blocks of the persistent kernels for nvec items (0: not available),
 // sized once per grid size and pole form.
+struct SweepGrids {
+  int pers, tma, wave, local;
+};
 template <bool POLES>
-static void sweep_grids(long long nvec, int* pers, int* tma, int* wave = nullptr) {
-  static int tma_blocks = -1, pers_blocks = -1, wave_blocks = -1;
+static SweepGrids sweep_grids(long long nvec) {
+  static SweepGrids gr = {-1, -1, -1, -1};
   static long long sized_for = -1;
   if (sized_for != nvec) {
-    tma_blocks = persistent_grid(sweeps32_tma<POLES>, kTmaThreads, kTmaSmem, nvec);
-    pers_blocks = persistent_grid(sweeps32_persistent<POLES>, kPersistThreads, 0, nvec);
-    wave_blocks = persistent_grid(sweeps32_wave<POLES>, kPersistThreads, 0, nvec);
+    gr.tma = persistent_grid(sweeps32_tma<POLES>, kTmaThreads, kTmaSmem, nvec);
+    gr.pers = persistent_grid(sweeps32_persistent<POLES>, kPersistThreads, 0, nvec);
+    gr.wave = nvec < (1LL << 31) ? persistent_grid(sweeps32_wave<POLES>, kPersistThreads, 0, nvec) : 0;
+    gr.local = persistent_grid(sweeps32_local<POLES>, kPersistThreads, 0, nvec);
+    if (gr.local > kMaxLocalBlocks) gr.local = 0;
     sized_for = nvec;
   }
-  if (pers) *pers = pers_blocks;
-  if (tma) *tma = tma_blocks;
-  if (wave) *wave = wave_blocks;
+  return gr;
+}
+static SweepGrids sweep_grids_of(const Cmp& g) {
+  const long long nvec = g.rows * (g.nxp >> 2);
+  return g.poles ? sweep_grids<true>(nvec) : sweep_grids<false>(nvec);
+}
+// The form runs as one launch that stops itself.
+static bool one_launch_form(const SweepGrids& gr, SweepForm form) {
+  return (form == kFormPersistent && gr.pers > 0) || (form == kFormTma && gr.tma > 0) ||
+         (form == kFormWave && gr.wave > 0) || (form == kFormLocal && gr.local > 0);
 }
 
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
@@ -831,24 +961,35 @@ static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, doubl
   double* partials = c->partials;
   int stall = stall_check ? 1 : 0;
   void* args[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall};
-  int pers_blocks = 0, tma_blocks = 0, wave_blocks = 0;
-  sweep_grids<POLES>(nvec, &pers_blocks, &tma_blocks, &wave_blocks);
-  if (form == kFormWave && wave_blocks > 0 && nvec < (1LL << 31)) {
+  const SweepGrids gr = sweep_grids<POLES>(nvec);
+  if (form != kFormSplit)  // the grid barrier counts arrivals from zero
+    TT_CHECK(cudaMemsetAsync(&sol->arrivals, 0, sizeof(unsigned long long), c->stream));
+  if (form == kFormWave && gr.wave > 0) {
     int planes = wave_planes(g);
     void* wargs[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall, &planes};
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_wave<POLES>, dim3(wave_blocks),
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_wave<POLES>, dim3(gr.wave),
                                          dim3(kPersistThreads), wargs, 0, c->stream));
     count_launches(1);
     return 0;
   }
-  if (form == kFormTma && tma_blocks > 0) {
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma<POLES>, dim3(tma_blocks), dim3(kTmaThreads),
+  if (form == kFormLocal && gr.local > 0) {
+    unsigned int* flags = w->flags;
+    unsigned int base = w->flag_base;
+    void* largs[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall, &flags, &base};
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_local<POLES>, dim3(gr.local),
+                                         dim3(kPersistThreads), largs, 0, c->stream));
+    w->flag_base = base + 2u * (unsigned int)nsweeps;  // every block leaves its flag there
+    count_launches(1);
+    return 0;
+  }
+  if (form == kFormTma && gr.tma > 0) {
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_tma<POLES>, dim3(gr.tma), dim3(kTmaThreads),
                                          args, kTmaSmem, c->stream));
     count_launches(1);
     return 0;
   }
-  if (form != kFormSplit && pers_blocks > 0) {
-    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent<POLES>, dim3(pers_blocks),
+  if (form != kFormSplit && gr.pers > 0) {
+    TT_CHECK(cudaLaunchCooperativeKernel((const void*)sweeps32_persistent<POLES>, dim3(gr.pers),
                                          dim3(kPersistThreads), args, 0, c->stream));
     count_launches(1);
     return 0;
@@ -916,13 +1057,10 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   const SweepForm form = c->opts.sweep_form == 1   ? kFormTma
                          : c->opts.sweep_form == 2 ? kFormSplit
                          : c->opts.sweep_form == 3 ? kFormWave
+                         : c->opts.sweep_form == 4 ? kFormLocal
                                                    : kFormPersistent;
-  int pers_blocks = 0, tma_blocks = 0, wave_blocks = 0;
-  if (g.poles) sweep_grids<true>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks, &wave_blocks);
-  else sweep_grids<false>(g.rows * (g.nxp >> 2), &pers_blocks, &tma_blocks, &wave_blocks);
   // one launch per anchor needs a persistent kernel (it stops itself)
-  const bool one_launch = (form == kFormPersistent && pers_blocks > 0) || (form == kFormTma && tma_blocks > 0) ||
-                          (form == kFormWave && wave_blocks > 0 && g.rows * (g.nxp >> 2) < (1LL << 31));
+  const bool one_launch = one_launch_form(sweep_grids_of(g), form);
   if (guess_test) {
     if ((rc = rhat_of_b(c, b))) return rc;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
@@ -1211,10 +1349,15 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   // the n sweeps); 3 the same sweeps as two launches per sweep, 4 as one
   // launch of the TMA-staged persistent kernel, 5 as one launch of the
   // wavefront form with its own window size, 16 + P the wavefront with
-  // windows of P theta planes.  No stall test: all n run.
+  // windows of P theta planes, 6 as one launch of the neighbour-flag form.
+  // No stall test: all n run.
   const bool wave = solver == 5 || solver >= 16;
-  const bool mixed = solver == TTFLD_SOLVER_MIXED || solver == 3 || solver == 4 || wave;
-  const SweepForm form = solver == 3 ? kFormSplit : (solver == 4 ? kFormTma : (wave ? kFormWave : kFormPersistent));
+  const bool mixed = solver == TTFLD_SOLVER_MIXED || (solver >= 3 && solver <= 6) || wave;
+  const SweepForm form = solver == 3   ? kFormSplit
+                         : solver == 4 ? kFormTma
+                         : solver == 6 ? kFormLocal
+                         : wave        ? kFormWave
+                                       : kFormPersistent;
   struct PlanesOverride {  // restored however the timing ends
     PlanesOverride(int p) { g_wave_planes = p; }
     ~PlanesOverride() { g_wave_planes = 0; }
@@ -1246,6 +1389,6 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
 }  // namespace ttfld
 
 extern "C" int ttfld_time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
-  if (!c || !ms || solver < 0 || (solver > 5 && solver < 17) || solver > 16 + 256) return TTFLD_E_ARGS;
+  if (!c || !ms || solver < 0 || (solver > 6 && solver < 17) || solver > 16 + 256) return TTFLD_E_ARGS;
   return ttfld::time_sweeps(c, solver, n, ms);
 }
