@@ -142,10 +142,10 @@ class ClockSampler:
 
 
 def load_traffic():
-    """DRAM bytes (read + write) per sweep of the persistent FP32 sweep
-    kernel, from the committed ncu summary (one full sweep is the unit of
-    `achieved`)."""
-    p = os.path.join(ROOT, "profiles", "sweeps32_persistent_shell256.md")
+    """DRAM bytes (read + write) per sweep of the FP32 sweep kernel of the
+    product path (the neighbour-flag kernel), from the committed ncu summary
+    (one full sweep is the unit of `achieved`)."""
+    p = os.path.join(ROOT, "profiles", "sweeps32_local_shell256.md")
     if os.path.exists(p):
         with open(p) as f:
             for line in f:
@@ -317,10 +317,10 @@ def run_sweep_forms(args):
     """For the sweep-form comparison under profiles/: on the shell of
     --profile-dims (default 160,512,256), the first system of an implicit
     step, then ttfld_time_sweeps (CUDA events, 48 sweeps in one launch, the
-    in-sweep norm every 8th, twice each) for the persistent kernel, the
-    neighbour-flag form, the TMA-staged form, two launches per sweep, and the
-    wavefront form with its own window size and with windows of 1, 2, 3, 4,
-    6 and 8 theta planes."""
+    in-sweep norm every 8th, twice each) for the neighbour-flag kernel (the
+    solver's), the grid-barrier kernel, the TMA-staged form, two launches per
+    sweep, and the wavefront form with its own window size and with windows
+    of 1, 2, 3, 4, 6 and 8 theta planes."""
     import torch
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
@@ -330,7 +330,7 @@ def run_sweep_forms(args):
     sh.params["epsmat"] = 1e-10
     f = start_run(sh)
     first_system(f)
-    forms = [("persistent", "mixed"), ("local", "mixed_local"), ("tma", "mixed_tma"), ("split", "mixed_split"),
+    forms = [("neighbour", "mixed"), ("grid", "mixed_grid"), ("tma", "mixed_tma"), ("split", "mixed_split"),
              ("wave", "mixed_wave")]
     forms += [(f"wave_{p}_planes", 16 + p) for p in (1, 2, 3, 4, 6, 8)]
     out = {"dims": [nx, ny, nz], "unit": "us per sweep"}
@@ -516,7 +516,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "call": "ttfld_upload x11 + ttfld_begin_step + ttfld_solve_with_sor + ttfld_download (pinned host)"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "sweeps32_persistent (one full sweep)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "sweeps32_local (one full sweep)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * ncells, "ms_per_sweep": ms_sweep32,
                      "traffic": traffic},
@@ -622,7 +622,7 @@ def big_block(name, nsteps, peak, peak_kind):
             **v, "speedup_per_step_vs_fp64_fast": v["fp64_fast"]["ms_per_step"] / v["mixed_learned"]["ms_per_step"],
             "fallback_rate": v["mixed_learned"]["fallbacks"] / max(1, nsteps),
             "solve_with_hypre": {"first": hyp[0], "second": hyp[1]},
-            "roofline": {"kernel": "sweeps32_persistent (one full sweep)", "ms_per_sweep": ms,
+            "roofline": {"kernel": "sweeps32_local (one full sweep)", "ms_per_sweep": ms,
                          "algorithmic_bytes_per_sweep": BYTES_FP32_SWEEP * nx * ny * nz, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind},
             "wall_s": round(time.perf_counter() - t0, 1)}

@@ -185,20 +185,21 @@ typedef struct {
                                 not yet removed.
                             The mixed solver runs tests 0 and 3 with its own
                             FP32 sweeps and keeps the winner's sweeps.   */
-  int32_t sweep_form;  /* mixed solver's FP32 sweep kernel: 0 = one
-                          persistent cooperative launch per FP64 anchor
-                          (default; two launches per sweep where
-                          cooperative launch is unavailable), 1 = the same
-                          with TMA-staged coefficients (slower here),
-                          2 = two launches per sweep, 3 = the sweeps in
-                          pairs, each pair one wavefront over windows of
-                          theta planes with a grid barrier per phase
-                          (temporal blocking through L2; the same iterate),
-                          4 = one persistent launch in which each block
-                          waits only for the blocks within one theta plane
-                          of its items between the colours (per-block
-                          flags; a grid barrier after norm sweeps only; the
-                          same iterate) */
+  int32_t sweep_form;  /* mixed solver's FP32 sweep kernel, every form
+                          the same iterate: 0 = (default) one persistent
+                          cooperative launch per FP64 anchor in which each
+                          block waits between the colours only for the
+                          blocks within one theta plane of its items
+                          (per-block flags; a grid barrier after norm
+                          sweeps only; two launches per sweep where
+                          cooperative launch is unavailable), 1 = a
+                          persistent launch with TMA-staged coefficients
+                          (slower here), 2 = two launches per sweep, 3 = the
+                          sweeps in pairs, each pair one wavefront over
+                          windows of theta planes with a grid barrier per
+                          phase (temporal blocking through L2), 4 = one
+                          persistent launch with a grid barrier after each
+                          colour */
 } ttfld_solve_opts;
 
 typedef struct {
@@ -436,12 +437,12 @@ int ttfld_set_freedman_table(ttfld_ctx* ctx, const ttfld_freedman_table* table);
  * SOR64_FAST / MIXED: only their private iterate is touched) and returns
  * the mean device time of one full sweep (both colours), CUDA events on the
  * library's stream.  MIXED times the solver's own kernel (all n sweeps in
- * one persistent launch, the in-sweep norm every 8th); for comparison,
+ * one launch of sweep_form 0, the in-sweep norm every 8th); for comparison,
  * solver = 3 times the same FP32 sweeps issued as two launches per sweep,
  * solver = 4 as one launch of the TMA-staged persistent kernel, solver = 5
  * as one launch of the wavefront form (sweep_form 3) with its own window
  * size, solver = 16 + P with windows of P theta planes (P = 1..256) and
- * solver = 6 as one launch of the neighbour-flag form (sweep_form 4). */
+ * solver = 6 as one launch of the grid-barrier kernel (sweep_form 4). */
 int ttfld_time_sweeps(ttfld_ctx* ctx, int solver, int n, double* ms_per_sweep);
 /* Number of kernels this process has launched through libttfld. */
 uint64_t ttfld_kernel_launches(void);

@@ -200,13 +200,14 @@ def test_diffusion_parity(small):
     assert np.array_equal(f.download("SCALAR"), o.f("SCALAR"))
 
 
-@pytest.mark.parametrize("form", ["persistent", "tma", "split", "wave", "local"])
+@pytest.mark.parametrize("form", ["neighbour", "tma", "split", "wave", "grid"])
 def test_mixed_solver_multi_chunk_grid(form):
     """The FP32/FP64 solve on a 100x128x64 system with each form of its sweep
-    kernel (persistent; TMA-staged, which gives each block two chunks, the
-    second partial; two launches per sweep; the wavefront over theta
-    windows; neighbour flags between the colours) against the exact FP64
-    SOR (the reference loop, bitwise) converged to 1e-12."""
+    kernel (neighbour flags between the colours, the default; TMA-staged,
+    which gives each block two chunks, the second partial; two launches per
+    sweep; the wavefront over theta windows; a grid barrier after each
+    colour) against the exact FP64 SOR (the reference loop, bitwise)
+    converged to 1e-12."""
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
     sh = make_shell(100, 128, 64, seed=5, delt=100.0)
@@ -232,9 +233,9 @@ def test_mixed_solver_multi_chunk_grid(form):
 
 
 @pytest.mark.parametrize("poles", [False, True])
-def test_wave_form_is_the_persistent_iteration(poles):
+def test_wave_form_is_the_default_iteration(poles):
     """The wavefront form (sweeps in pairs, each pair a wavefront over windows
-    of theta planes, window sizes 1, 3 and the default) does the persistent
+    of theta planes, window sizes 1, 3 and the default) does the default
     kernel's iteration in another order: the same sweep count, the same
     anchors and the same solution bit for bit on a 60x96x40 system, with and
     without poles."""
@@ -244,7 +245,7 @@ def test_wave_form_is_the_persistent_iteration(poles):
     f = start_run(sh)
     f.set_solver("mixed", tol=1e-10)
     f.coupled_energy_eqs(True)
-    f.set_solver("mixed", tol=1e-10, sweep_form="persistent")
+    f.set_solver("mixed", tol=1e-10, sweep_form="neighbour")
     f.begin_step(new_run=True)
     st_p = f.solve_system()
     x_p = f.download("DELTA_ER")
@@ -263,15 +264,15 @@ def test_wave_form_is_the_persistent_iteration(poles):
 
 @pytest.mark.parametrize("dims", [(60, 96, 40), (60, 2048, 6), (100, 256, 128)])
 @pytest.mark.parametrize("poles", [False, True])
-def test_local_form_is_the_persistent_iteration(dims, poles):
+def test_neighbour_form_is_the_grid_barrier_iteration(dims, poles):
     """The neighbour-flag form (each block waits between the colours only
-    for the blocks within one theta plane of its items) does the persistent
-    kernel's iteration: the same solution bit for bit, the same sweep and
-    anchor counts, on grids where a block waits on its nearest one to four
-    blocks and on up to 44 (more than one per lane of the polling warp),
-    with and without poles.  Three solves in a row check
-    that the flags carry from launch to launch; the timing hook runs the form
-    as one launch of 24 sweeps."""
+    for the blocks within one theta plane of its items; the default) does
+    the grid-barrier kernel's iteration: the same solution bit for bit, the
+    same sweep and anchor counts, on grids where a block waits on its
+    nearest one to four blocks and on up to 44 (more than one per lane of
+    the polling warp), with and without poles.  Three solves in a row check
+    that the flags carry from launch to launch; the timing hook runs both
+    forms as one launch of 24 sweeps."""
     from ttcode_gb300.fld import start_run
     from ttcode_gb300.synthetic import make_shell
     sh = make_shell(*dims, seed=9, delt=100.0, poles=poles)
@@ -279,7 +280,7 @@ def test_local_form_is_the_persistent_iteration(dims, poles):
     f.set_solver("mixed", tol=1e-10)
     f.coupled_energy_eqs(True)
     out = {}
-    for form in ("persistent", "local"):
+    for form in ("grid", "neighbour"):
         f.set_solver("mixed", tol=1e-10, sweep_form=form)
         runs = []
         for _ in range(3):
@@ -287,11 +288,11 @@ def test_local_form_is_the_persistent_iteration(dims, poles):
             st = f.solve_system()
             runs.append((st.status, st.sor_iter, st.corrections, f.download("DELTA_ER")))
         out[form] = runs
-    for (sp, ip, cp, xp), (sl, il, cl, xl) in zip(out["persistent"], out["local"]):
+    for (sp, ip, cp, xp), (sl, il, cl, xl) in zip(out["grid"], out["neighbour"]):
         assert sp == 0 and sl == 0
         assert (il, cl) == (ip, cp), ((il, cl), (ip, cp))
         assert np.array_equal(xl, xp)
-    assert f.time_sweeps("mixed_local", 24) > 0.0
+    assert f.time_sweeps("mixed_grid", 24) > 0.0 and f.time_sweeps("mixed", 24) > 0.0
     f.close()
 
 

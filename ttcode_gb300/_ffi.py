@@ -47,7 +47,7 @@ class SolveOpts(ctypes.Structure):
 
 
 FALLBACK = {"first_sweep": 0, "never": 1, "residual": 2, "four_sweeps": 3}
-SWEEP_FORM = {"persistent": 0, "tma": 1, "split": 2, "wave": 3, "local": 4}
+SWEEP_FORM = {"neighbour": 0, "tma": 1, "split": 2, "wave": 3, "grid": 4}
 
 
 class SolveStats(ctypes.Structure):
@@ -108,7 +108,7 @@ FIELDS = {
 SOLVER = {"sor64_exact": 0, "sor64_fast": 1, "mixed": 2, "pcg": 3}
 # ttfld_time_sweeps also times the per-colour launches, the TMA-staged and the
 # wavefront forms (an int 16 + P: the wavefront with windows of P theta planes)
-TIMED_SWEEPS = dict(SOLVER, mixed_split=3, mixed_tma=4, mixed_wave=5, mixed_local=6)
+TIMED_SWEEPS = dict(SOLVER, mixed_split=3, mixed_tma=4, mixed_wave=5, mixed_grid=6)
 GUESS = {"zero": 0, "previous": 1, "learned": 2}
 
 STATUS = {0: "ok", 1: "iteration limit reached", 2: "learned guess rejected",

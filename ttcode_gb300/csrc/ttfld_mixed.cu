@@ -178,7 +178,19 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 // blocks' writes, as the PTX memory model defines it.
 __device__ __forceinline__ float4 lde4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float lde(const float* p) { return *p; }
-__device__ __forceinline__ float4 ldc4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+// Loads of the coefficients (couplings, r-hat, A: 32 of the 40 bytes of a
+// cell update, each read once per sweep) do not allocate in L1, so that the
+// stream of them does not evict the lines of e that neighbouring items of
+// the same block share.  The sweep kernels never write them.  Timed against
+// plain loads on one GB300: 28.1 against 34.1 us per sweep at 160x256x128,
+// 120.9 against 129.2 us at 160x512x256, within 1 % at 100x256x128.
+__device__ __forceinline__ float4 ldc4(const float* p) {
+  float4 v;
+  asm("ld.global.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
 
 // One colour of FP32 red-black SOR on A e = r (Jacobi-scaled), 4 cells per
 // thread: res = (e + sum a_nb e_nb) - rhat (the reference's in-sweep residual
@@ -326,9 +338,10 @@ __device__ __forceinline__ int norm_stop(SolverDev* sol, double tot, double stop
 
 constexpr int kPersistThreads = 768;  // one block per SM: few barrier arrivals
 
-// nsweeps FP32 sweeps in one launch: both colours of every sweep with a grid
-// barrier after each, every norm_every-th sweep (and the last) with the
-// in-sweep norm.  Each block reduces its partial of a norm sweep; after the
+// nsweeps FP32 sweeps in one launch (sweep_form 4, and the product form's
+// stand-in where its flags do not cover the grid's blocks): both colours of
+// every sweep with a grid barrier after each, every norm_every-th sweep (and
+// the last) with the in-sweep norm.  Each block reduces its partial of a norm sweep; after the
 // barrier every block adds all partials in the same fixed order, so all of
 // them reach the same stop decision and leave the loop together.  Every
 // thread keeps the same items from sweep to sweep.
@@ -369,7 +382,7 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
   }
 }
 
-// ---- neighbour flags instead of grid barriers (sweep_form 4) ---------------
+// ---- neighbour flags instead of grid barriers (sweep_form 0, the product) ---
 // Block b owns the contiguous items [n b / nb, n (b + 1) / nb).  A
 // half-sweep of item t reads the other colour within one theta plane of t
 // only (the theta neighbours one plane away, the phi neighbours in the same
@@ -387,6 +400,10 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_persistent(Cmp g, Mi
 // Flags count half-sweeps from a base that the host advances by 2 nsweeps
 // per launch, and every block leaves its flag at base + 2 nsweeps whenever
 // it returns, so all flags equal the base when the next launch starts.
+// Timed against the grid-barrier kernel in one process on a GB300: 4-6 %
+// faster per sweep at 100x128x128, 100x256x128, 100x256x160 and
+// 160x512x256, the same at 160x256x128 and 60x512x256 (a slow block holds
+// up only its neighbours, not the grid).
 
 __device__ __forceinline__ void st_release(unsigned int* p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -894,7 +911,10 @@ static int persistent_grid(K kernel, int threads, size_t smem, long long items) 
   return (int)(need < coresident ? need : coresident);
 }
 
-enum SweepForm { kFormPersistent = 0, kFormTma = 1, kFormSplit = 2, kFormWave = 3, kFormLocal = 4 };
+// sweep_form of ttfld_solve_opts: 0 the neighbour-flag kernel (the product
+// form), 1 TMA-staged coefficients, 2 two launches per sweep, 3 the
+// wavefront, 4 the grid-barrier kernel.
+enum SweepForm { kFormNeighbour = 0, kFormTma = 1, kFormSplit = 2, kFormWave = 3, kFormGrid = 4 };
 
 // Theta planes per window of the wavefront form: the seven windows a pair
 // keeps in flight should take at most 60 % of L2 (40 B per cell of the FP32
@@ -938,17 +958,19 @@ static SweepGrids sweep_grids_of(const Cmp& g) {
 }
 // The form runs as one launch that stops itself.
 static bool one_launch_form(const SweepGrids& gr, SweepForm form) {
-  return (form == kFormPersistent && gr.pers > 0) || (form == kFormTma && gr.tma > 0) ||
-         (form == kFormWave && gr.wave > 0) || (form == kFormLocal && gr.local > 0);
+  return ((form == kFormNeighbour || form == kFormGrid) && (gr.local > 0 || gr.pers > 0)) ||
+         (form == kFormTma && gr.tma > 0) || (form == kFormWave && gr.wave > 0);
 }
 
 // Queue nsweeps FP32 sweeps; every norm_every-th one (and the last) also
 // evaluates the in-sweep norm against stop_ratio (and, with stall_check,
 // stops at the FP32 rounding floor).  The product form is one persistent
-// launch; two launches per sweep are the fallback where cooperative launch
-// is unavailable.  The TMA-staged persistent kernel is kept for comparison:
-// it is slower on this workload (the per-chunk block barriers and cache
-// latencies of e outweigh the staged coefficient traffic).
+// launch of the neighbour-flag kernel; the grid-barrier kernel takes its
+// place where the flags do not cover the grid's blocks, and two launches
+// per sweep where cooperative launch is unavailable.  The TMA-staged and
+// wavefront kernels are kept for comparison: both are slower on this
+// workload (per-chunk block barriers and cache latencies of e; a grid
+// barrier per wavefront phase).
 template <bool POLES>
 static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, double stop_ratio, SweepForm form,
                                 bool stall_check) {
@@ -972,7 +994,7 @@ static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, doubl
     count_launches(1);
     return 0;
   }
-  if (form == kFormLocal && gr.local > 0) {
+  if (form == kFormNeighbour && gr.local > 0) {
     unsigned int* flags = w->flags;
     unsigned int base = w->flag_base;
     void* largs[] = {&g, &m, &omega, &sol, &partials, &stop_ratio, &nsweeps, &norm_every, &stall, &flags, &base};
@@ -1011,7 +1033,7 @@ static int launch_sweeps32_form(ttfld_ctx* c, int nsweeps, int norm_every, doubl
 }
 
 int launch_sweeps32(ttfld_ctx* c, int nsweeps, int norm_every = 0, double stop_ratio = -1.0,
-                    SweepForm form = kFormPersistent, bool stall_check = true) {
+                    SweepForm form = kFormNeighbour, bool stall_check = true) {
   return work(c)->g.poles ? launch_sweeps32_form<true>(c, nsweeps, norm_every, stop_ratio, form, stall_check)
                           : launch_sweeps32_form<false>(c, nsweeps, norm_every, stop_ratio, form, stall_check);
 }
@@ -1057,8 +1079,8 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   const SweepForm form = c->opts.sweep_form == 1   ? kFormTma
                          : c->opts.sweep_form == 2 ? kFormSplit
                          : c->opts.sweep_form == 3 ? kFormWave
-                         : c->opts.sweep_form == 4 ? kFormLocal
-                                                   : kFormPersistent;
+                         : c->opts.sweep_form == 4 ? kFormGrid
+                                                   : kFormNeighbour;
   // one launch per anchor needs a persistent kernel (it stops itself)
   const bool one_launch = one_launch_form(sweep_grids_of(g), form);
   if (guess_test) {
@@ -1345,19 +1367,19 @@ int time_sweeps(ttfld_ctx* c, int solver, int n, double* ms) {
   if (n < 1) return TTFLD_E_ARGS;
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   if ((rc = rhs_norm(c, c->d.RHS, nullptr))) return rc;
-  // TTFLD_SOLVER_MIXED times the solver's kernel (one persistent launch for
-  // the n sweeps); 3 the same sweeps as two launches per sweep, 4 as one
-  // launch of the TMA-staged persistent kernel, 5 as one launch of the
-  // wavefront form with its own window size, 16 + P the wavefront with
-  // windows of P theta planes, 6 as one launch of the neighbour-flag form.
-  // No stall test: all n run.
+  // TTFLD_SOLVER_MIXED times the solver's kernel (one launch of the
+  // neighbour-flag kernel for the n sweeps); 3 the same sweeps as two
+  // launches per sweep, 4 as one launch of the TMA-staged persistent kernel,
+  // 5 as one launch of the wavefront form with its own window size, 16 + P
+  // the wavefront with windows of P theta planes, 6 as one launch of the
+  // grid-barrier kernel.  No stall test: all n run.
   const bool wave = solver == 5 || solver >= 16;
   const bool mixed = solver == TTFLD_SOLVER_MIXED || (solver >= 3 && solver <= 6) || wave;
   const SweepForm form = solver == 3   ? kFormSplit
                          : solver == 4 ? kFormTma
-                         : solver == 6 ? kFormLocal
+                         : solver == 6 ? kFormGrid
                          : wave        ? kFormWave
-                                       : kFormPersistent;
+                                       : kFormNeighbour;
   struct PlanesOverride {  // restored however the timing ends
     PlanesOverride(int p) { g_wave_planes = p; }
     ~PlanesOverride() { g_wave_planes = 0; }

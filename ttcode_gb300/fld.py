@@ -93,7 +93,7 @@ class FLD:
 
     def set_solver(self, solver: str = "sor64_exact", guess: str = "zero", tol: float = 1e-10,
                    inner_digits: int = 0, max_sweeps: int = 0,
-                   fallback: str = "four_sweeps", sweep_form: str = "persistent"):
+                   fallback: str = "four_sweeps", sweep_form: str = "neighbour"):
         o = _ffi.SolveOpts(SOLVER[solver], GUESS[guess], tol, inner_digits, 0, max_sweeps,
                            _ffi.FALLBACK[fallback], _ffi.SWEEP_FORM[sweep_form])
         check("ttfld_set_solver", self.L.ttfld_set_solver(self.h, ctypes.byref(o)))
