@@ -172,10 +172,10 @@ static int prep32(ttfld_ctx* c) {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 // Loads of the correction e are plain coherent loads, never the read-only
-// path: the persistent kernel writes e in one half-sweep and reads it, from
-// other SMs, in the next.  The barrier between them (a fence and an acquire
-// by one thread, then a block barrier) orders those loads after the other
-// blocks' writes, as the PTX memory model defines it.
+// path: the persistent kernels write e in one half-sweep and read it, from
+// other SMs, in the next.  The wait between them (acquire loads and a fence
+// by the polling threads, then a block barrier) orders those loads after
+// the other blocks' writes, as the PTX memory model defines it.
 __device__ __forceinline__ float4 lde4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float lde(const float* p) { return *p; }
 // Loads of the coefficients (couplings, r-hat, A: 32 of the 40 bytes of a
@@ -518,8 +518,8 @@ __global__ void __launch_bounds__(kPersistThreads) sweeps32_local(Cmp g, Mix32 m
 // with a grid barrier after every phase.  A half-sweep of plane k reads the
 // other colour at planes k-1, k and k+1 only, so a lag of two windows per
 // stage keeps every read after the write it needs and before the write that
-// replaces it: the iterate after each pair is the persistent kernel's, bit
-// for bit.  The seven windows between a window's first and last stage are
+// replaces it: the iterate after each pair is the other forms', bit for
+// bit.  The seven windows between a window's first and last stage are
 // meant to stay in L2, so that each array crosses DRAM once per pair
 // instead of once per sweep; the price is nwin + 6 grid barriers per pair
 // instead of four.  A pair whose first sweep carries the in-sweep norm, and
@@ -1042,7 +1042,7 @@ static int poll(ttfld_ctx* c) {
   TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
   TT_CHECK(cudaStreamSynchronize(c->stream));
   if (c->host_sol->bar_timeout) {
-    fprintf(stderr, "ttfld: a grid barrier of the persistent sweep kernel timed out\n");
+    fprintf(stderr, "ttfld: a wait of the persistent sweep kernel timed out\n");
     return TTFLD_E_CUDA;
   }
   return 0;
