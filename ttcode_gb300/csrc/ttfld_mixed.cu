@@ -798,6 +798,27 @@ static int add_correction(ttfld_ctx* c, double* x) {
   return 0;
 }
 
+// The same, queued behind the sweeps before their state is read back: it
+// does nothing when they made no progress (SOR_ITER still it0) or met a
+// non-finite norm, the cases in which the solve loop leaves x as it is.
+static int add_correction_unless(ttfld_ctx* c, double* x, int it0) {
+  MixWork* w = work(c);
+  Dev d = c->d;
+  Cmp g = w->g;
+  const float* e0 = w->m32.e[0];
+  const float* e1 = w->m32.e[1];
+  const SolverDev* sol = c->sol;
+  launch_box(c->stream, box(1, d.nx, 1, d.ny, 1, d.nz), [=] __device__(int i, int j, int k) {
+    if (sol->iter == it0 || sol->nonfinite) return;
+    int col = (i + j + k) & 1;
+    const float* e = col ? e1 : e0;
+    size_t q = hidx(d, i, j, k);
+    x[q] = x[q] + (double)e[gslot(g, j - 1, k - 1, (i - 1) >> 1)];
+  });
+  TT_CHECK_LAUNCH();
+  return 0;
+}
+
 // r = b - A x in FP64 (FMA), its L1 norm (fixed-order) and rhat = r/A in FP32.
 __global__ void __launch_bounds__(kThreads) resid32_kernel(Dev d, Cmp g, Mix32 m, const double* __restrict__ x,
                                                            const double* __restrict__ b, double* partials) {
@@ -844,13 +865,21 @@ __global__ void __launch_bounds__(kThreads) resid32_kernel(Dev d, Cmp g, Mix32 m
   }
 }
 
-static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
+// The FP64 anchor queued: SolverDev::true_l1 holds ||b - A x||_1 once it has
+// run (read back with the next poll).
+static int resid32_launch(ttfld_ctx* c, const double* x, const double* b) {
   MixWork* w = work(c);
   int nb = grid_for((long long)ncell(c->d));
   if (nb > kMaxPartials) nb = kMaxPartials;
   resid32_kernel<<<nb, kThreads, 0, c->stream>>>(c->d, w->g, w->m32, x, b, c->partials + kMaxPartials);
   count_launches(1);
   TT_CHECK_LAUNCH();
+  return 0;
+}
+
+static int resid32(ttfld_ctx* c, const double* x, const double* b, double* l1) {
+  int rc = resid32_launch(c, x, b);
+  if (rc) return rc;
   TT_CHECK(cudaMemcpyAsync(c->host_sol, c->sol, sizeof(SolverDev), cudaMemcpyDeviceToHost, c->stream));
   TT_CHECK(cudaStreamSynchronize(c->stream));
   *l1 = c->host_sol->true_l1;
@@ -1067,7 +1096,9 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   const Cmp& g = w->g;
   TT_CHECK(cudaMemsetAsync(c->sol, 0, sizeof(SolverDev), c->stream));
   double bl1 = 0.0, l1 = 0.0;
-  if ((rc = rhs_norm(c, b, &bl1))) return rc;
+  // ||b||_1 (SolverDev::rhsnorm, which nothing changes during the solve)
+  // comes back with the first readback below
+  if ((rc = rhs_norm(c, b, nullptr))) return rc;
   const double tol = c->opts.tol;
   const long long budget = c->opts.max_sweeps > 0 ? c->opts.max_sweeps : (long long)c->d.itmax;
   const int period = 8;
@@ -1086,10 +1117,14 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
   if (guess_test) {
     if ((rc = rhat_of_b(c, b))) return rc;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
-    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0, form)) || (rc = poll(c))) return rc;
-    const double r_zero = c->host_sol->rnorm;
+    if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0, form))) return rc;
+    // the guess's FP64 residual (and its r-hat) queued behind the sweeps from
+    // zero: one readback gives their norm, that residual and ||b||_1
     TT_CHECK(cudaMemsetAsync(&c->sol->iter, 0, sizeof(int), c->stream));
-    if ((rc = resid32(c, x, b, &l1))) return rc;
+    if ((rc = resid32_launch(c, x, b)) || (rc = poll(c))) return rc;
+    const double r_zero = c->host_sol->rnorm;
+    l1 = c->host_sol->true_l1;
+    bl1 = c->host_sol->rhsnorm;
     if (st) st->guess_resid_l1 = l1;
     TT_CHECK(cudaMemsetAsync(w->m32.e[0], 0, 2 * g.gsz * sizeof(float), c->stream));
     if ((rc = launch_sweeps32(c, guess_test, guess_test, -1.0, form)) || (rc = poll(c))) return rc;
@@ -1103,10 +1138,13 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
       if ((rc = poll(c))) return rc;
     }
   }
+  bool anchor_due = !resume;  // the residual of x is still to be formed
   for (;;) {
-    if (!resume) {
+    if (anchor_due) {
       if ((rc = resid32(c, x, b, &l1))) return rc;
+      bl1 = c->host_sol->rhsnorm;
     }
+    anchor_due = false;
     ++corrections;
     if (!isfinite(l1)) { status = TTFLD_E_NONFINITE; break; }
     if (!(l1 > tol * bl1)) break;
@@ -1125,15 +1163,20 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     bool have_norm = false;  // r_prev is an in-sweep norm (the anchor is a true residual)
     if (one_launch) {
       // the persistent kernel stops itself (target reached, FP32 floor, or
-      // the budget), so one launch per anchor and one poll suffice
+      // the budget), so one launch per anchor suffices; x += e and the next
+      // anchor's residual are queued behind it, and one readback returns
+      // the sweeps' state and that residual
       const long long left = budget - c->host_sol->iter;
       const int n = (int)(left < (1LL << 24) ? (left > 0 ? left : 1) : (1LL << 24));
-      if ((rc = launch_sweeps32(c, n, period, stop, form)) || (rc = poll(c))) return rc;
+      if ((rc = launch_sweeps32(c, n, period, stop, form)) || (rc = add_correction_unless(c, x, it0)) ||
+          (rc = resid32_launch(c, x, b)) || (rc = poll(c)))
+        return rc;
       if (c->host_sol->nonfinite) status = TTFLD_E_NONFINITE;
       if (c->host_sol->stalled) {
         ++stalls;
         TT_CHECK(cudaMemsetAsync(&c->sol->stalled, 0, sizeof(int), c->stream));
       }
+      l1 = c->host_sol->true_l1;
     }
     for (; !one_launch;) {
       if ((rc = launch_sweeps32(c, chunk, chunk <= period ? 1 : period, stop, kFormSplit))) return rc;
@@ -1160,7 +1203,10 @@ int solve_mixed(ttfld_ctx* c, double* x, const double* b, ttfld_solve_stats* st,
     }
     if (status < 0) break;
     if (c->host_sol->iter == it0) { status = TTFLD_MAXITER; break; }  // no progress possible
-    if ((rc = add_correction(c, x))) return rc;
+    if (!one_launch) {
+      if ((rc = add_correction(c, x))) return rc;
+      anchor_due = true;
+    }
   }
   if ((rc = halo_shift(c, x)) || (rc = pole_shift(c, x))) return rc;
   if (st) {
