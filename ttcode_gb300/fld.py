@@ -94,6 +94,14 @@ class FLD:
     def set_solver(self, solver: str = "sor64_exact", guess: str = "zero", tol: float = 1e-10,
                    inner_digits: int = 0, max_sweeps: int = 0,
                    fallback: str = "four_sweeps", sweep_form: str = "neighbour"):
+        """ttfld_set_solver: the solver of SOLVE_WITH_SOR's system (a key of
+        SOLVER: sor64_exact, the reference loop; sor64_fast; mixed, FP32
+        sweeps in FP64 defect correction; pcg), the initial guess (zero,
+        previous, learned), the tolerance on ||b - Ax||_1 / ||b||_1, the
+        mixed solver's inner target (0: its default of four digits) and sweep
+        budget (0: ITMAX), the guess's fallback rule (a key of FALLBACK) and
+        the mixed solver's FP32 sweep kernel (a key of SWEEP_FORM: neighbour,
+        the default; grid; split; tma; wave -- all the same iterate)."""
         o = _ffi.SolveOpts(SOLVER[solver], GUESS[guess], tol, inner_digits, 0, max_sweeps,
                            _ffi.FALLBACK[fallback], _ffi.SWEEP_FORM[sweep_form])
         check("ttfld_set_solver", self.L.ttfld_set_solver(self.h, ctypes.byref(o)))
